@@ -1,0 +1,452 @@
+"""Benchmark of the Gaussian->Fock hot path on one GB300 (or N, one process per GPU).
+
+Workload (the batched configuration the headline metric is quoted on): 4096 triples with
+D ~ U{1..4} modes, per-mode cutoff ~ U{5..40}, A = Q diag(s) Q^T (Q Haar unitary,
+s ~ U(0, 0.8)), b complex normal sigma = 0.3, c = 1, complex128, seeded per instance;
+upstream dL/dG complex normal.  One step = forward + VJP of every instance (one CUDA-graph
+replay of the ragged plan).  Synthetic data of exactly that shape; inputs (G, dL/dG: GBs)
+are far larger than L2, so no flush is needed between steps.
+
+Arms: ``--impl gb300`` (default) times the CUDA library; ``--impl reference`` times the CPU
+oracle (C restatement of the reference's numba strategies, OpenMP over instances on every
+host core) on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Fock amplitudes/s fwd+VJP (c128, <=1e-12 rel) batched vs plain, 1 GB300"
+UNIT = "amplitudes/s"
+N_INST = 4096
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(base_seed: int, n: int = N_INST):
+    """Per-instance seeded triples: (shapes, As, bs, cs)."""
+    from scipy.stats import unitary_group
+
+    shapes, As, bs = [], [], []
+    for k in range(n):
+        rng = np.random.default_rng(base_seed + k)
+        D = int(rng.integers(1, 5))
+        shape = tuple(int(x) for x in rng.integers(5, 41, D))
+        if D == 1:
+            Q = np.exp(1j * rng.uniform(0, 2 * np.pi, (1, 1)))
+        else:
+            Q = unitary_group.rvs(D, random_state=rng)
+        s = rng.uniform(0.0, 0.8, D)
+        A = (Q * s) @ Q.T
+        b = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+        shapes.append(shape)
+        As.append(A.astype(np.complex128))
+        bs.append(b.astype(np.complex128))
+    cs = np.ones(n, np.complex128)
+    return shapes, As, bs, cs
+
+
+def fp64_ops(shape):
+    """FP64 pipe instructions (DFMA/DMUL each 1) of the forward and the VJP kernels for one shape."""
+    C = np.array(shape, np.float64)
+    n = float(np.prod(C))
+    D = len(shape)
+    fwd = 0.0
+    for i in range(D):
+        inner = float(np.prod(C[i + 1:]))
+        lvl = (C[i] - 1) * inner
+        fwd += 6 * lvl + 4 * max(C[i] - 2, 0) * inner
+        for j in range(i + 1, D):
+            fwd += 4 * (C[i] - 1) * (C[j] - 1) * inner / C[j]
+    N1 = lambda i: n * (C[i] - 1) / C[i]  # noqa: E731
+    N2 = lambda i: n * max(C[i] - 2, 0) / C[i]  # noqa: E731
+    N11 = lambda i, j: n * (C[i] - 1) * (C[j] - 1) / (C[i] * C[j])  # noqa: E731
+    vjp = 4 * n + 6 * N1(0) + 6 * N2(0) + sum(4 * N11(0, j) for j in range(1, D))
+    for i in range(1, D):
+        vjp += 4 * N1(i) + 4 * N2(i) + sum(4 * N11(i, j) for j in range(i + 1, D))
+    return fwd, vjp
+
+
+# ------------------------------------------------------------------ helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        loaded = sorted(sm)[len(sm) // 4:] if len(sm) > 4 else sm  # ignore the ramp at the start
+        return {"sm_mhz": float(np.median(loaded)) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import oracle
+
+    oracle.build()
+    shapes, As, bs, cs = make_workload(20260000)
+    rh = oracle.RaggedHost(shapes)
+    A = np.concatenate([a.ravel() for a in As])
+    b = np.concatenate(bs)
+    rng = np.random.default_rng(7)
+    g = (rng.standard_normal(rh.total) + 1j * rng.standard_normal(rh.total)).astype(np.complex128)
+    G = np.empty(rh.total, np.complex128)
+
+    # bounded sample: a fixed subset of instances (cost-weighted stride) so a step takes a few seconds
+    t0 = time.perf_counter()
+    oracle.fwd_ragged(rh, A, b, cs, out=G)
+    oracle.vjp_ragged(rh, G, cs, g)
+    full_s = time.perf_counter() - t0
+    frac = min(1.0, 4.0 / full_s) if full_s > 0 else 1.0
+    idx = rh.order[:: max(1, int(round(1 / frac)))] if frac < 1 else rh.order
+    amps = int(rh.sizes[idx].sum())
+    for _ in range(args.warmup):
+        oracle.fwd_ragged(rh, A, b, cs, out=G, indices=idx)
+        oracle.vjp_ragged(rh, G, cs, g, indices=idx)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.fwd_ragged(rh, A, b, cs, out=G, indices=idx)
+        oracle.vjp_ragged(rh, G, cs, g, indices=idx)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    value = amps / t
+    sample = (f"{len(idx)} of {N_INST} instances ({amps} of {rh.total} amplitudes), fwd+VJP per step"
+              if len(idx) < N_INST else f"all {N_INST} instances ({amps} amplitudes), fwd+VJP per step")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": "ragged batch: 4096 triples, D~U{1..4}, cutoff~U{5..40}, Takagi A s~U(0,0.8), "
+                               "b sigma 0.3, c=1, fwd+VJP", "instances": N_INST, "amplitudes": int(rh.total)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GB300 arm
+def run_gb300(args, rank, local_rank, world):
+    import torch
+
+    import mrmustard_gb300 as mm
+    from mrmustard_gb300 import _lib
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+
+    # --- workload (weak scaling: every rank its own 4096 triples)
+    shapes, As, bs, cs = make_workload(20260000 + rank * N_INST)
+    rb = mm.RaggedBatch(shapes, device=dev)
+    A, b, c = rb.pack(As, bs, cs)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7 + rank)
+    g = torch.complex(torch.randn(rb.total, generator=gen, device=dev, dtype=torch.float64),
+                      torch.randn(rb.total, generator=gen, device=dev, dtype=torch.float64))
+    total = rb.total
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    # --- correctness gate on a few instances (largest D=4 ones and random others) vs the oracle
+    with mm.settings(CHECK_DEVICE_STATUS=True):
+        G_chk = rb.forward(A, b, c)
+        dA_chk, db_chk, dc_chk = rb.vjp(G_chk, c, g)
+    max_err = 0.0
+    if rank == 0:
+        import oracle
+
+        oracle.build()
+        pick = list(rb_order_largest(rb, 3)) + list(np.random.default_rng(3).choice(len(shapes), 5, replace=False))
+        Gh = G_chk.cpu().numpy()
+        gh = g.cpu().numpy()
+        dAh, dbh, dch = dA_chk.cpu().numpy(), db_chk.cpu().numpy(), dc_chk.cpu().numpy()
+        for k in pick:
+            o, n, sh = rb.g_off[k], rb.sizes[k], shapes[k]
+            ref = oracle.vanilla(sh, As[k], bs[k], cs[k])
+            max_err = max(max_err, oracle.rel_err(Gh[o:o + n].reshape(sh), ref))
+            rA, rbb, rc = oracle.vjp(ref, cs[k], gh[o:o + n].reshape(sh))
+            D = len(sh)
+            max_err = max(max_err, oracle.rel_err(dAh[rb.a_off[k]:rb.a_off[k] + D * D].reshape(D, D), rA))
+            max_err = max(max_err, oracle.rel_err(dbh[rb.b_off[k]:rb.b_off[k] + D], rbb))
+        del Gh, gh
+    del G_chk
+
+    # --- one CUDA graph: forward + VJP of every instance
+    n_before = int(lib.mm_launch_count())
+    graph, G, grads = rb.capture(A, b, c, g, warmup=1)
+    # rb.capture runs forward + VJP once eagerly (warm-up) and once under capture
+    launches_per_step = (int(lib.mm_launch_count()) - n_before) // 2
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            graph.replay()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if pg is not None:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = total * world / (ms * 1e-3)
+    clocks = clk.summary()
+
+    # --- device status after the timed region
+    rb.ws.check_status("timed region")
+
+    # --- per-kernel timing (eager, same stream) for the roofline
+    def time_eager(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        t_fwd = time_eager(lambda: rb.forward(A, b, c, out=G))
+        t_vjp = time_eager(lambda: rb.vjp(G, c, g, out=grads))
+    fwd_ops = vjp_ops = 0.0
+    for sh in shapes:
+        f_, v_ = fp64_ops(sh)
+        fwd_ops += f_
+        vjp_ops += v_
+
+    # FP64 pipe peak (DFMA instructions/s) from the probe
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = sms * 8, 4096
+    probe_out = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
+
+    def probe():
+        _lib.check(lib.mm_probe_dfma(probe_out.data_ptr(), blocks, iters, stream.cuda_stream), "mm_probe_dfma")
+
+    t_probe = time_eager(probe, reps=5)
+    dfma_peak = 8.0 * iters * blocks * 256 / (t_probe * 1e-3)
+
+    hbm_peak, peak_kind = measured_peaks()
+    if t_vjp >= t_fwd:
+        dom, t_dom, bytes_dom, ops_dom = "vjp_items_kernel", t_vjp, 32.0 * total, vjp_ops
+    else:
+        dom, t_dom, bytes_dom, ops_dom = "fwd_cta_kernel", t_fwd, 16.0 * total, fwd_ops
+    achieved_gbs = bytes_dom / (t_dom * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get(dom)
+
+    # --- e2e through the public API with pinned host buffers
+    A_h = A.cpu().pin_memory()
+    b_h = b.cpu().pin_memory()
+    c_h = c.cpu().pin_memory()
+    g_h = g.cpu().pin_memory()
+    G_h = torch.empty(total, dtype=torch.complex128).pin_memory()
+    dA_h = torch.empty(rb.n_a, dtype=torch.complex128).pin_memory()
+    db_h = torch.empty(rb.n_b, dtype=torch.complex128).pin_memory()
+    dc_h = torch.empty(rb.B, dtype=torch.complex128).pin_memory()
+    h2d = sum(t.numel() * 16 for t in (A_h, b_h, c_h, g_h))
+    d2h = sum(t.numel() * 16 for t in (G_h, dA_h, db_h, dc_h))
+
+    def e2e_step():
+        A.copy_(A_h, non_blocking=True)
+        b.copy_(b_h, non_blocking=True)
+        c.copy_(c_h, non_blocking=True)
+        g.copy_(g_h, non_blocking=True)
+        rb.forward(A, b, c, out=G)
+        rb.vjp(G, c, g, out=grads)
+        G_h.copy_(G, non_blocking=True)
+        dA_h.copy_(grads[0], non_blocking=True)
+        db_h.copy_(grads[1], non_blocking=True)
+        dc_h.copy_(grads[2], non_blocking=True)
+
+    e2e_steps = max(2, min(args.steps, 5))
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    rb.ws.check_status("e2e")
+
+    # --- plain per-instance GPU path on a sample of instances (scaled to amplitudes/s)
+    rng = np.random.default_rng(11)
+    sample = rng.choice(len(shapes), 256, replace=False)
+    dev_inputs = [(torch.as_tensor(As[k], device=dev), torch.as_tensor(bs[k], device=dev),
+                   torch.tensor(cs[k], device=dev), g[rb.g_off[k]:rb.g_off[k] + rb.sizes[k]].reshape(shapes[k]))
+                  for k in sample]
+    amps_sample = int(rb.sizes[sample].sum())
+
+    def plain():
+        for (Ak, bk, ck, gk), k in zip(dev_inputs, sample):
+            Gk = mm.device_fwd(Ak, bk, ck, shapes[k])
+            mm.device_vjp(Gk, ck, gk, batched=False)
+
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        t_plain = time_eager(plain, reps=2)
+    plain_value = amps_sample / (t_plain * 1e-3)
+
+    # --- CPU baseline: the oracle (C port) on the host cores, full workload, one pass
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        import oracle
+
+        rh = oracle.RaggedHost(shapes)
+        A_np = np.concatenate([a.ravel() for a in As])
+        b_np = np.concatenate(bs)
+        g_np = g_h.numpy()
+        G_np = np.empty(total, np.complex128)
+        t0 = time.perf_counter()
+        oracle.fwd_ragged(rh, A_np, b_np, cs, out=G_np)
+        oracle.vjp_ragged(rh, G_np, cs, g_np)
+        tc = time.perf_counter() - t0
+        cpu = {"value": total / tc, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"all {N_INST} instances ({total} amplitudes), one fwd+VJP pass, {tc:.2f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "ragged batch: 4096 triples, D~U{1..4}, cutoff~U{5..40}, Takagi A s~U(0,0.8), "
+                                   "b sigma 0.3, c=1, fwd+VJP (one CUDA graph replay per step)",
+                       "instances": N_INST, "amplitudes": total, "l2": "inputs larger than L2 (G, dLdG ~4.4 GB each)",
+                       "parallelism": f"replicas x{world} (instances independent)"},
+            "e2e": {"value": total * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": bytes_dom, "ms_per_launch": t_dom,
+                         "fp64": {"achieved_dfma_per_s": ops_dom / (t_dom * 1e-3), "peak_dfma_per_s": dfma_peak,
+                                  "frac": ops_dom / (t_dom * 1e-3) / dfma_peak,
+                                  "peak_kind": "measured (mm_probe_dfma)"}},
+            "kernels_ms": {"forward": t_fwd, "vjp": t_vjp},
+            "plain_loop": {"value": plain_value, "unit": UNIT, "sample": f"{len(sample)} instances, "
+                           "device_fwd + device_vjp per instance", "batched_over_plain": value / world / plain_value},
+            "max_rel_err_vs_oracle": max_err,
+            "clocks": clocks,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def rb_order_largest(rb, n):
+    return list(np.argsort(-rb.sizes, kind="stable")[:n])
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-oracle baseline leg")
+    args = ap.parse_args(argv)
+    args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
+    rank, local_rank, world = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gb300(args, rank, local_rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,183 @@
+/*
+ * mm_gb300.h -- C ABI of the GB300-native Gaussian->Fock hot path.
+ *
+ * The library computes MrMustard's renormalised multidimensional Hermite
+ * recurrence (Bargmann triple (A, b, c) -> Fock amplitudes G, complex128,
+ * row-major), its closed-form vector-Jacobian product, and the Fock-space
+ * contraction that follows it, with hand-written sm_103a CUDA kernels.
+ *
+ * Conventions (every entry point):
+ *  - complex128 values are mm_c128 {re, im}: the layout of numpy complex128,
+ *    C99 double _Complex and std::complex<double>.
+ *  - Arrays named A, b, c, G, dLdG, dA, db, dc, U, X, Y are DEVICE pointers;
+ *    `shape`, `D`, `shapes` are HOST arrays.  Tensors are C-contiguous.
+ *  - Calls are asynchronous on `stream` (a cudaStream_t; NULL = legacy default).
+ *  - `ws` is caller-owned device scratch of at least the size the matching
+ *    *_workspace_bytes query returns, 256-byte aligned.  Its first 4 bytes
+ *    are a sticky device status word: kernels that give up a bounded wait
+ *    record MM_ERR_WAIT_TIMEOUT there.  Zero it once with mm_workspace_init and
+ *    read it with mm_workspace_status.
+ *  - Return value: MM_OK or an mm_status code; nothing aborts or traps.
+ *  - There is no CPU fallback: without a CUDA device every compute entry
+ *    point returns MM_ERR_NO_DEVICE.
+ */
+#ifndef MM_GB300_H
+#define MM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MM_API __attribute__((visibility("default")))
+#else
+#define MM_API
+#endif
+
+typedef struct {
+  double re, im;
+} mm_c128;
+
+typedef struct CUstream_st *mm_stream_t; /* identical to cudaStream_t */
+
+enum mm_status {
+  MM_OK = 0,
+  MM_ERR_INVALID_ARG = 1,   /* bad pointer, shape entry < 1, D < 1, ... */
+  MM_ERR_UNSUPPORTED = 2,   /* D > mm_max_modes() */
+  MM_ERR_TOO_LARGE = 3,     /* a slab of the recurrence exceeds 2^31 - 1 amplitudes */
+  MM_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+  MM_ERR_WAIT_TIMEOUT = 5,  /* a bounded inter-CTA wait gave up (device status word) */
+  MM_ERR_WORKSPACE = 6,     /* workspace missing, misaligned or too small */
+  MM_ERR_NO_DEVICE = 7      /* no CUDA device */
+};
+
+/* Human-readable text of a status code (static storage). */
+MM_API const char *mm_status_string(int status);
+/* Largest number of modes (tensor rank) an instance may have. */
+MM_API int mm_max_modes(void);
+/* Text of the last CUDA error seen by this thread (static storage, "" if none). */
+MM_API const char *mm_last_cuda_error(void);
+
+/* Zero the workspace status word (async on stream). */
+MM_API int mm_workspace_init(void *ws, size_t ws_bytes, mm_stream_t stream);
+/* Synchronise `stream`, read the workspace status word into *status and clear it. */
+MM_API int mm_workspace_status(void *ws, mm_stream_t stream, int *status);
+
+/* ------------------------------------------------------------------ forward */
+
+/*
+ * Workspace bytes for mm_hermite_fwd / _batched / mm_hermite_vjp / _batched
+ * on `batch` instances of one shape (batch = 1 for the unbatched calls).
+ */
+MM_API size_t mm_hermite_workspace_bytes(int D, const int64_t *shape, int64_t batch);
+
+/*
+ * G = vanilla_numba(shape, A, b, c)            (stable = 0)
+ * G = stable_numba(shape, A, b, c)             (stable != 0)
+ * Replaces mrmustard/math/lattice/strategies/vanilla/core.py:25-124 (vanilla_numba)
+ * and core.py:127-213 (stable_numba), reached from
+ * mrmustard/math/backend_numpy.py:381-392 (BackendNumpy.hermite_renormalized).
+ * A: D x D row-major, b: D, c: 1 element, G: prod(shape) elements (every one written).
+ */
+MM_API int mm_hermite_fwd(int D, const int64_t *shape, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c, int stable,
+                   mm_c128 *G, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/*
+ * G[k] = vanilla_numba / stable_numba(shape, A[k], b[k], c[k]) for k < B.
+ * Replaces mrmustard/math/lattice/strategies/vanilla/batch.py:27-61 (vanilla_batch_numba),
+ * reached from mrmustard/math/backend_numpy.py:394-403 (hermite_renormalized_batched).
+ * A: B x D x D, b: B x D, c: B, G: B x prod(shape).
+ */
+MM_API int mm_hermite_fwd_batched(int64_t B, int D, const int64_t *shape, const mm_c128 *A, const mm_c128 *b,
+                           const mm_c128 *c, int stable, mm_c128 *G, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/* ---------------------------------------------------------------------- VJP */
+
+/*
+ * (dA, db, dc) = vanilla_vjp_numba(G, c, dLdG): holomorphic VJP (no conjugation),
+ * dA symmetrised as (dLdA + dLdA^T) / 2.
+ * Replaces mrmustard/math/lattice/strategies/vanilla/gradients.py:25-82, reached from
+ * mrmustard/math/jax_vjps/hermite.py:86-102 (hermite_renormalized_jax_bwd).
+ * dA: D x D, db: D, dc: 1.
+ */
+MM_API int mm_hermite_vjp(int D, const int64_t *shape, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG, mm_c128 *dA,
+                   mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/*
+ * Batched VJP over B instances of one shape.
+ * Replaces mrmustard/math/lattice/strategies/vanilla/gradients.py:85-116
+ * (vanilla_batch_vjp_numba), reached from mrmustard/math/jax_vjps/hermite.py:158-175.
+ * dA: B x D x D, db: B x D, dc: B.
+ */
+MM_API int mm_hermite_vjp_batched(int64_t B, int D, const int64_t *shape, const mm_c128 *G, const mm_c128 *c,
+                           const mm_c128 *dLdG, mm_c128 *dA, mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes,
+                           mm_stream_t stream);
+
+/* ------------------------------------------------------------ ragged batches */
+
+/*
+ * A ragged batch holds B instances with their own mode count D[k] and shape
+ * (shapes[] concatenates the B shapes).  The reference has no ragged entry
+ * point: its batch API (batch.py:27-61, backend_manager.py:683-720) needs one
+ * shape, so a ragged batch there is a Python loop of vanilla_numba /
+ * vanilla_vjp_numba calls; these entry points replace that loop with
+ * persistent launches over a cost-sorted work queue.
+ *
+ * Packing (host offsets from mm_ragged_plan_offsets): instance k's tensor G_k
+ * starts at element g_off[k] of G (and of dLdG), A_k at element a_off[k] of A
+ * (D_k^2 entries), b_k at b_off[k] of b (D_k entries), c_k = c[k]; dA/db use
+ * the a_off/b_off packing, dc[k] is one element per instance.
+ */
+typedef struct mm_ragged_plan mm_ragged_plan;
+
+MM_API int mm_ragged_plan_create(int64_t B, const int32_t *D, const int64_t *shapes, mm_ragged_plan **plan);
+MM_API void mm_ragged_plan_destroy(mm_ragged_plan *plan);
+MM_API size_t mm_ragged_plan_workspace_bytes(const mm_ragged_plan *plan);
+MM_API int64_t mm_ragged_plan_amplitudes(const mm_ragged_plan *plan);
+/* Host arrays of B entries each (any may be NULL). */
+MM_API int mm_ragged_plan_offsets(const mm_ragged_plan *plan, int64_t *g_off, int64_t *a_off, int64_t *b_off);
+/*
+ * Tuning knobs of the plan (set before mm_ragged_plan_upload):
+ *   team_min_amps:  instances with at least this many amplitudes run their forward on a
+ *                   cluster of CTAs instead of one CTA (0 = never);
+ *   vjp_item_amps:  target amplitudes per VJP work item.
+ */
+MM_API int mm_ragged_plan_set_tuning(mm_ragged_plan *plan, int64_t team_min_amps, int64_t vjp_item_amps);
+/* Copy the plan's descriptors and work queues into ws (blocks the host until copied). */
+MM_API int mm_ragged_plan_upload(const mm_ragged_plan *plan, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/* Forward of every instance of an uploaded plan (vanilla or stable). */
+MM_API int mm_ragged_fwd(const mm_ragged_plan *plan, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c, int stable,
+                  mm_c128 *G, void *ws, size_t ws_bytes, mm_stream_t stream);
+/* VJP of every instance of an uploaded plan. */
+MM_API int mm_ragged_vjp(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG, mm_c128 *dA,
+                  mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/* ------------------------------------------------------------- diagnostics */
+
+/*
+ * Launch a two-CTA cooperative kernel whose grid barrier can never complete,
+ * so that its bounded wait gives up after budget_ns and records
+ * MM_ERR_WAIT_TIMEOUT in the workspace status word.  Used by the tests of the
+ * timeout path; no GPU fault is involved.
+ */
+MM_API int mm_test_wait_timeout(void *ws, size_t ws_bytes, uint64_t budget_ns, mm_stream_t stream);
+
+/*
+ * FP64 pipe probe: `blocks` CTAs of 256 threads, each thread running 8 independent
+ * DFMA chains of `iters` steps (2 * 8 * iters * blocks * 256 FLOP per launch); `out`
+ * receives blocks * 256 doubles.  Gives the measured FP64 peak that the recurrence's
+ * FP64 roofline is quoted against (no counterpart in the reference).
+ */
+MM_API int mm_probe_dfma(double *out, int blocks, int iters, mm_stream_t stream);
+
+/* Number of kernel launches issued by this library since load (all threads). */
+MM_API int64_t mm_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MM_GB300_H */

@@ -1,0 +1,65 @@
+"""GB300-native Gaussian->Fock hot path of MrMustard.
+
+The renormalised multidimensional Hermite recurrence (``vanilla`` / ``stable`` /
+batched / VJP) and the Fock contraction after it, computed by hand-written sm_103a CUDA
+kernels in ``libmm_gb300.so`` behind a C ABI (include/mm_gb300.h).  The Python layer mirrors
+the reference's interface for this path; it has no CPU compute path.
+"""
+
+from __future__ import annotations
+
+from ._build_ext import build as build_library
+from .autograd import HermiteRenormalizedFn, hermite_renormalized_autograd
+from .backend import BackendGB300
+from .hermite import (
+    device_fwd,
+    device_vjp,
+    hermite_renormalized,
+    hermite_renormalized_batched,
+    stable,
+    stable_numba,
+    vanilla,
+    vanilla_batch,
+    vanilla_batch_numba,
+    vanilla_batch_vjp,
+    vanilla_batch_vjp_numba,
+    vanilla_numba,
+    vanilla_vjp,
+    vanilla_vjp_numba,
+)
+from .ragged import RaggedBatch
+from .settings import settings
+
+__version__ = "0.1.0"
+
+
+def launch_count() -> int:
+    """Kernel launches issued by libmm_gb300 in this process."""
+    from . import _lib
+
+    return int(_lib.load().mm_launch_count())
+
+
+__all__ = [
+    "BackendGB300",
+    "HermiteRenormalizedFn",
+    "RaggedBatch",
+    "build_library",
+    "device_fwd",
+    "device_vjp",
+    "hermite_renormalized",
+    "hermite_renormalized_autograd",
+    "hermite_renormalized_batched",
+    "launch_count",
+    "settings",
+    "stable",
+    "stable_numba",
+    "vanilla",
+    "vanilla_batch",
+    "vanilla_batch_numba",
+    "vanilla_batch_vjp",
+    "vanilla_batch_vjp_numba",
+    "vanilla_numba",
+    "vanilla_vjp",
+    "vanilla_vjp_numba",
+]

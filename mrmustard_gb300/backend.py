@@ -1,0 +1,25 @@
+"""Backend object with the reference's plug-in interface for this path.
+
+MrMustard dispatches ``math.hermite_renormalized`` by name to the active backend
+(``BackendManager._apply``, mrmustard/math/backend_manager.py:89-116), which for the numpy
+backend calls ``hermite_renormalized`` / ``hermite_renormalized_batched``
+(mrmustard/math/backend_numpy.py:381-403).  ``BackendGB300`` provides those two methods with the
+same signatures; a maintainer mixes it into the numpy backend so every
+other op keeps its numpy implementation.
+"""
+
+from __future__ import annotations
+
+from .hermite import stable_numba, vanilla_batch_numba, vanilla_numba
+
+
+class BackendGB300:
+    name = "gb300"
+
+    def hermite_renormalized(self, A, b, c, shape, stable=False, out=None):
+        if stable:
+            return stable_numba(tuple(shape), A, b, c, out)
+        return vanilla_numba(tuple(shape), A, b, c, out)
+
+    def hermite_renormalized_batched(self, A, b, c, shape, stable=False, out=None):
+        return vanilla_batch_numba(tuple(shape), A, b, c, stable, out)

@@ -1,0 +1,612 @@
+// C ABI of the GB300 Hermite library: argument checks, workspace layout,
+// ragged-batch planning and kernel launches.  See include/mm_gb300.h.
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "kernels.cuh"
+
+using namespace mm;
+
+namespace {
+
+thread_local char g_last_cuda_error[256] = "";
+std::atomic<int64_t> g_launches{0};
+
+constexpr int64_t kGridMinAmps = 8192;     // single instances at least this large use the whole grid
+constexpr uint32_t kSmallChunk = 256;      // grid kernel: chunks smaller than this run on CTA 0
+constexpr int kGridBlock = 512;            // threads per CTA of the cooperative grid kernel
+constexpr int64_t kVjpItemAmps = 65536;    // default amplitudes per VJP work item
+constexpr size_t kAlign = 256;
+
+int cuda_fail(cudaError_t e) {
+  snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+  return MM_ERR_CUDA;
+}
+#define MM_CUDA(call)                        \
+  do {                                       \
+    cudaError_t _e = (call);                 \
+    if (_e != cudaSuccess) return cuda_fail(_e); \
+  } while (0)
+#define MM_LAUNCHED()                            \
+  do {                                           \
+    g_launches.fetch_add(1);                     \
+    cudaError_t _e = cudaGetLastError();         \
+    if (_e != cudaSuccess) return cuda_fail(_e); \
+  } while (0)
+
+uint64_t wait_budget_ns() {
+  static uint64_t v = [] {
+    const char* s = getenv("MM_WAIT_BUDGET_NS");
+    return s ? strtoull(s, nullptr, 10) : 2000000000ull;
+  }();
+  return v;
+}
+
+struct DevInfo {
+  int sms = 0;
+  int coop = 0;
+};
+
+int device_info(DevInfo& di) {
+  static std::mutex mu;
+  static DevInfo cache[64];
+  static bool have[64] = {};
+  int dev = 0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return MM_ERR_NO_DEVICE;
+  }
+  MM_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 64 && have[dev]) {
+    di = cache[dev];
+    return MM_OK;
+  }
+  MM_CUDA(cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev));
+  MM_CUDA(cudaDeviceGetAttribute(&di.coop, cudaDevAttrCooperativeLaunch, dev));
+  if (dev < 64) {
+    cache[dev] = di;
+    have[dev] = true;
+  }
+  return MM_OK;
+}
+
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Fill a Geom from D and a host shape; checks every limit of the kernels.
+int make_geom(int D, const int64_t* shape, Geom& g) {
+  if (D < 1 || shape == nullptr) return MM_ERR_INVALID_ARG;
+  if (D > MM_MAXD) return MM_ERR_UNSUPPORTED;
+  memset(&g, 0, sizeof(g));
+  g.D = D;
+  int64_t n = 1, sumC = 0;
+  int32_t maxC = 0;
+  for (int i = 0; i < D; ++i) {
+    if (shape[i] < 1) return MM_ERR_INVALID_ARG;
+    if (shape[i] > (int64_t)INT32_MAX / 2) return MM_ERR_TOO_LARGE;
+    if (n > ((int64_t)1 << 62) / shape[i]) return MM_ERR_TOO_LARGE;
+    n *= shape[i];
+    g.shape[i] = shape[i];
+    g.prefC[i] = (int32_t)sumC;
+    sumC += shape[i];
+    maxC = std::max<int32_t>(maxC, (int32_t)shape[i]);
+  }
+  if (sumC > (int64_t)INT32_MAX / 2) return MM_ERR_TOO_LARGE;
+  g.strides[D - 1] = 1;
+  for (int i = D - 1; i > 0; --i) g.strides[i - 1] = g.strides[i] * g.shape[i];
+  // chunk / fiber / prefix indices are 32-bit
+  if (g.strides[0] > (int64_t)INT32_MAX) return MM_ERR_TOO_LARGE;
+  if (n / g.shape[D - 1] > (int64_t)INT32_MAX) return MM_ERR_TOO_LARGE;
+  g.n = n;
+  g.sumC = sumC;
+  g.maxC = maxC;
+  return MM_OK;
+}
+
+// VJP work split of one instance: fibers per item and item count.
+void vjp_split(const Geom& g, int64_t target_amps, uint32_t& fpi, int64_t& items) {
+  const int64_t s0 = g.strides[0], C0 = g.shape[0];
+  int64_t f = (target_amps + C0 - 1) / C0;
+  f = (f + MM_BLOCK - 1) / MM_BLOCK * MM_BLOCK;
+  if (f < MM_BLOCK) f = MM_BLOCK;
+  if (f > s0) f = s0;
+  fpi = (uint32_t)f;
+  items = (s0 + f - 1) / f;
+}
+
+// Workspace regions shared by every entry point.
+struct Layout {
+  size_t tables = 0, coef = 0, partials = 0, desc = 0, order = 0, items = 0, total = 0;
+  int64_t kmax = 0;
+};
+
+Layout make_layout(int64_t kmax, int64_t coef_entries_total, int64_t n_items, int64_t n_desc, int64_t n_order) {
+  Layout L;
+  L.kmax = kmax;
+  size_t off = sizeof(WsHeader);
+  L.tables = off;
+  off = align_up(off + 3 * (size_t)kmax * sizeof(double));
+  L.coef = off;
+  off = align_up(off + (size_t)coef_entries_total * sizeof(double2));
+  L.partials = off;
+  off = align_up(off + (size_t)n_items * MM_NV_MAX * sizeof(double2));
+  L.desc = off;
+  off = align_up(off + (size_t)n_desc * sizeof(InstDesc));
+  L.order = off;
+  off = align_up(off + (size_t)n_order * sizeof(int32_t));
+  L.items = off;
+  off = align_up(off + (size_t)n_items * sizeof(VjpItem));
+  L.total = off;
+  return L;
+}
+
+// Uniform (one shape) plan of a call.
+struct UniformPlan {
+  Geom g;
+  int64_t B;
+  uint32_t fpi;
+  int64_t items_per_inst;
+  Layout L;
+};
+
+int plan_uniform(int64_t B, int D, const int64_t* shape, UniformPlan& P, int sms) {
+  int rc = make_geom(D, shape, P.g);
+  if (rc) return rc;
+  if (B < 0) return MM_ERR_INVALID_ARG;
+  P.B = B;
+  // enough VJP items to fill the GPU several times over
+  const int64_t total = B * P.g.n;
+  int64_t want_items = std::max<int64_t>((total + kVjpItemAmps - 1) / kVjpItemAmps, 4 * (int64_t)std::max(sms, 1));
+  int64_t per_inst = std::max<int64_t>(1, (want_items + std::max<int64_t>(B, 1) - 1) / std::max<int64_t>(B, 1));
+  int64_t target = std::max<int64_t>(1, P.g.n / per_inst);
+  vjp_split(P.g, target, P.fpi, P.items_per_inst);
+  P.L = make_layout(P.g.maxC + 1, B * coef_entries(P.g), B * P.items_per_inst, 0, 0);
+  return MM_OK;
+}
+
+int check_ws(void* ws, size_t ws_bytes, size_t need) {
+  if (ws == nullptr || ((uintptr_t)ws % kAlign) != 0 || ws_bytes < need) return MM_ERR_WORKSPACE;
+  return MM_OK;
+}
+
+UniformSrc uniform_src(const UniformPlan& P, const double2* A, const double2* b, const double2* c, double2* G,
+                       const double2* dLdG, char* ws) {
+  UniformSrc s;
+  s.g = P.g;
+  s.B = P.B;
+  s.A = A;
+  s.b = b;
+  s.c = c;
+  s.G = G;
+  s.dLdG = dLdG;
+  s.coef = reinterpret_cast<double2*>(ws + P.L.coef);
+  s.coef_stride = coef_entries(P.g);
+  s.items_per_inst = P.items_per_inst;
+  s.fibers_per_item = P.fpi;
+  return s;
+}
+
+Tables tables_of(char* ws, const Layout& L) {
+  Tables T;
+  double* base = reinterpret_cast<double*>(ws + L.tables);
+  T.sq = base;
+  T.rs = base + L.kmax;
+  T.hh = base + 2 * L.kmax;
+  T.kmax = L.kmax;
+  return T;
+}
+
+int reset_launch_state(char* ws, cudaStream_t st) {
+  MM_CUDA(cudaMemsetAsync(ws + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st));
+  return MM_OK;
+}
+
+template <class Src>
+int launch_setup(const Src& src, int64_t n_inst, char* ws, const Layout& L, int do_coef, cudaStream_t st) {
+  double* base = reinterpret_cast<double*>(ws + L.tables);
+  int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(do_coef ? n_inst : 1, 65535));
+  blocks = std::max<int64_t>(blocks, std::min<int64_t>((L.kmax + 255) / 256, 65535));
+  setup_kernel<Src><<<(unsigned)blocks, 256, 0, st>>>(src, base, base + L.kmax, base + 2 * L.kmax, L.kmax, do_coef);
+  MM_LAUNCHED();
+  return MM_OK;
+}
+
+template <int D>
+int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, int stable, const DevInfo& di,
+                         cudaStream_t st) {
+  const double* rs = tables_of(ws, P.L).rs;
+  if (P.B == 1 && P.g.n >= kGridMinAmps && di.coop) {
+    int per_sm = 0;
+    MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_grid_kernel<D>, kGridBlock, 0));
+    if (per_sm >= 1) {
+      WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+      uint32_t small = kSmallChunk;
+      uint64_t budget = wait_budget_ns();
+      UniformSrc s = src;
+      void* args[] = {&s, (void*)&rs, &h, &small, &budget, &stable};
+      MM_CUDA(cudaLaunchCooperativeKernel((void*)fwd_grid_kernel<D>, dim3(di.sms), dim3(kGridBlock), args, 0, st));
+      g_launches.fetch_add(1);
+      return MM_OK;
+    }
+  }
+  if (P.B > 0) {
+    fwd_cta_kernel<D, D, UniformSrc><<<(unsigned)P.B, MM_BLOCK, 0, st>>>(src, rs, stable);
+    MM_LAUNCHED();
+  }
+  return MM_OK;
+}
+
+int launch_fwd_uniform(const UniformPlan& P, const UniformSrc& src, char* ws, int stable, const DevInfo& di,
+                       cudaStream_t st) {
+  switch (P.g.D) {
+    case 1: return launch_fwd_uniform_D<1>(P, src, ws, stable, di, st);
+    case 2: return launch_fwd_uniform_D<2>(P, src, ws, stable, di, st);
+    case 3: return launch_fwd_uniform_D<3>(P, src, ws, stable, di, st);
+    case 4: return launch_fwd_uniform_D<4>(P, src, ws, stable, di, st);
+    case 5: return launch_fwd_uniform_D<5>(P, src, ws, stable, di, st);
+    case 6: return launch_fwd_uniform_D<6>(P, src, ws, stable, di, st);
+    case 7: return launch_fwd_uniform_D<7>(P, src, ws, stable, di, st);
+    case 8: return launch_fwd_uniform_D<8>(P, src, ws, stable, di, st);
+  }
+  return MM_ERR_UNSUPPORTED;
+}
+
+template <class Src>
+int launch_vjp_items(int D, const Src& src, Tables T, double2* partials, int64_t item_base, int64_t n_items,
+                     cudaStream_t st) {
+  if (n_items <= 0) return MM_OK;
+  // gridDim.x limit is 2^31 - 1; split very long item lists
+  for (int64_t done = 0; done < n_items;) {
+    const unsigned nb = (unsigned)std::min<int64_t>(n_items - done, INT32_MAX);
+    const int64_t base = item_base + done;
+    switch (D) {
+      case 1: vjp_items_kernel<1, 1, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 2: vjp_items_kernel<2, 2, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 3: vjp_items_kernel<3, 3, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 4: vjp_items_kernel<4, 4, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 5: vjp_items_kernel<5, 5, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 6: vjp_items_kernel<6, 6, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 7: vjp_items_kernel<7, 7, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      case 8: vjp_items_kernel<8, 8, Src><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, base); break;
+      default: return MM_ERR_UNSUPPORTED;
+    }
+    MM_LAUNCHED();
+    done += nb;
+  }
+  return MM_OK;
+}
+
+template <class Src>
+int launch_vjp_reduce(const Src& src, int64_t n_inst, const double2* partials, double2* dA, double2* db, double2* dc,
+                      cudaStream_t st) {
+  if (n_inst <= 0) return MM_OK;
+  const int64_t blocks = (n_inst + 3) / 4;
+  vjp_reduce_kernel<Src><<<(unsigned)blocks, 128, 0, st>>>(src, partials, dA, db, dc);
+  MM_LAUNCHED();
+  return MM_OK;
+}
+
+int common_checks(void* ws, mm_stream_t stream, DevInfo& di) {
+  (void)ws;
+  (void)stream;
+  return device_info(di);
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+struct mm_ragged_plan {
+  int64_t B = 0;
+  std::vector<InstDesc> desc;
+  std::vector<int32_t> order;     // forward schedule: instances by decreasing cost
+  std::vector<VjpItem> items;     // VJP items grouped by D, then instance
+  std::vector<int64_t> d_item_begin, d_item_count;  // per D (index D)
+  int maxD = 0;
+  int64_t kmax = 0;
+  int64_t total_amps = 0;
+  int64_t total_coef = 0;
+  int64_t team_min_amps = 0;
+  int64_t vjp_item_amps = kVjpItemAmps;
+  Layout L;
+};
+
+namespace {
+int ragged_build(mm_ragged_plan* p) {
+  const int64_t B = p->B;
+  // VJP items: grouped by D (one launch per D), instances by decreasing size
+  std::vector<int32_t> byD(p->order);
+  std::stable_sort(byD.begin(), byD.end(), [&](int32_t a, int32_t b) { return p->desc[a].g.D < p->desc[b].g.D; });
+  p->items.clear();
+  p->d_item_begin.assign(MM_MAXD + 1, 0);
+  p->d_item_count.assign(MM_MAXD + 1, 0);
+  for (int32_t k : byD) {
+    InstDesc& d = p->desc[k];
+    uint32_t fpi;
+    int64_t nit;
+    vjp_split(d.g, p->vjp_item_amps, fpi, nit);
+    d.item_begin = (int64_t)p->items.size();
+    d.n_items = nit;
+    d.fibers_per_item = fpi;
+    if (p->d_item_count[d.g.D] == 0) p->d_item_begin[d.g.D] = d.item_begin;
+    p->d_item_count[d.g.D] += nit;
+    for (int64_t r = 0; r < nit; ++r) {
+      VjpItem it;
+      it.inst = k;
+      it.q0 = (uint32_t)(r * fpi);
+      it.q1 = (uint32_t)std::min<int64_t>((r + 1) * (int64_t)fpi, d.g.strides[0]);
+      it.pad = 0;
+      p->items.push_back(it);
+    }
+  }
+  (void)B;
+  p->L = make_layout(p->kmax, p->total_coef, (int64_t)p->items.size(), p->B, p->B);
+  return MM_OK;
+}
+
+RaggedSrc ragged_src(const mm_ragged_plan* p, char* ws, const double2* A, const double2* b, const double2* c,
+                     double2* G, const double2* dLdG) {
+  RaggedSrc s;
+  s.desc = reinterpret_cast<const InstDesc*>(ws + p->L.desc);
+  s.order = reinterpret_cast<const int32_t*>(ws + p->L.order);
+  s.B = p->B;
+  s.A = A;
+  s.b = b;
+  s.c = c;
+  s.G = G;
+  s.dLdG = dLdG;
+  s.coef = reinterpret_cast<double2*>(ws + p->L.coef);
+  s.items = reinterpret_cast<const VjpItem*>(ws + p->L.items);
+  return s;
+}
+}  // namespace
+
+extern "C" {
+
+const char* mm_status_string(int status) {
+  switch (status) {
+    case MM_OK: return "ok";
+    case MM_ERR_INVALID_ARG: return "invalid argument";
+    case MM_ERR_UNSUPPORTED: return "unsupported number of modes";
+    case MM_ERR_TOO_LARGE: return "tensor too large for the kernels' 32-bit slab indices";
+    case MM_ERR_CUDA: return "CUDA runtime error";
+    case MM_ERR_WAIT_TIMEOUT: return "bounded inter-CTA wait timed out";
+    case MM_ERR_WORKSPACE: return "workspace missing, misaligned or too small";
+    case MM_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+int mm_max_modes(void) { return MM_MAXD; }
+const char* mm_last_cuda_error(void) { return g_last_cuda_error; }
+int64_t mm_launch_count(void) { return g_launches.load(); }
+
+int mm_workspace_init(void* ws, size_t ws_bytes, mm_stream_t stream) {
+  if (ws == nullptr || ws_bytes < sizeof(WsHeader)) return MM_ERR_WORKSPACE;
+  MM_CUDA(cudaMemsetAsync(ws, 0, sizeof(WsHeader), (cudaStream_t)stream));
+  return MM_OK;
+}
+
+int mm_workspace_status(void* ws, mm_stream_t stream, int* status) {
+  if (ws == nullptr || status == nullptr) return MM_ERR_INVALID_ARG;
+  MM_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  int32_t v = 0;
+  MM_CUDA(cudaMemcpy(&v, ws, sizeof(v), cudaMemcpyDeviceToHost));
+  MM_CUDA(cudaMemset(ws, 0, sizeof(int32_t)));
+  *status = v;
+  return MM_OK;
+}
+
+size_t mm_hermite_workspace_bytes(int D, const int64_t* shape, int64_t batch) {
+  DevInfo di;
+  int sms = device_info(di) == MM_OK ? di.sms : 152;
+  UniformPlan P;
+  if (plan_uniform(batch < 1 ? 1 : batch, D, shape, P, sms)) return 0;
+  return P.L.total;
+}
+
+int mm_hermite_fwd_batched(int64_t B, int D, const int64_t* shape, const mm_c128* A, const mm_c128* b,
+                           const mm_c128* c, int stable, mm_c128* G, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  DevInfo di;
+  int rc = common_checks(ws, stream, di);
+  if (rc) return rc;
+  UniformPlan P;
+  if ((rc = plan_uniform(B, D, shape, P, di.sms))) return rc;
+  if (B == 0) return MM_OK;
+  if (!A || !b || !c || !G) return MM_ERR_INVALID_ARG;
+  if ((rc = check_ws(ws, ws_bytes, P.L.total))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  UniformSrc src = uniform_src(P, (const double2*)A, (const double2*)b, (const double2*)c, (double2*)G, nullptr, w);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  if ((rc = launch_setup(src, B, w, P.L, 1, st))) return rc;
+  return launch_fwd_uniform(P, src, w, stable, di, st);
+}
+
+int mm_hermite_fwd(int D, const int64_t* shape, const mm_c128* A, const mm_c128* b, const mm_c128* c, int stable,
+                   mm_c128* G, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  return mm_hermite_fwd_batched(1, D, shape, A, b, c, stable, G, ws, ws_bytes, stream);
+}
+
+int mm_hermite_vjp_batched(int64_t B, int D, const int64_t* shape, const mm_c128* G, const mm_c128* c,
+                           const mm_c128* dLdG, mm_c128* dA, mm_c128* db, mm_c128* dc, void* ws, size_t ws_bytes,
+                           mm_stream_t stream) {
+  DevInfo di;
+  int rc = common_checks(ws, stream, di);
+  if (rc) return rc;
+  UniformPlan P;
+  if ((rc = plan_uniform(B, D, shape, P, di.sms))) return rc;
+  if (B == 0) return MM_OK;
+  if (!G || !c || !dLdG || !dA || !db || !dc) return MM_ERR_INVALID_ARG;
+  if ((rc = check_ws(ws, ws_bytes, P.L.total))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  UniformSrc src =
+      uniform_src(P, nullptr, nullptr, (const double2*)c, (double2*)G, (const double2*)dLdG, w);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  if ((rc = launch_setup(src, B, w, P.L, 0, st))) return rc;
+  double2* partials = reinterpret_cast<double2*>(w + P.L.partials);
+  if ((rc = launch_vjp_items(D, src, tables_of(w, P.L), partials, 0, B * P.items_per_inst, st))) return rc;
+  return launch_vjp_reduce(src, B, partials, (double2*)dA, (double2*)db, (double2*)dc, st);
+}
+
+int mm_hermite_vjp(int D, const int64_t* shape, const mm_c128* G, const mm_c128* c, const mm_c128* dLdG, mm_c128* dA,
+                   mm_c128* db, mm_c128* dc, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  return mm_hermite_vjp_batched(1, D, shape, G, c, dLdG, dA, db, dc, ws, ws_bytes, stream);
+}
+
+// ------------------------------------------------------------------- ragged
+int mm_ragged_plan_create(int64_t B, const int32_t* D, const int64_t* shapes, mm_ragged_plan** plan) {
+  if (plan == nullptr || B < 0 || (B > 0 && (D == nullptr || shapes == nullptr))) return MM_ERR_INVALID_ARG;
+  if (B > INT32_MAX) return MM_ERR_TOO_LARGE;
+  mm_ragged_plan* p = new (std::nothrow) mm_ragged_plan();
+  if (!p) return MM_ERR_INVALID_ARG;
+  p->B = B;
+  p->desc.resize(B);
+  int64_t off_g = 0, off_a = 0, off_b = 0, off_coef = 0, off_s = 0;
+  for (int64_t k = 0; k < B; ++k) {
+    InstDesc& d = p->desc[k];
+    memset(&d, 0, sizeof(d));
+    int rc = make_geom(D[k], shapes + off_s, d.g);
+    if (rc) {
+      delete p;
+      return rc;
+    }
+    off_s += D[k];
+    d.g_off = off_g;
+    d.a_off = off_a;
+    d.b_off = off_b;
+    d.coef_off = off_coef;
+    off_g += d.g.n;
+    off_a += (int64_t)D[k] * D[k];
+    off_b += D[k];
+    off_coef += coef_entries(d.g);
+    p->maxD = std::max(p->maxD, (int)D[k]);
+    p->kmax = std::max<int64_t>(p->kmax, d.g.maxC + 1);
+  }
+  p->total_amps = off_g;
+  p->total_coef = off_coef;
+  p->order.resize(B);
+  for (int64_t k = 0; k < B; ++k) p->order[k] = (int32_t)k;
+  // largest first: cost ~ amplitudes * (D + 1) terms
+  std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) {
+    return p->desc[a].g.n * (p->desc[a].g.D + 1) > p->desc[b].g.n * (p->desc[b].g.D + 1);
+  });
+  ragged_build(p);
+  *plan = p;
+  return MM_OK;
+}
+
+void mm_ragged_plan_destroy(mm_ragged_plan* plan) { delete plan; }
+size_t mm_ragged_plan_workspace_bytes(const mm_ragged_plan* plan) { return plan ? plan->L.total : 0; }
+int64_t mm_ragged_plan_amplitudes(const mm_ragged_plan* plan) { return plan ? plan->total_amps : 0; }
+
+int mm_ragged_plan_offsets(const mm_ragged_plan* plan, int64_t* g_off, int64_t* a_off, int64_t* b_off) {
+  if (!plan) return MM_ERR_INVALID_ARG;
+  for (int64_t k = 0; k < plan->B; ++k) {
+    if (g_off) g_off[k] = plan->desc[k].g_off;
+    if (a_off) a_off[k] = plan->desc[k].a_off;
+    if (b_off) b_off[k] = plan->desc[k].b_off;
+  }
+  return MM_OK;
+}
+
+int mm_ragged_plan_set_tuning(mm_ragged_plan* plan, int64_t team_min_amps, int64_t vjp_item_amps) {
+  if (!plan || team_min_amps < 0 || vjp_item_amps < 1) return MM_ERR_INVALID_ARG;
+  plan->team_min_amps = team_min_amps;
+  plan->vjp_item_amps = vjp_item_amps;
+  return ragged_build(plan);
+}
+
+int mm_ragged_plan_upload(const mm_ragged_plan* plan, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  if (!plan) return MM_ERR_INVALID_ARG;
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  if ((rc = check_ws(ws, ws_bytes, plan->L.total))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  if (plan->B > 0) {
+    MM_CUDA(cudaMemcpyAsync(w + plan->L.desc, plan->desc.data(), plan->desc.size() * sizeof(InstDesc),
+                            cudaMemcpyHostToDevice, st));
+    MM_CUDA(cudaMemcpyAsync(w + plan->L.order, plan->order.data(), plan->order.size() * sizeof(int32_t),
+                            cudaMemcpyHostToDevice, st));
+  }
+  if (!plan->items.empty())
+    MM_CUDA(cudaMemcpyAsync(w + plan->L.items, plan->items.data(), plan->items.size() * sizeof(VjpItem),
+                            cudaMemcpyHostToDevice, st));
+  MM_CUDA(cudaStreamSynchronize(st));
+  return MM_OK;
+}
+
+int mm_ragged_fwd(const mm_ragged_plan* plan, const mm_c128* A, const mm_c128* b, const mm_c128* c, int stable,
+                  mm_c128* G, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  if (!plan) return MM_ERR_INVALID_ARG;
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  if (plan->B == 0) return MM_OK;
+  if (!A || !b || !c || !G) return MM_ERR_INVALID_ARG;
+  if ((rc = check_ws(ws, ws_bytes, plan->L.total))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  RaggedSrc src = ragged_src(plan, w, (const double2*)A, (const double2*)b, (const double2*)c, (double2*)G, nullptr);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  if ((rc = launch_setup(src, plan->B, w, plan->L, 1, st))) return rc;
+  const double* rs = tables_of(w, plan->L).rs;
+  const unsigned nb = (unsigned)plan->B;
+  if (plan->maxD <= 2) fwd_cta_kernel<1, 2, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, rs, stable);
+  else if (plan->maxD <= 4) fwd_cta_kernel<1, 4, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, rs, stable);
+  else fwd_cta_kernel<1, 8, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, rs, stable);
+  MM_LAUNCHED();
+  return MM_OK;
+}
+
+int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c, const mm_c128* dLdG, mm_c128* dA,
+                  mm_c128* db, mm_c128* dc, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  if (!plan) return MM_ERR_INVALID_ARG;
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  if (plan->B == 0) return MM_OK;
+  if (!G || !c || !dLdG || !dA || !db || !dc) return MM_ERR_INVALID_ARG;
+  if ((rc = check_ws(ws, ws_bytes, plan->L.total))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  RaggedSrc src = ragged_src(plan, w, nullptr, nullptr, (const double2*)c, (double2*)G, (const double2*)dLdG);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  if ((rc = launch_setup(src, plan->B, w, plan->L, 0, st))) return rc;
+  double2* partials = reinterpret_cast<double2*>(w + plan->L.partials);
+  Tables T = tables_of(w, plan->L);
+  for (int D = 1; D <= MM_MAXD; ++D) {
+    if (plan->d_item_count[D] == 0) continue;
+    if ((rc = launch_vjp_items(D, src, T, partials, plan->d_item_begin[D], plan->d_item_count[D], st))) return rc;
+  }
+  return launch_vjp_reduce(src, plan->B, partials, (double2*)dA, (double2*)db, (double2*)dc, st);
+}
+
+// ---------------------------------------------------------------- diagnostics
+int mm_test_wait_timeout(void* ws, size_t ws_bytes, uint64_t budget_ns, mm_stream_t stream) {
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  if ((rc = check_ws(ws, ws_bytes, sizeof(WsHeader)))) return rc;
+  if (!di.coop) return MM_ERR_UNSUPPORTED;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  WsHeader* h = reinterpret_cast<WsHeader*>(w);
+  void* args[] = {&h, &budget_ns};
+  MM_CUDA(cudaLaunchCooperativeKernel((void*)wait_timeout_test_kernel, dim3(2), dim3(32), args, 0, st));
+  g_launches.fetch_add(1);
+  return MM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,567 @@
+// Device code of the Hermite recurrence, its stable variant and its VJP.
+//
+// Schedules
+// ---------
+// vanilla (reference: mrmustard/math/lattice/strategies/vanilla/core.py:25-124).
+//   The reference walks the flat C-order index f and takes as pivot axis i the
+//   first non-zero coordinate of k (core.py:88-94; i = 0 in the bulk,
+//   core.py:108-122).  Group the flat indices by that axis: "level" i holds
+//   every k with k_0..k_{i-1} = 0 and k_i >= 1, i.e. f in [strides[i],
+//   strides[i-1]); inside a level, "chunk" m = k_i is the contiguous run
+//   [m*strides[i], (m+1)*strides[i]).  Every amplitude of chunk (i, m) reads
+//   only chunks (i, m-1) and (i, m-2) (pivot f - s_i, neighbours f - s_i - s_j),
+//   so a chunk is fully parallel and levels run D-1, ..., 0, chunks m = 1, 2, ...
+//   This reproduces the reference's pivot choice and operation order
+//   (b_i G_p + A_ii sqrt(m-1) G_{p-1_i} + sum_{j>i} A_ij sqrt(k_j) G_{p-1_j})
+//   exactly; the final division by sqrt(m) becomes a multiply by 1/sqrt(m)
+//   and products are fused (DFMA), so results agree to rounding.
+//   Writes are contiguous (one chunk = one slab of the row-major tensor).
+// stable (core.py:127-213).  Every valid pivot is averaged, so an amplitude also
+//   reads amplitudes of its own chunk; the schedule is the |k| anti-diagonal
+//   wavefront (all reads sit on wavefronts |k|-1 and |k|-2).
+// VJP (gradients.py:25-82).  A reduction: no ordering constraint.  One thread
+//   owns a "fiber" (fixed k_1..k_{D-1}) and walks k_0, so the weights
+//   sqrt(k_i) sqrt(k_j) of every term not involving axis 0 are constant along
+//   the fiber and are applied once per fiber; the axis-0 weights are folded
+//   into the cotangent once per amplitude.
+#pragma once
+
+#include "common.cuh"
+
+namespace mm {
+
+struct InstView {
+  Geom g;
+  const double2* A;
+  const double2* b;
+  double2 c;
+  double2* G;
+  const double2* dLdG;
+  const double2* coef;
+};
+
+struct VjpItem {
+  int32_t inst;
+  uint32_t q0;
+  uint32_t q1;
+  int32_t pad;
+};
+
+// One shape, B instances (the unbatched call is B = 1).
+struct UniformSrc {
+  Geom g;
+  int64_t B;
+  const double2* A;
+  const double2* b;
+  const double2* c;
+  double2* G;
+  const double2* dLdG;
+  double2* coef;
+  int64_t coef_stride;
+  int64_t items_per_inst;
+  uint32_t fibers_per_item;
+  __device__ __forceinline__ int64_t n_inst() const { return B; }
+  __device__ __forceinline__ int64_t sched(int64_t t) const { return t; }
+  __device__ __forceinline__ void load(int64_t k, InstView& v) const {
+    v.g = g;
+    v.A = A + k * g.D * g.D;
+    v.b = b + k * g.D;
+    v.c = c[k];
+    v.G = G + k * g.n;
+    v.dLdG = dLdG ? dLdG + k * g.n : nullptr;
+    v.coef = coef + k * coef_stride;
+  }
+  __device__ __forceinline__ const Geom& geom(int64_t) const { return g; }
+  __device__ __forceinline__ double2* coef_of(int64_t k) const { return coef + k * coef_stride; }
+  __device__ __forceinline__ void item(int64_t it, int64_t& k, uint32_t& q0, uint32_t& q1) const {
+    k = it / items_per_inst;
+    const int64_t r = it - k * items_per_inst;
+    q0 = (uint32_t)(r * fibers_per_item);
+    const int64_t e = (r + 1) * (int64_t)fibers_per_item;
+    q1 = (uint32_t)(e < g.strides[0] ? e : g.strides[0]);
+  }
+  __device__ __forceinline__ void items_of(int64_t k, int64_t& begin, int64_t& count) const {
+    begin = k * items_per_inst;
+    count = items_per_inst;
+  }
+  __device__ __forceinline__ int64_t a_off(int64_t k) const { return k * g.D * g.D; }
+  __device__ __forceinline__ int64_t b_off(int64_t k) const { return k * g.D; }
+};
+
+// B instances with their own D and shape; descriptors live in the workspace.
+struct RaggedSrc {
+  const InstDesc* desc;
+  const int32_t* order;  // instances in schedule order (largest first)
+  int64_t B;
+  const double2* A;
+  const double2* b;
+  const double2* c;
+  double2* G;
+  const double2* dLdG;
+  double2* coef;
+  const VjpItem* items;
+  __device__ __forceinline__ int64_t n_inst() const { return B; }
+  __device__ __forceinline__ int64_t sched(int64_t t) const { return order[t]; }
+  __device__ __forceinline__ void load(int64_t k, InstView& v) const {
+    const InstDesc& d = desc[k];
+    v.g = d.g;
+    v.A = A + d.a_off;
+    v.b = b + d.b_off;
+    v.c = c[k];
+    v.G = G + d.g_off;
+    v.dLdG = dLdG ? dLdG + d.g_off : nullptr;
+    v.coef = coef + d.coef_off;
+  }
+  __device__ __forceinline__ const Geom& geom(int64_t k) const { return desc[k].g; }
+  __device__ __forceinline__ double2* coef_of(int64_t k) const { return coef + desc[k].coef_off; }
+  __device__ __forceinline__ void item(int64_t it, int64_t& k, uint32_t& q0, uint32_t& q1) const {
+    const VjpItem x = items[it];
+    k = x.inst;
+    q0 = x.q0;
+    q1 = x.q1;
+  }
+  __device__ __forceinline__ void items_of(int64_t k, int64_t& begin, int64_t& count) const {
+    begin = desc[k].item_begin;
+    count = desc[k].n_items;
+  }
+  __device__ __forceinline__ int64_t a_off(int64_t k) const { return desc[k].a_off; }
+  __device__ __forceinline__ int64_t b_off(int64_t k) const { return desc[k].b_off; }
+};
+
+template <bool CG>
+__device__ __forceinline__ double2 ldG(const double2* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return *p;
+}
+
+__device__ __forceinline__ void load_view_to_smem(InstView* sv, const InstView& v) { *sv = v; }
+
+// ============================================================== setup kernel
+// Scalar tables (grid-strided) and each instance's coefficient block (one CTA
+// per instance, grid-strided over instances).
+template <class Src>
+__global__ void __launch_bounds__(256) setup_kernel(Src src, double* sq, double* rs, double* hh, int64_t kmax,
+                                                    int do_coef) {
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = gtid; k < kmax; k += gstride) {
+    const double s = sqrt((double)k);
+    sq[k] = s;
+    rs[k] = k > 0 ? 1.0 / s : 0.0;
+    hh[k] = k > 1 ? (0.5 * s) * sqrt((double)(k - 1)) : 0.0;
+  }
+  if (!do_coef) return;
+  for (int64_t k = blockIdx.x; k < src.n_inst(); k += gridDim.x) {
+    const Geom& g = src.geom(k);
+    InstView v;
+    src.load(k, v);
+    double2* coef = src.coef_of(k);
+    const int64_t total = coef_entries(g);
+    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const int i = (int)(e / g.sumC);
+      const int32_t r = (int32_t)(e - (int64_t)i * g.sumC);
+      int j = 0;
+      while (j + 1 < g.D && g.prefC[j + 1] <= r) ++j;
+      const int32_t kk = r - g.prefC[j];
+      const double2 a = v.A[i * g.D + j];
+      double2 val;
+      if (j == i) {  // cd[i][m] = A_ii * sqrt(m - 1) (zero at m = 0, 1)
+        const double s = kk >= 1 ? sqrt((double)(kk - 1)) : 0.0;
+        val = cmk(a.x * s, a.y * s);
+      } else {  // W[i][j][k] = A_ij * sqrt(k)
+        const double s = sqrt((double)kk);
+        val = cmk(a.x * s, a.y * s);
+      }
+      coef[e] = val;
+    }
+  }
+}
+
+// ============================================================== vanilla forward
+// Chunk (level i, index m), amplitudes q in [q_begin, q_end) stepping by q_step
+// from thread rank t.
+template <int D, bool CG>
+__device__ __forceinline__ void fwd_chunk(const InstView& v, const double* __restrict__ rs, int i, int m,
+                                          uint32_t q_begin, uint32_t q_end, uint32_t q_step, uint32_t t) {
+  const Geom& g = v.g;
+  const int64_t si = g.strides[i];
+  const double2 bi = __ldg(v.b + i);
+  const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
+  const double2 cd = (m >= 2) ? crow[g.prefC[i] + m] : cmk(0.0, 0.0);
+  const double rsm = rs[m];
+  double2* G = v.G;
+  const int64_t base = (int64_t)m * si;
+  int64_t sj[D];
+  int32_t pj[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    sj[j] = g.strides[j];
+    pj[j] = g.prefC[j];
+  }
+  for (uint32_t q = q_begin + t; q < q_end; q += q_step) {
+    int32_t k[D];
+    decompose<D>(q, i + 1, g, k);
+    const int64_t f = base + q;
+    const int64_t p = f - si;
+    double2 acc = cmul(bi, ldG<CG>(G + p));
+    if (m >= 2) acc = cfma(cd, ldG<CG>(G + p - si), acc);
+#pragma unroll
+    for (int j = 1; j < D; ++j) {
+      if (j > i && k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + p - sj[j]), acc);
+    }
+    G[f] = cscale(rsm, acc);
+  }
+}
+
+// Whole instance on one CTA (chunks separated by __syncthreads).
+template <int D>
+__device__ void fwd_instance_cta(const InstView& v, const double* rs) {
+  if (threadIdx.x == 0) v.G[0] = v.c;
+  __syncthreads();
+  for (int i = D - 1; i >= 0; --i) {
+    const int Ci = (int)v.g.shape[i];
+    const uint32_t si = (uint32_t)v.g.strides[i];
+    for (int m = 1; m < Ci; ++m) {
+      fwd_chunk<D, false>(v, rs, i, m, 0u, si, blockDim.x, threadIdx.x);
+      __syncthreads();
+    }
+  }
+}
+
+// ============================================================== stable forward
+static __constant__ double c_inv_n[MM_MAXD + 1] = {0.0,       1.0,       1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0,
+                                            1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0, 1.0 / 8.0};
+
+// Wavefront |k| = w; prefixes p over axes 0..D-2 in [p_begin, p_end) by p_step.
+template <int D, bool CG>
+__device__ __forceinline__ void stable_wave(const InstView& v, const double* __restrict__ rs, int w, uint32_t p_begin,
+                                            uint32_t p_end, uint32_t p_step, uint32_t t) {
+  const Geom& g = v.g;
+  const int32_t CL = (int32_t)g.shape[D - 1];
+  double2* G = v.G;
+  int64_t sj[D];
+  int32_t pj[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    sj[j] = g.strides[j];
+    pj[j] = g.prefC[j];
+  }
+  for (uint32_t p = p_begin + t; p < p_end; p += p_step) {
+    int32_t k[D];
+    int32_t sum = 0;
+    uint32_t q = p;
+#pragma unroll
+    for (int j = D - 2; j >= 0; --j) {
+      const uint32_t c = (uint32_t)g.shape[j];
+      k[j] = (int32_t)(q % c);
+      q /= c;
+      sum += k[j];
+    }
+    const int32_t kl = w - sum;
+    if (kl < 0 || kl >= CL) continue;
+    k[D - 1] = kl;
+    const int64_t f = (int64_t)p * CL + kl;
+    double2 vals = cmk(0.0, 0.0);
+    int npiv = 0;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      if (k[i] > 0) {
+        ++npiv;
+        const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
+        const int64_t pv = f - sj[i];
+        double2 acc = cmul(__ldg(v.b + i), ldG<CG>(G + pv));
+#pragma unroll
+        for (int j = 0; j < i; ++j)
+          if (k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + pv - sj[j]), acc);
+        if (k[i] >= 2) acc = cfma(crow[pj[i] + k[i]], ldG<CG>(G + pv - sj[i]), acc);
+#pragma unroll
+        for (int j = i + 1; j < D; ++j)
+          if (k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + pv - sj[j]), acc);
+        vals = crfma(rs[k[i]], acc, vals);
+      }
+    }
+    G[f] = cscale(c_inv_n[npiv], vals);
+  }
+}
+
+template <int D>
+__device__ void stable_instance_cta(const InstView& v, const double* rs) {
+  if (threadIdx.x == 0) v.G[0] = v.c;
+  __syncthreads();
+  int wmax = 0;
+  for (int i = 0; i < D; ++i) wmax += (int)v.g.shape[i] - 1;
+  const uint32_t P = (uint32_t)(v.g.n / v.g.shape[D - 1]);
+  for (int w = 1; w <= wmax; ++w) {
+    stable_wave<D, false>(v, rs, w, 0u, P, blockDim.x, threadIdx.x);
+    __syncthreads();
+  }
+}
+
+// One CTA per instance, instances taken in schedule order (largest first).
+template <int DLO, int DHI, class Src>
+__global__ void __launch_bounds__(MM_BLOCK) fwd_cta_kernel(Src src, const double* __restrict__ rs, int stable) {
+  __shared__ InstView sv;
+  const int64_t k = src.sched(blockIdx.x);
+  if (threadIdx.x == 0) {
+    InstView v;
+    src.load(k, v);
+    sv = v;
+  }
+  __syncthreads();
+  const int D = sv.g.D;
+#define MM_FWD_CASE(DD)                                        \
+  if constexpr (DLO <= DD && DD <= DHI) {                      \
+    if (D == DD) {                                             \
+      if (stable) stable_instance_cta<DD>(sv, rs);             \
+      else fwd_instance_cta<DD>(sv, rs);                       \
+      return;                                                  \
+    }                                                          \
+  }
+  MM_FWD_CASE(1)
+  MM_FWD_CASE(2)
+  MM_FWD_CASE(3)
+  MM_FWD_CASE(4)
+  MM_FWD_CASE(5)
+  MM_FWD_CASE(6)
+  MM_FWD_CASE(7)
+  MM_FWD_CASE(8)
+#undef MM_FWD_CASE
+}
+
+// ------------------------------------------------ single large instance, whole grid
+// Cooperative launch (every CTA resident).  Levels whose chunks hold fewer than
+// `small_chunk` amplitudes run on CTA 0 alone; each larger chunk is split over
+// all CTAs in contiguous ranges with a bounded grid barrier after it.
+template <int D>
+__global__ void __launch_bounds__(512) fwd_grid_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
+                                                       uint32_t small_chunk, uint64_t budget_ns, int stable) {
+  __shared__ InstView sv;
+  if (threadIdx.x == 0) {
+    InstView v;
+    src.load(0, v);
+    sv = v;
+  }
+  __syncthreads();
+  const Geom& g = sv.g;
+  uint32_t epoch = 0;
+  if (!stable) {
+    int lvl_big = -1;  // levels 0..lvl_big use the whole grid
+    for (int i = 0; i < D; ++i)
+      if ((uint32_t)g.strides[i] >= small_chunk) lvl_big = i;
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) sv.G[0] = sv.c;
+      __syncthreads();
+      for (int i = D - 1; i > lvl_big; --i) {
+        const uint32_t si = (uint32_t)g.strides[i];
+        for (int m = 1; m < (int)g.shape[i]; ++m) {
+          fwd_chunk<D, false>(sv, rs, i, m, 0u, si, blockDim.x, threadIdx.x);
+          if (threadIdx.x == 0 && (m & 63) == 0) heartbeat(h);
+          __syncthreads();
+        }
+      }
+    }
+    if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+    for (int i = lvl_big; i >= 0; --i) {
+      const uint32_t si = (uint32_t)g.strides[i];
+      const uint32_t per = (si + gridDim.x - 1) / gridDim.x;
+      const uint32_t lo = min(si, per * blockIdx.x), hi = min(si, lo + per);
+      for (int m = 1; m < (int)g.shape[i]; ++m) {
+        fwd_chunk<D, true>(sv, rs, i, m, lo, hi, blockDim.x, threadIdx.x);
+        if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+      }
+    }
+  } else {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sv.G[0] = sv.c;
+    if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+    int wmax = 0;
+    for (int i = 0; i < D; ++i) wmax += (int)g.shape[i] - 1;
+    const uint32_t P = (uint32_t)(g.n / g.shape[D - 1]);
+    const uint32_t per = (P + gridDim.x - 1) / gridDim.x;
+    const uint32_t lo = min(P, per * blockIdx.x), hi = min(P, lo + per);
+    for (int w = 1; w <= wmax; ++w) {
+      stable_wave<D, true>(sv, rs, w, lo, hi, blockDim.x, threadIdx.x);
+      if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+    }
+  }
+}
+
+// Test kernel: a barrier whose target can never be reached (one extra arrival
+// is required), so every CTA gives up after budget_ns.
+__global__ void wait_timeout_test_kernel(WsHeader* h, uint64_t budget_ns) { grid_barrier(h, 1, budget_ns, 1); }
+
+// ============================================================== VJP
+// Per-thread accumulation over the fibers q of [q0, q1) (q = flat index over
+// axes 1..D-1) for one instance; results go to tot[] (weights applied).
+template <int D>
+__device__ __forceinline__ void vjp_fibers(const InstView& v, const Tables& T, uint32_t q0, uint32_t q1,
+                                           double2 (&tot)[vjp_nv(D)]) {
+  constexpr int NV = vjp_nv(D);
+  const Geom& g = v.g;
+  const int C0 = (int)g.shape[0];
+  const int64_t s0 = g.strides[0];
+  int64_t sj[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) sj[j] = g.strides[j];
+  const double2* __restrict__ G = v.G;
+  const double2* __restrict__ gb = v.dLdG;
+  const double* __restrict__ sq = T.sq;
+  const double* __restrict__ hh = T.hh;
+  for (uint32_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+    int32_t r[D];
+    decompose<D>(q, 1, g, r);
+    double2 a[NV];
+#pragma unroll
+    for (int s = 0; s < NV; ++s) a[s] = cmk(0.0, 0.0);
+    for (int m = 0; m < C0; ++m) {
+      const int64_t f = (int64_t)m * s0 + q;
+      const double2 gu = __ldg(gb + f);
+      a[0] = cfma(__ldg(G + f), gu, a[0]);
+      if (m >= 1) {
+        const double2 h0 = cscale(sq[m], gu);
+        a[1] = cfma(__ldg(G + f - s0), h0, a[1]);
+#pragma unroll
+        for (int j = 1; j < D; ++j)
+          if (r[j] >= 1) a[vjp_slot(D, 0, j)] = cfma(__ldg(G + f - s0 - sj[j]), h0, a[vjp_slot(D, 0, j)]);
+        if (m >= 2) {
+          const double2 h00 = cscale(hh[m], gu);
+          a[vjp_slot(D, 0, 0)] = cfma(__ldg(G + f - 2 * s0), h00, a[vjp_slot(D, 0, 0)]);
+        }
+      }
+#pragma unroll
+      for (int i = 1; i < D; ++i) {
+        if (r[i] >= 1) {
+          a[1 + i] = cfma(__ldg(G + f - sj[i]), gu, a[1 + i]);
+          if (r[i] >= 2) a[vjp_slot(D, i, i)] = cfma(__ldg(G + f - 2 * sj[i]), gu, a[vjp_slot(D, i, i)]);
+#pragma unroll
+          for (int j = i + 1; j < D; ++j)
+            if (r[j] >= 1) a[vjp_slot(D, i, j)] = cfma(__ldg(G + f - sj[i] - sj[j]), gu, a[vjp_slot(D, i, j)]);
+        }
+      }
+    }
+    // fold the fiber's sums with the weights that are constant along it
+    tot[0] = cadd(tot[0], a[0]);
+    tot[1] = cadd(tot[1], a[1]);
+    tot[vjp_slot(D, 0, 0)] = cadd(tot[vjp_slot(D, 0, 0)], a[vjp_slot(D, 0, 0)]);
+#pragma unroll
+    for (int j = 1; j < D; ++j) tot[vjp_slot(D, 0, j)] = crfma(sq[r[j]], a[vjp_slot(D, 0, j)], tot[vjp_slot(D, 0, j)]);
+#pragma unroll
+    for (int i = 1; i < D; ++i) {
+      tot[1 + i] = crfma(sq[r[i]], a[1 + i], tot[1 + i]);
+      tot[vjp_slot(D, i, i)] = crfma(hh[r[i]], a[vjp_slot(D, i, i)], tot[vjp_slot(D, i, i)]);
+#pragma unroll
+      for (int j = i + 1; j < D; ++j)
+        tot[vjp_slot(D, i, j)] = crfma(sq[r[i]] * sq[r[j]], a[vjp_slot(D, i, j)], tot[vjp_slot(D, i, j)]);
+    }
+  }
+}
+
+// Deterministic CTA reduction of NV complex values (fixed shuffle tree, then
+// warps in order); thread 0..NV-1 end up writing out[s].
+template <int NV>
+__device__ __forceinline__ void block_reduce_write(double2 (&tot)[NV], double2* out) {
+  __shared__ double2 red[MM_BLOCK / 32][MM_NV_MAX];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < NV; ++s) {
+    double x = tot[s].x, y = tot[s].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    if (lane == 0) red[warp][s] = cmk(x, y);
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  for (int s = threadIdx.x; s < NV; s += blockDim.x) {
+    double2 acc = red[0][s];
+    for (int w = 1; w < nw; ++w) acc = cadd(acc, red[w][s]);
+    out[s] = acc;
+  }
+}
+
+// One CTA per work item; partial sums to partials[item * MM_NV_MAX + slot].
+template <int DLO, int DHI, class Src>
+__global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, double2* __restrict__ partials,
+                                                             int64_t item_base) {
+  __shared__ InstView sv;
+  __shared__ uint32_t sq0, sq1;
+  const int64_t item = item_base + blockIdx.x;
+  if (threadIdx.x == 0) {
+    int64_t k;
+    uint32_t q0, q1;
+    src.item(item, k, q0, q1);
+    InstView v;
+    src.load(k, v);
+    sv = v;
+    sq0 = q0;
+    sq1 = q1;
+  }
+  __syncthreads();
+  const int D = sv.g.D;
+  double2* out = partials + item * MM_NV_MAX;
+#define MM_VJP_CASE(DD)                                       \
+  if constexpr (DLO <= DD && DD <= DHI) {                     \
+    if (D == DD) {                                            \
+      double2 tot[vjp_nv(DD)];                                \
+      for (int s = 0; s < vjp_nv(DD); ++s) tot[s] = cmk(0, 0); \
+      vjp_fibers<DD>(sv, T, sq0, sq1, tot);                   \
+      block_reduce_write<vjp_nv(DD)>(tot, out);               \
+      return;                                                 \
+    }                                                         \
+  }
+  MM_VJP_CASE(1)
+  MM_VJP_CASE(2)
+  MM_VJP_CASE(3)
+  MM_VJP_CASE(4)
+  MM_VJP_CASE(5)
+  MM_VJP_CASE(6)
+  MM_VJP_CASE(7)
+  MM_VJP_CASE(8)
+#undef MM_VJP_CASE
+}
+
+// One warp per instance: sum its items' partials in item order, then write
+// dA (symmetrised as (X + X^T)/2, gradients.py:82), db, dc = sum(G dLdG) / c.
+template <class Src>
+__global__ void __launch_bounds__(128) vjp_reduce_kernel(Src src, const double2* __restrict__ partials,
+                                                         double2* __restrict__ dA, double2* __restrict__ db,
+                                                         double2* __restrict__ dc) {
+  const int warps = blockDim.x >> 5;
+  const int64_t k = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (k >= src.n_inst()) return;
+  const Geom& g = src.geom(k);
+  const int D = g.D;
+  const int NV = vjp_nv(D);
+  int64_t it0, nit;
+  src.items_of(k, it0, nit);
+  double2* dAk = dA + src.a_off(k);
+  double2* dbk = db + src.b_off(k);
+  for (int s = lane; s < NV; s += 32) {
+    double2 acc = cmk(0.0, 0.0);
+    for (int64_t it = 0; it < nit; ++it) acc = cadd(acc, partials[(it0 + it) * MM_NV_MAX + s]);
+    if (s == 0) {
+      dc[k] = cdiv_smith(acc, __ldg(src.c + k));
+    } else if (s <= D) {
+      dbk[s - 1] = acc;
+    } else {
+      // locate (i, j) of slot s
+      int i = 0, base = 1 + D;
+      while (s >= base + (D - i)) {
+        base += D - i;
+        ++i;
+      }
+      const int j = i + (s - base);
+      if (i == j) {
+        dAk[i * D + i] = acc;
+      } else {
+        const double2 half = cmk(acc.x / 2.0, acc.y / 2.0);
+        dAk[i * D + j] = half;
+        dAk[j * D + i] = half;
+      }
+    }
+  }
+}
+
+}  // namespace mm

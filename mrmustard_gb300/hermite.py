@@ -1,0 +1,304 @@
+"""Host-side mirror of MrMustard's ``hermite_renormalized`` path on the GB300 library.
+
+Two layers, both with the reference's names, argument meaning and errors:
+
+* kernel level (``mrmustard/math/lattice/strategies/vanilla/__init__.py:17-27``):
+  ``vanilla``, ``stable``, ``vanilla_batch``, ``vanilla_vjp``, ``vanilla_batch_vjp`` and the
+  drop-in aliases ``vanilla_numba``, ``stable_numba``, ``vanilla_batch_numba``,
+  ``vanilla_vjp_numba``, ``vanilla_batch_vjp_numba``;
+* facade level: ``hermite_renormalized(A, b, c, shape, stable=False, out=None)`` with the
+  batching / broadcasting / ``out`` rules of ``BackendManager.hermite_renormalized``
+  (``mrmustard/math/backend_manager.py:643-727``).
+
+Arrays may be numpy arrays (host; results come back as numpy, like the reference's numpy
+backend) or torch tensors on a CUDA device (results stay on the device).  All compute runs
+in ``libmm_gb300.so``; without a CUDA device every call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections.abc import Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .settings import settings
+
+__all__ = [
+    "vanilla",
+    "stable",
+    "vanilla_batch",
+    "vanilla_vjp",
+    "vanilla_batch_vjp",
+    "vanilla_numba",
+    "stable_numba",
+    "vanilla_batch_numba",
+    "vanilla_vjp_numba",
+    "vanilla_batch_vjp_numba",
+    "hermite_renormalized",
+    "hermite_renormalized_batched",
+    "device_fwd",
+    "device_vjp",
+]
+
+
+# ----------------------------------------------------------------- plumbing
+def require_cuda() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("mrmustard_gb300 computes on a CUDA device only; no CUDA device is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _is_dev(x) -> bool:
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def _to_dev(x, device) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        t = x.detach()
+        if t.dtype != torch.complex128:
+            t = t.to(torch.complex128)
+        return t.to(device).contiguous()
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+    return torch.from_numpy(a).to(device)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _shape_arr(shape: Sequence[int]):
+    shape = tuple(int(s) for s in shape)
+    return shape, (ctypes.c_int64 * max(1, len(shape)))(*shape)
+
+
+class Workspace:
+    """Per-call device scratch from torch's stream-ordered caching allocator."""
+
+    def __init__(self, nbytes: int, device):
+        lib = _lib.load()
+        self.nbytes = max(int(nbytes), 512)
+        self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+        _lib.check(lib.mm_workspace_init(self.ptr, self.nbytes, _stream()), "mm_workspace_init")
+
+    @property
+    def ptr(self) -> int:
+        return self.buf.data_ptr()
+
+    def check_status(self, where: str) -> None:
+        st = ctypes.c_int(0)
+        lib = _lib.load()
+        _lib.check(lib.mm_workspace_status(self.ptr, _stream(), ctypes.byref(st)), "mm_workspace_status")
+        if st.value != 0:
+            raise _lib.MMError(st.value, where, "device status word")
+
+
+def _finish(ws: Workspace, where: str) -> None:
+    if settings.CHECK_DEVICE_STATUS:
+        ws.check_status(where)
+
+
+# ----------------------------------------------------------- device entry points
+def device_fwd(A: torch.Tensor, b: torch.Tensor, c: torch.Tensor, shape, stable: bool = False,
+               out: torch.Tensor | None = None) -> torch.Tensor:
+    """Forward on device tensors.  A: (B,D,D) or (D,D); b: (B,D) or (D,); c: (B,) or ()."""
+    lib = _lib.load()
+    batched = A.dim() == 3
+    shape, sh = _shape_arr(shape)
+    D = len(shape)
+    B = A.shape[0] if batched else 1
+    if A.shape[-1] != D or A.shape[-2] != D or b.shape[-1] != D:
+        raise ValueError(f"A {tuple(A.shape)} / b {tuple(b.shape)} do not match the {D} axes of shape {shape}")
+    full = ((B,) if batched else ()) + shape
+    if out is None:
+        out = torch.empty(full, dtype=torch.complex128, device=A.device)
+    elif tuple(out.shape) != full or out.dtype != torch.complex128 or not out.is_contiguous() or not out.is_cuda:
+        raise ValueError(f"out must be a contiguous complex128 CUDA tensor of shape {full}")
+    if B == 0 or out.numel() == 0:
+        return out
+    ws = Workspace(lib.mm_hermite_workspace_bytes(D, sh, B), A.device)
+    c = c.reshape(-1)
+    if batched:
+        rc = lib.mm_hermite_fwd_batched(B, D, sh, _ptr(A), _ptr(b), _ptr(c), int(bool(stable)), _ptr(out), ws.ptr,
+                                        ws.nbytes, _stream())
+    else:
+        rc = lib.mm_hermite_fwd(D, sh, _ptr(A), _ptr(b), _ptr(c), int(bool(stable)), _ptr(out), ws.ptr, ws.nbytes,
+                                _stream())
+    _lib.check(rc, "mm_hermite_fwd")
+    _finish(ws, "hermite forward")
+    return out
+
+
+def device_vjp(G: torch.Tensor, c: torch.Tensor, dLdG: torch.Tensor, batched: bool):
+    """VJP on device tensors; returns (dA, db, dc) on the device."""
+    lib = _lib.load()
+    shape = tuple(G.shape[1:]) if batched else tuple(G.shape)
+    shape, sh = _shape_arr(shape)
+    D = len(shape)
+    B = G.shape[0] if batched else 1
+    if tuple(dLdG.shape) != tuple(G.shape):
+        raise ValueError(f"dLdG shape {tuple(dLdG.shape)} must equal G shape {tuple(G.shape)}")
+    dev = G.device
+    dA = torch.empty(((B,) if batched else ()) + (D, D), dtype=torch.complex128, device=dev)
+    db = torch.empty(((B,) if batched else ()) + (D,), dtype=torch.complex128, device=dev)
+    dc = torch.empty((B,) if batched else (), dtype=torch.complex128, device=dev)
+    if B == 0:
+        return dA, db, dc
+    ws = Workspace(lib.mm_hermite_workspace_bytes(D, sh, B), dev)
+    c = c.reshape(-1)
+    if batched:
+        rc = lib.mm_hermite_vjp_batched(B, D, sh, _ptr(G), _ptr(c), _ptr(dLdG), _ptr(dA), _ptr(db), _ptr(dc), ws.ptr,
+                                        ws.nbytes, _stream())
+    else:
+        rc = lib.mm_hermite_vjp(D, sh, _ptr(G), _ptr(c), _ptr(dLdG), _ptr(dA), _ptr(db), _ptr(dc), ws.ptr, ws.nbytes,
+                                _stream())
+    _lib.check(rc, "mm_hermite_vjp")
+    _finish(ws, "hermite vjp")
+    return dA, db, dc
+
+
+# ------------------------------------------------------------ kernel-level API
+def _host_or_dev(*xs):
+    dev_mode = any(_is_dev(x) for x in xs if x is not None)
+    device = next((x.device for x in xs if _is_dev(x)), None) or require_cuda()
+    return dev_mode, device
+
+
+def _deliver(res: torch.Tensor, out, dev_mode: bool):
+    """Return like the reference: into `out` when given, numpy for host callers."""
+    if out is not None:
+        if isinstance(out, torch.Tensor):
+            if out.data_ptr() != res.data_ptr():
+                out.copy_(res.reshape(out.shape))
+            return out
+        out[...] = res.cpu().numpy().reshape(out.shape)
+        return out
+    return res if dev_mode else res.cpu().numpy()
+
+
+def _fwd_common(shape, A, b, c, stable_flag, out, batched):
+    dev_mode, device = _host_or_dev(A, b, c, out)
+    A_d, b_d, c_d = _to_dev(A, device), _to_dev(b, device), _to_dev(c, device)
+    direct = (
+        isinstance(out, torch.Tensor) and out.is_cuda and out.is_contiguous() and out.dtype == torch.complex128
+        and tuple(out.shape) == ((A_d.shape[0],) if batched else ()) + tuple(int(s) for s in shape)
+    )
+    res = device_fwd(A_d, b_d, c_d, shape, stable_flag, out if direct else None)
+    return _deliver(res, out, dev_mode)
+
+
+def vanilla(shape, A, b, c, out=None):
+    """``vanilla_numba`` (core.py:25-124) on the GPU: Fock amplitudes of shape ``shape``."""
+    return _fwd_common(shape, A, b, c, False, out, batched=False)
+
+
+def stable(shape, A, b, c, out=None):
+    """``stable_numba`` (core.py:127-213) on the GPU."""
+    return _fwd_common(shape, A, b, c, True, out, batched=False)
+
+
+def vanilla_batch(shape, A, b, c, stable=False, out=None):
+    """``vanilla_batch_numba`` (batch.py:27-61): batch on axis 0 of A, b and c."""
+    return _fwd_common(shape, A, b, c, bool(stable), out, batched=True)
+
+
+def _vjp_common(G, c, dLdG, batched):
+    dev_mode, device = _host_or_dev(G, c, dLdG)
+    G_d, c_d, g_d = _to_dev(G, device), _to_dev(c, device), _to_dev(dLdG, device)
+    dA, db, dc = device_vjp(G_d, c_d, g_d, batched)
+    if dev_mode:
+        return dA, db, dc
+    return dA.cpu().numpy(), db.cpu().numpy(), (dc.cpu().numpy() if batched else complex(dc.item()))
+
+
+def vanilla_vjp(G, c, dLdG):
+    """``vanilla_vjp_numba`` (gradients.py:25-82): returns dL/dA, dL/db, dL/dc."""
+    return _vjp_common(G, c, dLdG, batched=False)
+
+
+def vanilla_batch_vjp(G, c, dLdG):
+    """``vanilla_batch_vjp_numba`` (gradients.py:85-116)."""
+    return _vjp_common(G, c, dLdG, batched=True)
+
+
+# drop-in aliases with the reference's names
+vanilla_numba = vanilla
+stable_numba = stable
+vanilla_batch_numba = vanilla_batch
+vanilla_vjp_numba = vanilla_vjp
+vanilla_batch_vjp_numba = vanilla_batch_vjp
+
+
+# ----------------------------------------------------------------- facade
+def _ndim(x):
+    return x.dim() if isinstance(x, torch.Tensor) else np.ndim(x)
+
+
+def _shp(x):
+    return tuple(x.shape) if isinstance(x, (torch.Tensor, np.ndarray)) else np.shape(x)
+
+
+def _reshape(x, s):
+    return x.reshape(s)
+
+
+def _broadcast(x, s):
+    if isinstance(x, torch.Tensor):
+        return x.broadcast_to(s)
+    return np.broadcast_to(np.asarray(x), s)
+
+
+def hermite_renormalized_batched(A, b, c, shape, stable=False, out=None):
+    """``BackendNumpy.hermite_renormalized_batched`` (backend_numpy.py:394-403)."""
+    return vanilla_batch(tuple(shape), A, b, c, stable, out)
+
+
+def hermite_renormalized(A, b, c, shape, stable=False, out=None):
+    """``math.hermite_renormalized`` (backend_manager.py:643-727) on the GB300 library.
+
+    1. A.ndim = 2, b.ndim = 1, c scalar: unbatched;
+    2. A.ndim = 2, b.ndim > 1: b-batched, A and c broadcast over b's batch dims;
+    3. A.ndim > 2, b.ndim > 1, c.ndim > 0: fully batched, batch dims flattened.
+    ``stable`` is also switched on by ``settings.STABLE_FOCK_CONVERSION``.
+    """
+    shape = tuple(int(s) for s in shape)
+
+    def check_out_shape(batch_shape):
+        if out is not None and any(d_out < d for d_out, d in zip(_shp(out), batch_shape + shape)):
+            raise ValueError(f"batch+shape {batch_shape + shape} is too large for out.shape={_shp(out)}")
+
+    stable = stable or settings.STABLE_FOCK_CONVERSION
+    if _ndim(A) > 2 and _ndim(b) > 1 and _ndim(c) > 0:
+        batch_shape = _shp(A)[:-2]
+        check_out_shape(batch_shape)
+        if _shp(b)[:-1] != batch_shape:
+            raise ValueError(f"b.shape={_shp(b)} must match batch_shape={batch_shape}")
+        if _shp(c)[: len(batch_shape)] != batch_shape:
+            raise ValueError(f"c.shape={_shp(c)} must match batch_shape={batch_shape}")
+        n = int(np.prod(batch_shape))
+        A2 = _reshape(A, (n, *_shp(A)[-2:]))
+        b2 = _reshape(b, (n, _shp(b)[-1]))
+        c2 = _reshape(c, (n,))
+        out2 = _reshape(out, (n, *shape)) if out is not None else None
+        res = hermite_renormalized_batched(A2, b2, c2, shape, stable, out2)
+        return out if out is not None else _reshape(res, batch_shape + shape)
+    if _ndim(A) == 2 and _ndim(b) > 1:
+        batch_shape = _shp(b)[:-1]
+        check_out_shape(batch_shape)
+        n = int(np.prod(batch_shape))
+        b2 = _reshape(b, (n, _shp(b)[-1]))
+        A2 = _broadcast(A, (n, *_shp(A)))
+        c2 = _broadcast(c, (n,))
+        out2 = _reshape(out, (n, *shape)) if out is not None else None
+        res = hermite_renormalized_batched(A2, b2, c2, shape, stable, out2)
+        return out if out is not None else _reshape(res, batch_shape + shape)
+    check_out_shape(())
+    if stable:
+        return stable_numba(shape, A, b, c, out)
+    return vanilla_numba(shape, A, b, c, out)

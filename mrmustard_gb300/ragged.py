@@ -1,0 +1,135 @@
+"""Ragged batches: thousands of triples with their own mode count and cutoffs.
+
+The reference batches only triples that share D and shape
+(mrmustard/math/lattice/strategies/vanilla/batch.py:27-61,
+mrmustard/math/backend_manager.py:683-720); a ragged set is a Python loop of
+``vanilla_numba`` / ``vanilla_vjp_numba`` calls there.  ``RaggedBatch`` plans the set once on
+the host (cost-sorted instance schedule, VJP work items), uploads the plan into a persistent
+device workspace, and then runs the forward / VJP of every instance in a few launches that
+can be captured in one CUDA graph.  Per instance, results equal ``vanilla_numba`` /
+``vanilla_vjp_numba`` of that instance.
+
+A ``RaggedBatch`` owns one workspace: use it from one stream at a time.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .hermite import Workspace, _stream, require_cuda
+from .settings import settings
+
+__all__ = ["RaggedBatch"]
+
+
+class RaggedBatch:
+    def __init__(self, shapes, device=None, team_min_amps: int | None = None, vjp_item_amps: int | None = None):
+        lib = _lib.load()
+        self.device = torch.device(device) if device is not None else require_cuda()
+        self.shapes = [tuple(int(x) for x in s) for s in shapes]
+        self.B = len(self.shapes)
+        self.D = np.array([len(s) for s in self.shapes], np.int32)
+        flat = np.array([x for s in self.shapes for x in s] or [0], np.int64)
+        plan = ctypes.c_void_p()
+        _lib.check(lib.mm_ragged_plan_create(self.B, self.D.ctypes.data, flat.ctypes.data, ctypes.byref(plan)),
+                   "mm_ragged_plan_create")
+        self._plan = plan
+        if team_min_amps is not None or vjp_item_amps is not None:
+            _lib.check(lib.mm_ragged_plan_set_tuning(plan, int(team_min_amps or 0), int(vjp_item_amps or 65536)),
+                       "mm_ragged_plan_set_tuning")
+        self.g_off = np.zeros(self.B, np.int64)
+        self.a_off = np.zeros(self.B, np.int64)
+        self.b_off = np.zeros(self.B, np.int64)
+        _lib.check(lib.mm_ragged_plan_offsets(plan, self.g_off.ctypes.data, self.a_off.ctypes.data,
+                                              self.b_off.ctypes.data), "mm_ragged_plan_offsets")
+        self.sizes = np.array([int(np.prod(s)) for s in self.shapes], np.int64)
+        self.total = int(lib.mm_ragged_plan_amplitudes(plan))
+        self.n_a = int((self.D.astype(np.int64) ** 2).sum())
+        self.n_b = int(self.D.sum())
+        self.ws = Workspace(lib.mm_ragged_plan_workspace_bytes(plan), self.device)
+        _lib.check(lib.mm_ragged_plan_upload(plan, self.ws.ptr, self.ws.nbytes, _stream()), "mm_ragged_plan_upload")
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and plan.value:
+            try:
+                _lib.load().mm_ragged_plan_destroy(plan)
+            except Exception:  # interpreter shutdown
+                pass
+            self._plan = None
+
+    # ------------------------------------------------------------ packing
+    def pack(self, As, bs, cs):
+        """Pack per-instance (A_k, b_k, c_k) into the flat device layout of the plan."""
+        A = np.concatenate([np.asarray(a, np.complex128).reshape(-1) for a in As]) if self.B else np.zeros(0, complex)
+        b = np.concatenate([np.asarray(x, np.complex128).reshape(-1) for x in bs]) if self.B else np.zeros(0, complex)
+        c = np.asarray(cs, np.complex128).reshape(-1)
+        to = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(self.device)  # noqa: E731
+        return to(A), to(b), to(c)
+
+    def unpack(self, G_flat):
+        """Per-instance views of a flat result (tensor or array)."""
+        return [G_flat[o:o + n].reshape(s) for o, n, s in zip(self.g_off, self.sizes, self.shapes)]
+
+    def unpack_grads(self, dA, db):
+        dAs = [dA[o:o + d * d].reshape(d, d) for o, d in zip(self.a_off, self.D)]
+        dbs = [db[o:o + d] for o, d in zip(self.b_off, self.D)]
+        return dAs, dbs
+
+    # ------------------------------------------------------------ compute
+    def _check(self, where):
+        if settings.CHECK_DEVICE_STATUS and not torch.cuda.is_current_stream_capturing():
+            self.ws.check_status(where)
+
+    def forward(self, A, b, c, stable: bool = False, out=None):
+        """Flat G of every instance (device tensor of ``self.total`` complex128)."""
+        lib = _lib.load()
+        G = out if out is not None else torch.empty(self.total, dtype=torch.complex128, device=self.device)
+        _lib.check(lib.mm_ragged_fwd(self._plan, A.data_ptr(), b.data_ptr(), c.data_ptr(), int(bool(stable)),
+                                     G.data_ptr(), self.ws.ptr, self.ws.nbytes, _stream()), "mm_ragged_fwd")
+        self._check("ragged forward")
+        return G
+
+    def vjp(self, G, c, dLdG, out=None):
+        """(dA_flat, db_flat, dc) of every instance (holomorphic VJP, as vanilla_vjp_numba)."""
+        lib = _lib.load()
+        if out is None:
+            dA = torch.empty(self.n_a, dtype=torch.complex128, device=self.device)
+            db = torch.empty(self.n_b, dtype=torch.complex128, device=self.device)
+            dc = torch.empty(self.B, dtype=torch.complex128, device=self.device)
+        else:
+            dA, db, dc = out
+        _lib.check(lib.mm_ragged_vjp(self._plan, G.data_ptr(), c.data_ptr(), dLdG.data_ptr(), dA.data_ptr(),
+                                     db.data_ptr(), dc.data_ptr(), self.ws.ptr, self.ws.nbytes, _stream()),
+                   "mm_ragged_vjp")
+        self._check("ragged vjp")
+        return dA, db, dc
+
+    def capture(self, A, b, c, dLdG, stable: bool = False, warmup: int = 1):
+        """Capture forward + VJP on static buffers into one CUDA graph.
+
+        Returns (graph, G, (dA, db, dc)); ``graph.replay()`` recomputes them from the
+        current contents of A, b, c and dLdG.
+        """
+        G = torch.empty(self.total, dtype=torch.complex128, device=self.device)
+        grads = (torch.empty(self.n_a, dtype=torch.complex128, device=self.device),
+                 torch.empty(self.n_b, dtype=torch.complex128, device=self.device),
+                 torch.empty(self.B, dtype=torch.complex128, device=self.device))
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with settings(CHECK_DEVICE_STATUS=False):
+                for _ in range(warmup):
+                    self.forward(A, b, c, stable, out=G)
+                    self.vjp(G, c, dLdG, out=grads)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with settings(CHECK_DEVICE_STATUS=False):
+            with torch.cuda.graph(g):
+                self.forward(A, b, c, stable, out=G)
+                self.vjp(G, c, dLdG, out=grads)
+        return g, G, grads

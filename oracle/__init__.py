@@ -1,0 +1,222 @@
+"""CPU oracle for the Gaussian->Fock hot path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its CPU-baseline leg and its
+``--impl reference`` arm) may import this package.  The product package
+``mrmustard_gb300`` never does: it has no CPU path at all.
+
+Contents:
+
+* ``hermite_oracle.c`` -- a plain-C restatement of the reference's numba strategies
+  (``mrmustard/math/lattice/strategies/vanilla/{core,batch,gradients}.py``), compiled with gcc
+  (``-ffp-contract=off``, OpenMP over instances as numba's ``prange``).
+* this module -- ctypes bindings with numpy in/out, plus the FP64 CPU oracle of the Fock
+  contraction (numpy ``@``, i.e. BLAS zgemm, as ``ArrayAnsatz.contract`` reaches through
+  ``math.einsum`` -> opt_einsum -> tensordot, mrmustard/physics/ansatz/array_ansatz.py:223 and
+  mrmustard/math/backend_manager.py:526-548).
+
+Parity of the C restatement is pinned against outputs of the reference source itself
+(``tests/golden/hermite_golden.npz``, generated by ``tests/golden/make_golden.py``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "hermite_oracle.c"
+BUILD_DIR = HERE / "_build"
+LIB_PATH = BUILD_DIR / "liboracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the C restatement into ``oracle/_build/liboracle.so`` (OpenMP when available)."""
+    BUILD_DIR.mkdir(exist_ok=True)
+    if LIB_PATH.exists() and not force and LIB_PATH.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB_PATH
+    base = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", str(SRC)]
+    tmp = BUILD_DIR / f"liboracle.{os.getpid()}.so"
+    try:
+        subprocess.run(base + ["-fopenmp", "-o", str(tmp), "-lm"], check=True, capture_output=True)
+    except subprocess.CalledProcessError:
+        subprocess.run(base + ["-o", str(tmp), "-lm"], check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = ctypes.CDLL(str(LIB_PATH))
+        P, I64, I32, D = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
+        cplx = P
+        for name, args in {
+            "oracle_vanilla": [I32, P, P, P, cplx, P],
+            "oracle_stable": [I32, P, P, P, cplx, P],
+            "oracle_vjp": [I32, P, P, cplx, P, P, P, P],
+            "oracle_fwd_batch": [I64, I32, P, P, P, P, I32, P],
+            "oracle_vjp_batch": [I64, I32, P, P, P, P, P, P, P],
+            "oracle_fwd_ragged": [I64, P, P, P, P, P, P, P, P, I32, P, P, P],
+            "oracle_vjp_ragged": [I64, P, P, P, P, P, P, P, P, P, P, P, P, P],
+        }.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L.oracle_num_threads.restype = ctypes.c_int
+        L.oracle_set_numpy_division.argtypes = [ctypes.c_int]
+        L.oracle_set_numpy_division.restype = None
+        del D
+        _lib = L
+    return _lib
+
+
+def _c(x):
+    x = complex(x)
+    return ctypes.cast((ctypes.c_double * 2)(x.real, x.imag), ctypes.c_void_p)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _cc(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def set_numpy_division(on: bool) -> None:
+    """Select numpy's complex/real division (reference source under CPython) instead of numba's."""
+    lib().oracle_set_numpy_division(int(bool(on)))
+
+
+def num_threads() -> int:
+    return int(lib().oracle_num_threads())
+
+
+def vanilla(shape, A, b, c) -> np.ndarray:
+    """``vanilla_numba(shape, A, b, c)`` (core.py:25-124)."""
+    shape = tuple(int(s) for s in shape)
+    A, b = _cc(A), _cc(b)
+    sh = np.array(shape, np.int64)
+    G = np.empty(shape, np.complex128)
+    rc = lib().oracle_vanilla(len(shape), _ptr(sh), _ptr(A), _ptr(b), _c(c), _ptr(G))
+    if rc:
+        raise ValueError(f"oracle_vanilla failed ({rc})")
+    return G
+
+
+def stable(shape, A, b, c) -> np.ndarray:
+    """``stable_numba(shape, A, b, c)`` (core.py:127-213)."""
+    shape = tuple(int(s) for s in shape)
+    A, b = _cc(A), _cc(b)
+    sh = np.array(shape, np.int64)
+    G = np.empty(shape, np.complex128)
+    rc = lib().oracle_stable(len(shape), _ptr(sh), _ptr(A), _ptr(b), _c(c), _ptr(G))
+    if rc:
+        raise ValueError(f"oracle_stable failed ({rc})")
+    return G
+
+
+def vjp(G, c, dLdG):
+    """``vanilla_vjp_numba(G, c, dLdG)`` (gradients.py:25-82) -> (dA, db, dc)."""
+    G, g = _cc(G), _cc(dLdG)
+    D = G.ndim
+    sh = np.array(G.shape, np.int64)
+    dA = np.empty((D, D), np.complex128)
+    db = np.empty(D, np.complex128)
+    dc = np.empty(1, np.complex128)
+    rc = lib().oracle_vjp(D, _ptr(sh), _ptr(G), _c(c), _ptr(g), _ptr(dA), _ptr(db), _ptr(dc))
+    if rc:
+        raise ValueError(f"oracle_vjp failed ({rc})")
+    return dA, db, dc[0]
+
+
+def fwd_batch(shape, A, b, c, stable=False) -> np.ndarray:
+    """``vanilla_batch_numba(shape, A, b, c, stable)`` (batch.py:27-61)."""
+    shape = tuple(int(s) for s in shape)
+    A, b, c = _cc(A), _cc(b), _cc(c)
+    B = A.shape[0]
+    sh = np.array(shape, np.int64)
+    G = np.empty((B, *shape), np.complex128)
+    rc = lib().oracle_fwd_batch(B, len(shape), _ptr(sh), _ptr(A), _ptr(b), _ptr(c), int(bool(stable)), _ptr(G))
+    if rc:
+        raise ValueError(f"oracle_fwd_batch failed ({rc})")
+    return G
+
+
+def vjp_batch(G, c, dLdG):
+    """``vanilla_batch_vjp_numba(G, c, dLdG)`` (gradients.py:85-116)."""
+    G, c, g = _cc(G), _cc(c), _cc(dLdG)
+    B, D = G.shape[0], G.ndim - 1
+    sh = np.array(G.shape[1:], np.int64)
+    dA = np.empty((B, D, D), np.complex128)
+    db = np.empty((B, D), np.complex128)
+    dc = np.empty(B, np.complex128)
+    rc = lib().oracle_vjp_batch(B, D, _ptr(sh), _ptr(G), _ptr(c), _ptr(g), _ptr(dA), _ptr(db), _ptr(dc))
+    if rc:
+        raise ValueError(f"oracle_vjp_batch failed ({rc})")
+    return dA, db, dc
+
+
+class RaggedHost:
+    """Packed host layout of a ragged batch (the same packing the GPU library uses)."""
+
+    def __init__(self, shapes):
+        self.shapes = [tuple(int(s) for s in sh) for sh in shapes]
+        self.B = len(self.shapes)
+        self.D = np.array([len(s) for s in self.shapes], np.int32)
+        self.sizes = np.array([int(np.prod(s)) for s in self.shapes], np.int64)
+        self.flat_shapes = np.array([x for s in self.shapes for x in s], np.int64)
+        self.shape_off = np.concatenate([[0], np.cumsum(self.D)[:-1]]).astype(np.int64)
+        self.a_off = np.concatenate([[0], np.cumsum(self.D.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+        self.b_off = self.shape_off.copy()
+        self.g_off = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
+        self.total = int(self.sizes.sum())
+        self.order = np.argsort(-self.sizes * (self.D + 1), kind="stable").astype(np.int64)
+
+
+def fwd_ragged(rh: RaggedHost, A, b, c, stable=False, out=None, indices=None):
+    """Per-instance loop of ``vanilla_numba`` over a packed ragged batch (OpenMP over instances)."""
+    A, b, c = _cc(A), _cc(b), _cc(c)
+    G = np.empty(rh.total, np.complex128) if out is None else out
+    order = rh.order if indices is None else np.ascontiguousarray(indices, np.int64)
+    rc = lib().oracle_fwd_ragged(len(order), _ptr(rh.D), _ptr(rh.flat_shapes), _ptr(rh.shape_off), _ptr(A),
+                                 _ptr(rh.a_off), _ptr(b), _ptr(rh.b_off), _ptr(c), int(bool(stable)), _ptr(G),
+                                 _ptr(rh.g_off), _ptr(order))
+    if rc:
+        raise ValueError(f"oracle_fwd_ragged failed ({rc})")
+    return G
+
+
+def vjp_ragged(rh: RaggedHost, G, c, dLdG, indices=None):
+    """Per-instance loop of ``vanilla_vjp_numba`` over a packed ragged batch."""
+    G, c, g = _cc(G), _cc(c), _cc(dLdG)
+    dA = np.zeros(int((rh.D.astype(np.int64) ** 2).sum()), np.complex128)
+    db = np.zeros(int(rh.D.sum()), np.complex128)
+    dc = np.zeros(rh.B, np.complex128)
+    order = rh.order if indices is None else np.ascontiguousarray(indices, np.int64)
+    rc = lib().oracle_vjp_ragged(len(order), _ptr(rh.D), _ptr(rh.flat_shapes), _ptr(rh.shape_off), _ptr(G),
+                                 _ptr(rh.g_off), _ptr(c), _ptr(g), _ptr(dA), _ptr(rh.a_off), _ptr(db),
+                                 _ptr(rh.b_off), _ptr(dc), _ptr(order))
+    if rc:
+        raise ValueError(f"oracle_vjp_ragged failed ({rc})")
+    return dA, db, dc
+
+
+def fock_gemm(U, B):
+    """FP64 CPU oracle of the Fock contraction C = U @ B (numpy -> BLAS zgemm)."""
+    return np.asarray(U, np.complex128) @ np.asarray(B, np.complex128)
+
+
+def rel_err(x, ref) -> float:
+    """max|x - ref| / max|ref| (the per-instance error metric used throughout the tests)."""
+    x, ref = np.asarray(x), np.asarray(ref)
+    den = np.abs(ref).max() if ref.size else 0.0
+    return float(np.abs(x - ref).max() / den) if den > 0 else float(np.abs(x - ref).max() if x.size else 0.0)

@@ -1,0 +1,395 @@
+"""GPU parity of the Hermite hot path: the CUDA library (through its C ABI, via the package's
+ctypes layer) against the reference's own outputs (golden fixtures) and the CPU oracle.
+
+Tolerances (max|x - ref| / max|ref| per instance, the metric of the reference's recurrence whose
+amplitudes span tens of decades):
+  * forward, well-conditioned triples: 1e-13;
+  * forward, the 4-index density-matrix triple at cutoff 50 (error grows along the recurrence in
+    the reference itself): 1e-12;
+  * VJP (sums of up to millions of products, tree-ordered on the GPU, sequential in numba): 1e-12.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import mrmustard_gb300 as mm
+from conftest import golden_cases
+from mrmustard_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL = 1e-13
+FWD_TOL_ILL = 1e-12
+VJP_TOL = 1e-12
+
+
+def rel(x, ref):
+    x = x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x)
+    ref = np.asarray(ref)
+    den = np.abs(ref).max()
+    return float(np.abs(x - ref).max() / den) if den > 0 else float(np.abs(x).max())
+
+
+def takagi(D, smax, seed, sigma=0.3):
+    from scipy.stats import unitary_group
+
+    rng = np.random.default_rng(seed)
+    Q = unitary_group.rvs(D, random_state=seed) if D > 1 else np.exp(1j * rng.uniform(0, 2 * np.pi, (1, 1)))
+    s = rng.uniform(0, smax, D)
+    A = (Q * s) @ Q.T
+    b = sigma * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+    return A, b, 1.0 + 0j
+
+
+def dm_triple(D, norm, seed, sigma=0.3):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((D, D)) + 1j * rng.standard_normal((D, D))
+    A = X + X.T
+    A *= norm / np.linalg.norm(A, 2)
+    b = sigma * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+    return A, b, 1.0 + 0j
+
+
+def cn(shape, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+# ---------------------------------------------------------------- golden fixtures
+def test_golden_forward(golden, cuda):
+    for n in golden_cases(golden, ("G", "G_stable")):
+        sh = tuple(golden[f"{n}/shape"])
+        A, b, c = golden[f"{n}/A"], golden[f"{n}/b"], golden[f"{n}/c"]
+        G = mm.vanilla_numba(sh, A, b, c)
+        assert G.shape == sh and G.dtype == np.complex128
+        if n != "dgate":  # vanilla diverges there in the reference too
+            assert rel(G, golden[f"{n}/G"]) < FWD_TOL, n
+        assert rel(mm.stable_numba(sh, A, b, c), golden[f"{n}/G_stable"]) < FWD_TOL, n
+
+
+def test_golden_vjp(golden, cuda):
+    for n in golden_cases(golden, ("dA",)):
+        dA, db, dc = mm.vanilla_vjp_numba(golden[f"{n}/G"], golden[f"{n}/c"], golden[f"{n}/dLdG"])
+        assert rel(dA, golden[f"{n}/dA"]) < VJP_TOL, n
+        assert rel(db, golden[f"{n}/db"]) < VJP_TOL, n
+        assert abs(dc - golden[f"{n}/dc"]) <= VJP_TOL * max(1.0, abs(golden[f"{n}/dc"])), n
+
+
+def test_golden_batch(golden, cuda):
+    sh = tuple(golden["batch/shape"])
+    A, b, c = golden["batch/A"], golden["batch/b"], golden["batch/c"]
+    assert rel(mm.vanilla_batch_numba(sh, A, b, c), golden["batch/G"]) < FWD_TOL
+    assert rel(mm.vanilla_batch_numba(sh, A, b, c, True), golden["batch/G_stable"]) < FWD_TOL
+    dA, db, dc = mm.vanilla_batch_vjp_numba(golden["batch/G"], c, golden["batch/dLdG"])
+    assert rel(dA, golden["batch/dA"]) < VJP_TOL
+    assert rel(db, golden["batch/db"]) < VJP_TOL
+    assert rel(dc, golden["batch/dc"]) < VJP_TOL
+
+
+def test_known_answer_1d(golden, cuda):
+    from scipy.special import eval_hermite, factorial
+
+    x = golden["kat1d/x"]
+    expected = np.array([eval_hermite(i, x) / np.sqrt(factorial(i)) for i in range(5)]).T
+    got = np.array([mm.hermite_renormalized(-2 * np.ones((1, 1)), 2 * np.array([x0]), 1, (5,)) for x0 in x])
+    np.testing.assert_allclose(got, expected, atol=1e-12)
+
+
+def test_stable_dgate_displacement(golden, cuda):
+    G = mm.stable_numba((60, 60), golden["dgate/A"], golden["dgate/b"], golden["dgate/c"])
+    assert np.allclose(G, golden["dgate/displacement"])
+
+
+def test_stable_dgate_1000(cuda, oracle_lib):
+    """test_lattice_functions.py:141-152 at full size: stable Dgate(4+4j) at 1000x1000."""
+    alpha = 4 + 4j
+    A = np.array([[0, 1], [1, 0]], complex)
+    b = np.array([alpha, -np.conj(alpha)])
+    c = np.exp(-abs(alpha) ** 2 / 2)
+    with mm.settings(STABLE_FOCK_CONVERSION=True):
+        G = mm.hermite_renormalized(A, b, c, (1000, 1000))
+    ref = oracle_lib.stable((1000, 1000), A, b, c)
+    assert rel(G, ref) < 1e-12
+    r, phi = 4.0, 2.0
+    A = np.array([[-np.exp(1j * phi) * np.tanh(r), 1 / np.cosh(r)], [1 / np.cosh(r), np.exp(-1j * phi) * np.tanh(r)]])
+    with mm.settings(STABLE_FOCK_CONVERSION=True):
+        S = mm.hermite_renormalized(A, np.zeros(2), 1 / np.sqrt(np.cosh(r)), (1000, 1000))
+    assert np.max(np.abs(S)) < 1
+
+
+# ---------------------------------------------------------------- configs
+def test_cfg1_plain(cuda, oracle_lib):
+    A, b, c = takagi(3, 0.8, 101)
+    G = mm.vanilla_numba((20, 20, 20), A, b, c)
+    ref = oracle_lib.vanilla((20, 20, 20), A, b, c)
+    assert G.shape == (20, 20, 20)
+    assert rel(G, ref) < FWD_TOL
+
+
+@pytest.mark.parametrize("case", ["pure40", "dm50"])
+def test_cfg2_large_single(cuda, oracle_lib, case):
+    if case == "pure40":
+        A, b, c = takagi(4, 0.85, 202)
+        shape, tol = (40,) * 4, FWD_TOL
+    else:
+        A, b, c = dm_triple(4, 0.89, 203)
+        shape, tol = (50,) * 4, FWD_TOL_ILL
+    Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
+                       torch.tensor(c, dtype=torch.complex128, device=cuda), shape)
+    assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < tol
+
+
+def test_stable_large_single(cuda, oracle_lib):
+    A, b, c = takagi(4, 0.85, 204)
+    shape = (24,) * 4
+    G = mm.stable_numba(shape, A, b, c)
+    assert rel(G, oracle_lib.stable(shape, A, b, c)) < FWD_TOL
+
+
+def test_vjp_cfg4_vs_oracle(cuda, oracle_lib):
+    A, b, c = takagi(4, 0.8, 303)
+    shape = (30,) * 4
+    G = oracle_lib.vanilla(shape, A, b, c)
+    g = cn(shape, 304)
+    ref = oracle_lib.vjp(G, c, g)
+    got = mm.vanilla_vjp_numba(G, c, g)
+    assert rel(got[0], ref[0]) < VJP_TOL
+    assert rel(got[1], ref[1]) < VJP_TOL
+    assert abs(got[2] - ref[2]) <= VJP_TOL * abs(ref[2])
+
+
+def test_vjp_central_differences(cuda):
+    """dA, db, dc vs central finite differences (h = 1e-6) of L = sum(dLdG * G) (holomorphic)."""
+    A, b, c = takagi(3, 0.8, 305)
+    c = 0.9 + 0.2j
+    shape = (6, 5, 7)
+    g = cn(shape, 306)
+    G = mm.vanilla_numba(shape, A, b, c)
+    dA, db, dc = mm.vanilla_vjp_numba(G, c, g)
+    L = lambda A_, b_, c_: np.sum(g * mm.vanilla_numba(shape, A_, b_, c_))  # noqa: E731
+    h = 1e-6
+    for i in range(3):
+        e = np.zeros(3)
+        e[i] = h
+        fd = (L(A, b + e, c) - L(A, b - e, c)) / (2 * h)
+        assert abs(fd - db[i]) < 1e-6 * max(1, abs(fd))
+        for j in range(3):
+            E = np.zeros((3, 3))
+            E[i, j] = h
+            fdij = (L(A + E, b, c) - L(A - E, b, c)) / (2 * h)
+            E = np.zeros((3, 3))
+            E[j, i] = h
+            fdji = (L(A + E, b, c) - L(A - E, b, c)) / (2 * h)
+            assert abs((fdij + fdji) / 2 - dA[i, j]) < 1e-6 * max(1, abs(fdij))
+    fdc = (L(A, b, c + h) - L(A, b, c - h)) / (2 * h)
+    assert abs(fdc - dc) < 1e-6 * max(1, abs(fdc))
+
+
+# ---------------------------------------------------------------- facade (test_vanilla.py:164-238)
+def _rt(n, batch=(), seed=673):
+    rng = np.random.RandomState(seed)
+    A = rng.random((*batch, n, n)) + 1j * rng.random((*batch, n, n))
+    A = A + np.swapaxes(A, -1, -2)
+    A /= np.abs(np.linalg.eigvals(A)).max() + 0.2
+    b = rng.random((*batch, n)) + 1j * rng.random((*batch, n))
+    c = rng.random(batch) + 1j * rng.random(batch)
+    return A, b, c
+
+
+@pytest.mark.parametrize("stable", [True, False])
+def test_facade_unbatched_and_out(cuda, stable):
+    A, b, c = _rt(2)
+    G = mm.hermite_renormalized(A, b, c, (3, 3), stable=stable)
+    assert G.shape == (3, 3)
+    out = np.zeros((3, 3), complex)
+    G2 = mm.hermite_renormalized(A, b, c, (3, 3), stable=stable, out=out)
+    assert G2 is out
+    assert np.allclose(G2, G)
+
+
+@pytest.mark.parametrize("stable", [True, False])
+def test_facade_b_batched(cuda, stable):
+    A, b, c = _rt(2, (2, 1))
+    G = mm.hermite_renormalized(A[0, 0], b, c[0, 0], (4, 5), stable=stable)
+    assert G.shape == (2, 1, 4, 5)
+    assert np.allclose(G[0, 0], mm.hermite_renormalized(A[0, 0], b[0, 0], c[0, 0], (4, 5)))
+    assert np.allclose(G[1, 0], mm.hermite_renormalized(A[0, 0], b[1, 0], c[0, 0], (4, 5)))
+    out = np.zeros((2, 1, 4, 5), complex)
+    G2 = mm.hermite_renormalized(A[0, 0], b, c[0, 0], (4, 5), stable=stable, out=out)
+    assert np.allclose(G2, G) and np.allclose(out, G)
+
+
+@pytest.mark.parametrize("stable", [True, False])
+def test_facade_fully_batched(cuda, stable):
+    A, b, c = _rt(2, (2, 1))
+    G = mm.hermite_renormalized(A, b, c, (4, 5), stable=stable)
+    assert G.shape == (2, 1, 4, 5)
+    assert np.allclose(G[1, 0], mm.hermite_renormalized(A[1, 0], b[1, 0], c[1, 0], (4, 5)))
+    out = np.zeros((2, 1, 4, 5), complex)
+    mm.hermite_renormalized(A, b, c, (4, 5), stable=stable, out=out)
+    assert np.allclose(out, G)
+
+
+def test_device_tensors_stay_on_device(cuda, oracle_lib):
+    A, b, c = takagi(3, 0.7, 401)
+    At, bt = torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda)
+    ct = torch.tensor(c, dtype=torch.complex128, device=cuda)
+    G = mm.vanilla_numba((8, 9, 10), At, bt, ct)
+    assert isinstance(G, torch.Tensor) and G.is_cuda
+    assert rel(G, oracle_lib.vanilla((8, 9, 10), A, b, c)) < FWD_TOL
+    out = torch.full((8, 9, 10), float("nan"), dtype=torch.complex128, device=cuda)
+    G2 = mm.vanilla_numba((8, 9, 10), At, bt, ct, out=out)
+    assert G2 is out and not torch.isnan(out).any()
+
+
+def test_poisoned_output_fully_overwritten(cuda, oracle_lib):
+    for D, shape in [(1, (9,)), (2, (1, 6)), (3, (4, 1, 5)), (4, (3, 4, 2, 5))]:
+        A, b, c = takagi(D, 0.7, 500 + D)
+        for stable in (False, True):
+            out = torch.full(shape, complex(float("nan"), float("nan")), dtype=torch.complex128, device=cuda)
+            mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
+                          torch.tensor(c, dtype=torch.complex128, device=cuda), shape, stable, out=out)
+            assert not torch.isnan(out).any()
+            ref = (oracle_lib.stable if stable else oracle_lib.vanilla)(shape, A, b, c)
+            assert rel(out, ref) < FWD_TOL
+
+
+@pytest.mark.parametrize("D", [5, 6, 7, 8])
+def test_many_modes(cuda, oracle_lib, D):
+    A, b, c = takagi(D, 0.8, 600 + D)
+    shape = tuple([3, 2, 4, 2, 3, 2, 2, 3][:D])
+    assert rel(mm.vanilla_numba(shape, A, b, c), oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
+    assert rel(mm.stable_numba(shape, A, b, c), oracle_lib.stable(shape, A, b, c)) < FWD_TOL
+    G = oracle_lib.vanilla(shape, A, b, c)
+    g = cn(shape, 700 + D)
+    ref = oracle_lib.vjp(G, c, g)
+    got = mm.vanilla_vjp_numba(G, c, g)
+    assert rel(got[0], ref[0]) < VJP_TOL and rel(got[1], ref[1]) < VJP_TOL
+
+
+def test_too_many_modes_raises(cuda):
+    with pytest.raises(_lib.MMError, match="UNSUPPORTED"):
+        mm.vanilla_numba((2,) * 9, np.zeros((9, 9)), np.zeros(9), 1.0)
+
+
+# ---------------------------------------------------------------- ragged batch
+def _ragged_case(n, seed, cmax=12):
+    rng = np.random.default_rng(seed)
+    shapes, As, bs = [], [], []
+    for k in range(n):
+        D = int(rng.integers(1, 5))
+        shapes.append(tuple(int(x) for x in rng.integers(1, cmax + 1, D)))
+        A, b, _ = takagi(D, 0.8, seed * 100000 + k)
+        As.append(A)
+        bs.append(b)
+    cs = np.exp(1j * rng.uniform(0, 2 * np.pi, n)) * rng.uniform(0.5, 1.0, n)
+    return shapes, As, bs, cs
+
+
+def test_ragged_forward_vjp_parity(cuda, oracle_lib):
+    shapes, As, bs, cs = _ragged_case(300, 7)
+    rb = mm.RaggedBatch(shapes)
+    A, b, c = rb.pack(As, bs, cs)
+    for stable in (False, True):
+        G = rb.forward(A, b, c, stable=stable).cpu().numpy()
+        for k, Gk in enumerate(rb.unpack(G)):
+            ref = (oracle_lib.stable if stable else oracle_lib.vanilla)(shapes[k], As[k], bs[k], cs[k])
+            assert rel(Gk, ref) < FWD_TOL, (k, shapes[k], stable)
+    G = rb.forward(A, b, c)
+    g = torch.as_tensor(cn(rb.total, 9), device=cuda)
+    dA, db, dc = rb.vjp(G, c, g)
+    dAs, dbs = rb.unpack_grads(dA.cpu().numpy(), db.cpu().numpy())
+    Gs, gs = rb.unpack(G.cpu().numpy()), rb.unpack(g.cpu().numpy())
+    dc = dc.cpu().numpy()
+    for k in range(len(shapes)):
+        rA, rb_, rc = oracle_lib.vjp(Gs[k], cs[k], gs[k])
+        assert rel(dAs[k], rA) < VJP_TOL, k
+        assert rel(dbs[k], rb_) < VJP_TOL, k
+        assert abs(dc[k] - rc) <= VJP_TOL * max(1.0, abs(rc)), k
+
+
+def test_ragged_graph_replay(cuda, oracle_lib):
+    shapes, As, bs, cs = _ragged_case(64, 11, cmax=10)
+    rb = mm.RaggedBatch(shapes)
+    A, b, c = rb.pack(As, bs, cs)
+    g = torch.as_tensor(cn(rb.total, 12), device=cuda)
+    graph, G, (dA, db, dc) = rb.capture(A, b, c, g)
+    G_e = rb.forward(A, b, c).clone()
+    grads_e = [t.clone() for t in rb.vjp(G_e, c, g)]
+    A2, b2, c2 = rb.pack([a * 0.9 for a in As], [x * 1.1 for x in bs], cs)
+    A.copy_(A2)
+    b.copy_(b2)
+    graph.replay()
+    torch.cuda.synchronize()
+    for k, Gk in enumerate(rb.unpack(G.cpu().numpy())):
+        assert rel(Gk, oracle_lib.vanilla(shapes[k], As[k] * 0.9, bs[k] * 1.1, cs[k])) < FWD_TOL
+    A.copy_(rb.pack(As, bs, cs)[0])
+    b.copy_(rb.pack(As, bs, cs)[1])
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(G, G_e)
+    for t, e in zip((dA, db, dc), grads_e):
+        assert torch.equal(t, e)  # deterministic reductions: bitwise reproducible
+
+
+# ---------------------------------------------------------------- autograd
+def test_autograd_matches_finite_differences(cuda):
+    A, b, _ = takagi(3, 0.7, 801)
+    c = 0.8 + 0.1j
+    shape = (7, 6, 5)
+    T = torch.as_tensor(cn(shape, 802), device=cuda)
+    T = T / T.abs().pow(2).sum().sqrt()
+
+    def loss(A_, b_, c_):
+        G = mm.hermite_renormalized_autograd(A_, b_, c_, shape)
+        ov = (T.conj() * G).sum()
+        return 1 - ov.abs() ** 2 / (G.abs() ** 2).sum()
+
+    At = torch.tensor(A, device=cuda, requires_grad=True)
+    bt = torch.tensor(b, device=cuda, requires_grad=True)
+    ct = torch.tensor(c, dtype=torch.complex128, device=cuda, requires_grad=True)
+    loss(At, bt, ct).backward()
+    h = 1e-6
+    with torch.no_grad():
+        for i in range(3):
+            for part in (1.0, 1j):
+                e = torch.zeros(3, dtype=torch.complex128, device=cuda)
+                e[i] = h * part
+                fd = (loss(At, bt + e, ct) - loss(At, bt - e, ct)).item() / (2 * h)
+                got = bt.grad[i].real if part == 1.0 else bt.grad[i].imag
+                assert abs(fd - got.item()) < 1e-6
+            E = torch.zeros(3, 3, dtype=torch.complex128, device=cuda)
+            E[i, (i + 1) % 3] = h
+            E[(i + 1) % 3, i] = h
+            fd = (loss(At + E, bt, ct) - loss(At - E, bt, ct)).item() / (2 * h)
+            got = (At.grad[i, (i + 1) % 3] + At.grad[(i + 1) % 3, i]).real.item()
+            assert abs(fd - got) < 1e-6
+        fd = (loss(At, bt, ct + h) - loss(At, bt, ct - h)).item() / (2 * h)
+        assert abs(fd - ct.grad.real.item()) < 1e-6
+
+
+# ---------------------------------------------------------------- failure handling
+def test_bounded_wait_times_out_without_fault(cuda):
+    """A grid barrier that can never complete gives up after its budget and records
+    MM_ERR_WAIT_TIMEOUT in the workspace status word; the context stays usable."""
+    lib = _lib.load()
+    ws = torch.zeros(4096, dtype=torch.uint8, device=cuda)
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.mm_workspace_init(ws.data_ptr(), 4096, st) == 0
+    assert lib.mm_test_wait_timeout(ws.data_ptr(), 4096, 20_000_000, st) == 0
+    status = ctypes.c_int(-1)
+    assert lib.mm_workspace_status(ws.data_ptr(), st, ctypes.byref(status)) == 0
+    assert status.value == 5
+    G = mm.vanilla_numba((5, 5), np.eye(2) * 0.1, np.ones(2) * 0.2, 1.0)  # still works
+    assert np.isfinite(G).all()
+
+
+def test_launch_count_increments(cuda):
+    n0 = mm.launch_count()
+    mm.vanilla_numba((4, 4), np.eye(2) * 0.1, np.ones(2) * 0.2, 1.0)
+    assert mm.launch_count() >= n0 + 2

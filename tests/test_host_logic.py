@@ -1,0 +1,43 @@
+"""Host-side logic of the facade (mirrors backend_manager.py:643-727 argument checks) and of
+instance sharding.  These raise before any device work, so they run on the CPU."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import mrmustard_gb300 as mm
+from mrmustard_gb300 import shard
+
+
+def test_out_too_small_raises():
+    A, b, c = np.zeros((2, 2)), np.zeros(2), 1.0
+    with pytest.raises(ValueError, match="too large for out.shape"):
+        mm.hermite_renormalized(A, b, c, (4, 5), out=np.zeros((3, 5), complex))
+
+
+def test_batch_mismatch_raises():
+    A = np.zeros((3, 2, 2))
+    b = np.zeros((2, 2))
+    c = np.zeros(3)
+    with pytest.raises(ValueError, match="b.shape"):
+        mm.hermite_renormalized(A, b, c, (3, 3))
+    with pytest.raises(ValueError, match="c.shape"):
+        mm.hermite_renormalized(A, np.zeros((3, 2)), np.zeros(2), (3, 3))
+
+
+def test_settings_context():
+    assert mm.settings.STABLE_FOCK_CONVERSION is False
+    with mm.settings(STABLE_FOCK_CONVERSION=True):
+        assert mm.settings.STABLE_FOCK_CONVERSION is True
+    assert mm.settings.STABLE_FOCK_CONVERSION is False
+
+
+def test_shard_balances_cost():
+    rng = np.random.default_rng(0)
+    costs = rng.integers(1, 1000, 500)
+    parts = shard.shard_instances(costs, 4)
+    assert sorted(i for p in parts for i in p) == list(range(500))
+    loads = [costs[p].sum() for p in parts]
+    assert max(loads) - min(loads) <= costs.max()
+    assert shard.shard_instances(costs, 1)[0] == list(range(500))

@@ -1,0 +1,102 @@
+"""Pin the CPU oracle (oracle/hermite_oracle.c) against outputs of the reference source itself.
+
+tests/golden/hermite_golden.npz was produced by tests/golden/make_golden.py, which runs the
+reference's own vanilla/{core,batch,gradients}.py and displacement.py unmodified.  Under
+CPython the reference divides complex by real with numpy's reciprocal-multiply; with that
+lowering selected the oracle must reproduce the fixtures bit for bit.  With numba's lowering
+(true division, the default) it must agree to a few ulps.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+from scipy.special import eval_hermite, factorial
+
+from conftest import golden_cases
+
+import oracle
+
+
+@pytest.fixture(autouse=True)
+def _built():
+    oracle.build()
+    yield
+    oracle.set_numpy_division(False)
+
+
+def test_forward_bit_exact_numpy_division(golden):
+    oracle.set_numpy_division(True)
+    for n in golden_cases(golden, ("G", "G_stable")):
+        sh = tuple(golden[f"{n}/shape"])
+        A, b, c = golden[f"{n}/A"], golden[f"{n}/b"], golden[f"{n}/c"]
+        assert np.array_equal(oracle.vanilla(sh, A, b, c), golden[f"{n}/G"]), n
+        assert np.array_equal(oracle.stable(sh, A, b, c), golden[f"{n}/G_stable"]), n
+
+
+def test_forward_numba_division_within_ulps(golden):
+    for n in golden_cases(golden, ("G", "G_stable")):
+        if n == "dgate":  # vanilla is unstable there (amplitudes ~1e7): only stable is meaningful
+            continue
+        sh = tuple(golden[f"{n}/shape"])
+        A, b, c = golden[f"{n}/A"], golden[f"{n}/b"], golden[f"{n}/c"]
+        assert oracle.rel_err(oracle.vanilla(sh, A, b, c), golden[f"{n}/G"]) < 1e-15, n
+        assert oracle.rel_err(oracle.stable(sh, A, b, c), golden[f"{n}/G_stable"]) < 1e-15, n
+
+
+def test_vjp_matches_reference(golden):
+    for n in golden_cases(golden, ("dA",)):
+        G, c, g = golden[f"{n}/G"], golden[f"{n}/c"], golden[f"{n}/dLdG"]
+        dA, db, dc = oracle.vjp(G, c, g)
+        # the fixture's sum(G*dLdG) is numpy's pairwise sum; the oracle's is numba's sequential one
+        assert oracle.rel_err(dA, golden[f"{n}/dA"]) < 1e-14, n
+        assert oracle.rel_err(db, golden[f"{n}/db"]) < 1e-14, n
+        assert abs(dc - golden[f"{n}/dc"]) <= 1e-13 * max(1.0, abs(golden[f"{n}/dc"])), n
+
+
+def test_batch_matches_reference(golden):
+    sh = tuple(golden["batch/shape"])
+    oracle.set_numpy_division(True)
+    G = oracle.fwd_batch(sh, golden["batch/A"], golden["batch/b"], golden["batch/c"])
+    assert np.array_equal(G, golden["batch/G"])
+    Gs = oracle.fwd_batch(sh, golden["batch/A"], golden["batch/b"], golden["batch/c"], stable=True)
+    assert np.array_equal(Gs, golden["batch/G_stable"])
+    dA, db, dc = oracle.vjp_batch(golden["batch/G"], golden["batch/c"], golden["batch/dLdG"])
+    assert oracle.rel_err(dA, golden["batch/dA"]) < 1e-14
+    assert oracle.rel_err(db, golden["batch/db"]) < 1e-14
+    assert oracle.rel_err(dc, golden["batch/dc"]) < 1e-14
+
+
+def test_known_answer_hermite_1d(golden):
+    """tests/test_math/test_special.py:23-36: 1-D values are He-polynomials / sqrt(n!)."""
+    x = golden["kat1d/x"]
+    expected = np.array([eval_hermite(i, x) / np.sqrt(factorial(i)) for i in range(5)]).T
+    np.testing.assert_allclose(golden["kat1d/G"], expected, atol=1e-12)
+    got = np.array([oracle.vanilla((5,), -2 * np.ones((1, 1)), 2 * np.array([x0]), 1.0) for x0 in x])
+    np.testing.assert_allclose(got, expected, atol=1e-12)
+
+
+def test_stable_dgate_matches_displacement(golden):
+    """test_lattice_functions.py:141-152 at 60x60: stable == closed-form displacement."""
+    G = oracle.stable((60, 60), golden["dgate/A"], golden["dgate/b"], golden["dgate/c"])
+    assert np.allclose(G, golden["dgate/displacement"])
+
+
+def test_ragged_oracle_equals_per_instance(golden):
+    shapes = [tuple(golden[f"ragged{k}/shape"]) for k in range(7)]
+    rh = oracle.RaggedHost(shapes)
+    As = [golden[f"ragged{k}/A"] for k in range(7)]
+    bs = [golden[f"ragged{k}/b"] for k in range(7)]
+    cs = np.array([golden[f"ragged{k}/c"] for k in range(7)])
+    G = oracle.fwd_ragged(rh, np.concatenate([a.ravel() for a in As]), np.concatenate(bs), cs)
+    for k in range(7):
+        o, n = rh.g_off[k], rh.sizes[k]
+        assert np.array_equal(G[o:o + n].reshape(shapes[k]), oracle.vanilla(shapes[k], As[k], bs[k], cs[k]))
+    dA, db, dc = oracle.vjp_ragged(rh, G, cs, G.conj())
+    for k in range(7):
+        rA, rb, rc = oracle.vjp(G[rh.g_off[k]:rh.g_off[k] + rh.sizes[k]].reshape(shapes[k]), cs[k],
+                                G[rh.g_off[k]:rh.g_off[k] + rh.sizes[k]].conj().reshape(shapes[k]))
+        D = len(shapes[k])
+        assert np.array_equal(dA[rh.a_off[k]:rh.a_off[k] + D * D].reshape(D, D), rA)
+        assert np.array_equal(db[rh.b_off[k]:rh.b_off[k] + D], rb)
+        assert dc[k] == rc
