@@ -159,6 +159,17 @@ MM_API int mm_ragged_vjp(const mm_ragged_plan *plan, const mm_c128 *G, const mm_
 /* ------------------------------------------------------------- diagnostics */
 
 /*
+ * Device self-test of the kernels' instance views: builds the per-instance
+ * view of a one-shape batch and of a ragged batch on the device exactly as the
+ * compute kernels do and compares every field with the host's values; *nbad
+ * receives the number of mismatching fields (0 = pass).  Reads and writes only
+ * the first 8 KiB of ws (at least that many bytes are required); synchronises
+ * `stream`.  The Python layer runs it once per device before any compute call.
+ * (No counterpart in the reference.)
+ */
+MM_API int mm_selftest(void *ws, size_t ws_bytes, mm_stream_t stream, int *nbad);
+
+/*
  * Launch a two-CTA cooperative kernel whose grid barrier can never complete,
  * so that its bounded wait gives up after budget_ns and records
  * MM_ERR_WAIT_TIMEOUT in the workspace status word.  Used by the tests of the

@@ -36,7 +36,7 @@ class HermiteRenormalizedFn(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad):
         G, c = ctx.saved_tensors
-        dA, db, dc = device_vjp(G, c, grad.conj().contiguous(), ctx.batched)
+        dA, db, dc = device_vjp(G, c, grad.conj(), ctx.batched)  # device_vjp materialises the conj view
         return dA.conj(), db.conj(), dc.conj().reshape(ctx.c_shape), None, None
 
 

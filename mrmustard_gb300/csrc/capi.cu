@@ -593,6 +593,88 @@ int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c
 }
 
 // ---------------------------------------------------------------- diagnostics
+int mm_selftest(void* ws, size_t ws_bytes, mm_stream_t stream, int* nbad) {
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  if (!nbad) return MM_ERR_INVALID_ARG;
+  if ((rc = check_ws(ws, ws_bytes, 8192))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  const int64_t shape[3] = {12, 10, 11};
+  UniformPlan P;
+  if ((rc = plan_uniform(2, 3, shape, P, di.sms))) return rc;
+  // real addresses inside the workspace; only c is ever read by the kernel
+  double2* A = reinterpret_cast<double2*>(w + 512);
+  double2* b = reinterpret_cast<double2*>(w + 1024);
+  double2* c = reinterpret_cast<double2*>(w + 1280);
+  double2* G = reinterpret_cast<double2*>(w + 1536);
+  double2* dLdG = reinterpret_cast<double2*>(w + 1792);
+  double2* coef = reinterpret_cast<double2*>(w + 2048);
+  InstDesc* desc = reinterpret_cast<InstDesc*>(w + 4096);
+  InstView* expect = reinterpret_cast<InstView*>(w + 4608);
+  int32_t* bad = reinterpret_cast<int32_t*>(w + 5120);
+  int32_t* order = reinterpret_cast<int32_t*>(w + 5632);
+  const double2 cv[2] = {make_double2(0.25, -0.5), make_double2(-1.5, 2.75)};
+  MM_CUDA(cudaMemcpyAsync(c, cv, sizeof(cv), cudaMemcpyHostToDevice, st));
+  int total_bad = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    InstView e;
+    memset(&e, 0, sizeof(e));
+    const int64_t k = pass == 0 ? 1 : 0;
+    if (pass == 0) {
+      UniformSrc src = uniform_src(P, A, b, c, G, dLdG, w);
+      src.coef = coef;
+      e.g = P.g;
+      e.A = A + 9;
+      e.b = b + 3;
+      e.c = cv[1];
+      e.G = G + P.g.n;
+      e.dLdG = dLdG + P.g.n;
+      e.coef = coef + coef_entries(P.g);
+      MM_CUDA(cudaMemcpyAsync(expect, &e, sizeof(e), cudaMemcpyHostToDevice, st));
+      view_selftest_kernel<UniformSrc><<<1, 32, 0, st>>>(src, k, expect, bad);
+    } else {
+      InstDesc d;
+      memset(&d, 0, sizeof(d));
+      const int64_t shape2[4] = {3, 1, 4, 2};
+      if ((rc = make_geom(4, shape2, d.g))) return rc;
+      d.g_off = 5;
+      d.a_off = 7;
+      d.b_off = 2;
+      d.coef_off = 11;
+      MM_CUDA(cudaMemcpyAsync(desc, &d, sizeof(d), cudaMemcpyHostToDevice, st));
+      RaggedSrc src;
+      memset(&src, 0, sizeof(src));
+      src.desc = desc;
+      src.order = order;
+      src.B = 1;
+      src.A = A;
+      src.b = b;
+      src.c = c;
+      src.G = G;
+      src.dLdG = dLdG;
+      src.coef = coef;
+      e.g = d.g;
+      e.A = A + 7;
+      e.b = b + 2;
+      e.c = cv[0];
+      e.G = G + 5;
+      e.dLdG = dLdG + 5;
+      e.coef = coef + 11;
+      MM_CUDA(cudaMemcpyAsync(expect, &e, sizeof(e), cudaMemcpyHostToDevice, st));
+      view_selftest_kernel<RaggedSrc><<<1, 32, 0, st>>>(src, k, expect, bad);
+    }
+    MM_LAUNCHED();
+    int32_t hb = -1;
+    MM_CUDA(cudaMemcpyAsync(&hb, bad, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    MM_CUDA(cudaStreamSynchronize(st));
+    total_bad += hb;
+  }
+  *nbad = total_bad;
+  return MM_OK;
+}
+
 int mm_test_wait_timeout(void* ws, size_t ws_bytes, uint64_t budget_ns, mm_stream_t stream) {
   DevInfo di;
   int rc = device_info(di);
@@ -608,5 +690,30 @@ int mm_test_wait_timeout(void* ws, size_t ws_bytes, uint64_t budget_ns, mm_strea
   g_launches.fetch_add(1);
   return MM_OK;
 }
+
+#ifdef MM_DEVICE_CHECKS
+// Debug builds only: this runtime's view of a device pointer, and a copy-engine read of it.
+MM_API int mm_debug_ptr_attr(const void* p, int* type, int* device) {
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    cudaGetLastError();
+    return MM_ERR_CUDA;
+  }
+  *type = (int)a.type;
+  *device = a.device;
+  return MM_OK;
+}
+MM_API int mm_debug_read_bytes(const void* dev, void* host, size_t n) {
+  MM_CUDA(cudaMemcpy(host, dev, n, cudaMemcpyDeviceToHost));
+  return MM_OK;
+}
+// Debug builds only: copy the first recorded access violation (8 words) to host memory.
+MM_API int mm_debug_read(unsigned long long* out8) {
+  MM_CUDA(cudaMemcpyFromSymbol(out8, mm::mm_dbg_word, 8 * sizeof(unsigned long long)));
+  return MM_OK;
+}
+#endif
 
 }  // extern "C"

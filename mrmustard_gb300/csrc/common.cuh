@@ -120,6 +120,7 @@ __device__ __forceinline__ void set_status(WsHeader* h, int code) {
   atomicExch(&h->abort, 1);
 }
 
+#if defined(__CUDA_ARCH__)
 __device__ __forceinline__ uint64_t globaltimer_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -136,12 +137,17 @@ __device__ __forceinline__ int32_t ld_relaxed_i32(const int32_t* p) {
   asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+#else  // host compilation of the device code (CPU emulation of the kernels' indexing)
+__device__ __forceinline__ uint64_t globaltimer_ns() { return 0; }
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
+__device__ __forceinline__ int32_t ld_relaxed_i32(const int32_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+#endif
 
 // Progress signal for waits: a CTA that works alone while the others wait at a
 // barrier bumps the heartbeat, which restarts their timeout.
@@ -185,6 +191,33 @@ __device__ __forceinline__ bool grid_barrier(WsHeader* h, uint32_t epoch, uint64
   __syncthreads();
   return s_ok != 0;
 }
+
+// ---------------------------------------------------------------- debug checks
+// Built with -DMM_DEVICE_CHECKS (MM_DEVICE_CHECKS=1 in the environment of the
+// build), every global access of the recurrence kernels first checks its
+// address for alignment and for lying inside the buffer it belongs to; the
+// first violation is recorded in mm_dbg_word (tag, address, base, elements,
+// alignment) and the access is skipped.  Without the define the checks vanish.
+#ifdef MM_DEVICE_CHECKS
+static __device__ unsigned long long mm_dbg_word[8];
+__device__ __forceinline__ bool dbg_ok(const void* p, const void* base, long long n_elems, int esize, int align,
+                                       int tag) {
+  const unsigned long long a = (unsigned long long)p, b0 = (unsigned long long)base;
+  const bool ok = (a % (unsigned long long)align) == 0 && a >= b0 &&
+                  a + (unsigned long long)esize <= b0 + (unsigned long long)n_elems * (unsigned long long)esize;
+  if (!ok && atomicAdd(&mm_dbg_word[0], 1ull) == 0ull) {
+    mm_dbg_word[1] = (unsigned long long)tag;
+    mm_dbg_word[2] = a;
+    mm_dbg_word[3] = b0;
+    mm_dbg_word[4] = (unsigned long long)n_elems;
+    mm_dbg_word[5] = (unsigned long long)align;
+  }
+  return ok;
+}
+#define MM_CHK(p, base, n, T, tag) (::mm::dbg_ok((const void*)(p), (const void*)(base), (long long)(n), (int)sizeof(T), (int)alignof(T), (tag)))
+#else
+#define MM_CHK(p, base, n, T, tag) (true)
+#endif
 
 // Row-major multi-index decomposition helpers (32-bit: chunk sizes are < 2^31).
 template <int D>

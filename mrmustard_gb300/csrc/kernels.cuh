@@ -40,6 +40,27 @@ struct InstView {
   const double2* coef;
 };
 
+// Field-by-field geometry copy.  Views are never built by whole-struct
+// assignment: with nvcc 13.0 for sm_103a, building a view in a local struct
+// (geometry memcpy'd from the kernel-parameter struct, pointers stored after
+// it) and then assigning the whole struct to shared memory was compiled into a
+// byte copy of the parameter struct itself, so the view's pointer fields
+// received the parameter struct's unrelated fields.  Writing every field
+// straight into its destination avoids that transformation; mm_selftest checks
+// the result on the device before any kernel dereferences a view.
+__device__ __forceinline__ void copy_geom(Geom& d, const Geom& s) {
+  d.D = s.D;
+  d.maxC = s.maxC;
+  d.n = s.n;
+  d.sumC = s.sumC;
+#pragma unroll
+  for (int j = 0; j < MM_MAXD; ++j) {
+    d.shape[j] = s.shape[j];
+    d.strides[j] = s.strides[j];
+    d.prefC[j] = s.prefC[j];
+  }
+}
+
 struct VjpItem {
   int32_t inst;
   uint32_t q0;
@@ -63,7 +84,7 @@ struct UniformSrc {
   __device__ __forceinline__ int64_t n_inst() const { return B; }
   __device__ __forceinline__ int64_t sched(int64_t t) const { return t; }
   __device__ __forceinline__ void load(int64_t k, InstView& v) const {
-    v.g = g;
+    copy_geom(v.g, g);
     v.A = A + k * g.D * g.D;
     v.b = b + k * g.D;
     v.c = c[k];
@@ -104,7 +125,7 @@ struct RaggedSrc {
   __device__ __forceinline__ int64_t sched(int64_t t) const { return order[t]; }
   __device__ __forceinline__ void load(int64_t k, InstView& v) const {
     const InstDesc& d = desc[k];
-    v.g = d.g;
+    copy_geom(v.g, d.g);
     v.A = A + d.a_off;
     v.b = b + d.b_off;
     v.c = c[k];
@@ -134,7 +155,19 @@ __device__ __forceinline__ double2 ldG(const double2* p) {
   else return *p;
 }
 
-__device__ __forceinline__ void load_view_to_smem(InstView* sv, const InstView& v) { *sv = v; }
+// Checked forms of the recurrence's accesses (plain accesses unless MM_DEVICE_CHECKS).
+template <bool CG>
+__device__ __forceinline__ double2 ldGc(const InstView& v, const double2* p, int tag) {
+  if (!MM_CHK(p, v.G, v.g.n, double2, tag)) return cmk(0.0, 0.0);
+  return ldG<CG>(p);
+}
+__device__ __forceinline__ double2 ldCoef(const InstView& v, const double2* p, int tag) {
+  if (!MM_CHK(p, v.coef, coef_entries(v.g), double2, tag)) return cmk(0.0, 0.0);
+  return *p;
+}
+__device__ __forceinline__ void stG(const InstView& v, int64_t f, double2 x, int tag) {
+  if (MM_CHK(v.G + f, v.G, v.g.n, double2, tag)) v.G[f] = x;
+}
 
 // ============================================================== setup kernel
 // Scalar tables (grid-strided) and each instance's coefficient block (one CTA
@@ -145,6 +178,7 @@ __global__ void __launch_bounds__(256) setup_kernel(Src src, double* sq, double*
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = gtid; k < kmax; k += gstride) {
+    if (!MM_CHK(hh + k, sq, 3 * kmax, double, 11)) continue;
     const double s = sqrt((double)k);
     sq[k] = s;
     rs[k] = k > 0 ? 1.0 / s : 0.0;
@@ -163,7 +197,7 @@ __global__ void __launch_bounds__(256) setup_kernel(Src src, double* sq, double*
       int j = 0;
       while (j + 1 < g.D && g.prefC[j + 1] <= r) ++j;
       const int32_t kk = r - g.prefC[j];
-      const double2 a = v.A[i * g.D + j];
+      const double2 a = MM_CHK(v.A + i * g.D + j, v.A, g.D * g.D, double2, 9) ? v.A[i * g.D + j] : cmk(0.0, 0.0);
       double2 val;
       if (j == i) {  // cd[i][m] = A_ii * sqrt(m - 1) (zero at m = 0, 1)
         const double s = kk >= 1 ? sqrt((double)(kk - 1)) : 0.0;
@@ -172,7 +206,7 @@ __global__ void __launch_bounds__(256) setup_kernel(Src src, double* sq, double*
         const double s = sqrt((double)kk);
         val = cmk(a.x * s, a.y * s);
       }
-      coef[e] = val;
+      if (MM_CHK(coef + e, coef, total, double2, 10)) coef[e] = val;
     }
   }
 }
@@ -185,11 +219,11 @@ __device__ __forceinline__ void fwd_chunk(const InstView& v, const double* __res
                                           uint32_t q_begin, uint32_t q_end, uint32_t q_step, uint32_t t) {
   const Geom& g = v.g;
   const int64_t si = g.strides[i];
-  const double2 bi = __ldg(v.b + i);
+  const double2 bi = MM_CHK(v.b + i, v.b, g.D, double2, 1) ? __ldg(v.b + i) : cmk(0.0, 0.0);
   const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
-  const double2 cd = (m >= 2) ? crow[g.prefC[i] + m] : cmk(0.0, 0.0);
-  const double rsm = rs[m];
-  double2* G = v.G;
+  const double2 cd = (m >= 2) ? ldCoef(v, crow + g.prefC[i] + m, 2) : cmk(0.0, 0.0);
+  const double rsm = MM_CHK(rs + m, rs, g.maxC + 1, double, 3) ? rs[m] : 0.0;
+  const double2* G = v.G;
   const int64_t base = (int64_t)m * si;
   int64_t sj[D];
   int32_t pj[D];
@@ -203,20 +237,20 @@ __device__ __forceinline__ void fwd_chunk(const InstView& v, const double* __res
     decompose<D>(q, i + 1, g, k);
     const int64_t f = base + q;
     const int64_t p = f - si;
-    double2 acc = cmul(bi, ldG<CG>(G + p));
-    if (m >= 2) acc = cfma(cd, ldG<CG>(G + p - si), acc);
+    double2 acc = cmul(bi, ldGc<CG>(v, G + p, 4));
+    if (m >= 2) acc = cfma(cd, ldGc<CG>(v, G + p - si, 4), acc);
 #pragma unroll
     for (int j = 1; j < D; ++j) {
-      if (j > i && k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + p - sj[j]), acc);
+      if (j > i && k[j] > 0) acc = cfma(ldCoef(v, crow + pj[j] + k[j], 5), ldGc<CG>(v, G + p - sj[j], 4), acc);
     }
-    G[f] = cscale(rsm, acc);
+    stG(v, f, cscale(rsm, acc), 6);
   }
 }
 
 // Whole instance on one CTA (chunks separated by __syncthreads).
 template <int D>
 __device__ void fwd_instance_cta(const InstView& v, const double* rs) {
-  if (threadIdx.x == 0) v.G[0] = v.c;
+  if (threadIdx.x == 0) stG(v, 0, v.c, 7);
   __syncthreads();
   for (int i = D - 1; i >= 0; --i) {
     const int Ci = (int)v.g.shape[i];
@@ -302,11 +336,7 @@ template <int DLO, int DHI, class Src>
 __global__ void __launch_bounds__(MM_BLOCK) fwd_cta_kernel(Src src, const double* __restrict__ rs, int stable) {
   __shared__ InstView sv;
   const int64_t k = src.sched(blockIdx.x);
-  if (threadIdx.x == 0) {
-    InstView v;
-    src.load(k, v);
-    sv = v;
-  }
+  if (threadIdx.x == 0) src.load(k, sv);
   __syncthreads();
   const int D = sv.g.D;
 #define MM_FWD_CASE(DD)                                        \
@@ -336,11 +366,7 @@ template <int D>
 __global__ void __launch_bounds__(512) fwd_grid_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
                                                        uint32_t small_chunk, uint64_t budget_ns, int stable) {
   __shared__ InstView sv;
-  if (threadIdx.x == 0) {
-    InstView v;
-    src.load(0, v);
-    sv = v;
-  }
+  if (threadIdx.x == 0) src.load(0, sv);
   __syncthreads();
   const Geom& g = sv.g;
   uint32_t epoch = 0;
@@ -382,6 +408,30 @@ __global__ void __launch_bounds__(512) fwd_grid_kernel(UniformSrc src, const dou
       stable_wave<D, true>(sv, rs, w, lo, hi, blockDim.x, threadIdx.x);
       if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
     }
+  }
+}
+
+// Device self-test of view construction: load instance k of `src` into a
+// shared view exactly as the compute kernels do and compare every field with
+// the host's expectation.  Only `src.c[k]` (a valid workspace address) is read.
+template <class Src>
+__global__ void view_selftest_kernel(Src src, int64_t k, const InstView* __restrict__ expect, int32_t* bad) {
+  __shared__ InstView sv;
+  if (threadIdx.x == 0) src.load(k, sv);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const InstView& e = *expect;
+    int nbad = 0;
+    nbad += sv.A != e.A;
+    nbad += sv.b != e.b;
+    nbad += sv.G != e.G;
+    nbad += sv.dLdG != e.dLdG;
+    nbad += sv.coef != e.coef;
+    nbad += sv.c.x != e.c.x || sv.c.y != e.c.y;
+    nbad += sv.g.D != e.g.D || sv.g.maxC != e.g.maxC || sv.g.n != e.g.n || sv.g.sumC != e.g.sumC;
+    for (int j = 0; j < MM_MAXD; ++j)
+      nbad += sv.g.shape[j] != e.g.shape[j] || sv.g.strides[j] != e.g.strides[j] || sv.g.prefC[j] != e.g.prefC[j];
+    *bad = nbad;
   }
 }
 
@@ -491,9 +541,7 @@ __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, 
     int64_t k;
     uint32_t q0, q1;
     src.item(item, k, q0, q1);
-    InstView v;
-    src.load(k, v);
-    sv = v;
+    src.load(k, sv);
     sq0 = q0;
     sq1 = q1;
   }

@@ -51,6 +51,33 @@ def require_cuda() -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
+_SELFTESTED: set[int] = set()
+
+
+def ensure_device_ready(device) -> None:
+    """Run the library's device self-test once per device (raises if it fails)."""
+    idx = torch.device(device).index
+    idx = torch.cuda.current_device() if idx is None else idx
+    if idx in _SELFTESTED:
+        return
+    lib = _lib.load()
+    with torch.cuda.device(idx):
+        buf = torch.zeros(8192, dtype=torch.uint8, device=torch.device("cuda", idx))
+        nbad = ctypes.c_int(-1)
+        _lib.check(lib.mm_selftest(buf.data_ptr(), 8192, torch.cuda.current_stream().cuda_stream, ctypes.byref(nbad)),
+                   "mm_selftest")
+    if nbad.value != 0:
+        raise RuntimeError(f"libmm_gb300 device self-test failed ({nbad.value} view fields wrong): "
+                           "the kernels were mis-compiled for this GPU; refusing to run them")
+    _SELFTESTED.add(idx)
+
+
+def raw(t: torch.Tensor) -> torch.Tensor:
+    """Materialised, contiguous storage of a tensor (torch's lazy conj/neg bits resolved),
+    so that its data pointer holds exactly its values."""
+    return t.resolve_conj().resolve_neg().contiguous()
+
+
 def _is_dev(x) -> bool:
     return isinstance(x, torch.Tensor) and x.is_cuda
 
@@ -60,7 +87,7 @@ def _to_dev(x, device) -> torch.Tensor:
         t = x.detach()
         if t.dtype != torch.complex128:
             t = t.to(torch.complex128)
-        return t.to(device).contiguous()
+        return raw(t.to(device))
     a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
     return torch.from_numpy(a).to(device)
 
@@ -83,6 +110,7 @@ class Workspace:
 
     def __init__(self, nbytes: int, device):
         lib = _lib.load()
+        ensure_device_ready(device)
         self.nbytes = max(int(nbytes), 512)
         self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
         _lib.check(lib.mm_workspace_init(self.ptr, self.nbytes, _stream()), "mm_workspace_init")
@@ -109,6 +137,7 @@ def device_fwd(A: torch.Tensor, b: torch.Tensor, c: torch.Tensor, shape, stable:
                out: torch.Tensor | None = None) -> torch.Tensor:
     """Forward on device tensors.  A: (B,D,D) or (D,D); b: (B,D) or (D,); c: (B,) or ()."""
     lib = _lib.load()
+    A, b, c = raw(A), raw(b), raw(c)
     batched = A.dim() == 3
     shape, sh = _shape_arr(shape)
     D = len(shape)
@@ -138,6 +167,7 @@ def device_fwd(A: torch.Tensor, b: torch.Tensor, c: torch.Tensor, shape, stable:
 def device_vjp(G: torch.Tensor, c: torch.Tensor, dLdG: torch.Tensor, batched: bool):
     """VJP on device tensors; returns (dA, db, dc) on the device."""
     lib = _lib.load()
+    G, c, dLdG = raw(G), raw(c), raw(dLdG)
     shape = tuple(G.shape[1:]) if batched else tuple(G.shape)
     shape, sh = _shape_arr(shape)
     D = len(shape)

@@ -20,7 +20,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .hermite import Workspace, _stream, require_cuda
+from .hermite import Workspace, _stream, raw, require_cuda
 from .settings import settings
 
 __all__ = ["RaggedBatch"]
@@ -88,6 +88,7 @@ class RaggedBatch:
     def forward(self, A, b, c, stable: bool = False, out=None):
         """Flat G of every instance (device tensor of ``self.total`` complex128)."""
         lib = _lib.load()
+        A, b, c = raw(A), raw(b), raw(c)
         G = out if out is not None else torch.empty(self.total, dtype=torch.complex128, device=self.device)
         _lib.check(lib.mm_ragged_fwd(self._plan, A.data_ptr(), b.data_ptr(), c.data_ptr(), int(bool(stable)),
                                      G.data_ptr(), self.ws.ptr, self.ws.nbytes, _stream()), "mm_ragged_fwd")
@@ -97,6 +98,7 @@ class RaggedBatch:
     def vjp(self, G, c, dLdG, out=None):
         """(dA_flat, db_flat, dc) of every instance (holomorphic VJP, as vanilla_vjp_numba)."""
         lib = _lib.load()
+        G, c, dLdG = raw(G), raw(c), raw(dLdG)
         if out is None:
             dA = torch.empty(self.n_a, dtype=torch.complex128, device=self.device)
             db = torch.empty(self.n_b, dtype=torch.complex128, device=self.device)

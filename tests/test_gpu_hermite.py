@@ -61,15 +61,31 @@ def cn(shape, seed):
 
 
 # ---------------------------------------------------------------- golden fixtures
-def test_golden_forward(golden, cuda):
+def reference_sensitivity(oracle_lib, fn, shape, A, b, c):
+    """How far the reference's own result moves when only its complex/real division is lowered
+    differently (numba's true division vs numpy's reciprocal multiply): one ulp per division.
+    For ill-conditioned triples this, not 1e-13, is the resolution at which the reference is
+    defined."""
+    oracle_lib.set_numpy_division(True)
+    try:
+        x = fn(shape, A, b, c)
+    finally:
+        oracle_lib.set_numpy_division(False)
+    return rel(fn(shape, A, b, c), x)
+
+
+def test_golden_forward(golden, cuda, oracle_lib):
     for n in golden_cases(golden, ("G", "G_stable")):
         sh = tuple(golden[f"{n}/shape"])
         A, b, c = golden[f"{n}/A"], golden[f"{n}/b"], golden[f"{n}/c"]
         G = mm.vanilla_numba(sh, A, b, c)
         assert G.shape == sh and G.dtype == np.complex128
-        if n != "dgate":  # vanilla diverges there in the reference too
+        if n != "dgate":  # vanilla diverges there in the reference too (|G| ~ 1e7)
             assert rel(G, golden[f"{n}/G"]) < FWD_TOL, n
-        assert rel(mm.stable_numba(sh, A, b, c), golden[f"{n}/G_stable"]) < FWD_TOL, n
+        tol = FWD_TOL
+        if n == "dgate":  # stable Dgate(4+4j): the reference moves by 2.4e-11 under one-ulp changes
+            tol = max(FWD_TOL, 10 * reference_sensitivity(oracle_lib, oracle_lib.stable, sh, A, b, c))
+        assert rel(mm.stable_numba(sh, A, b, c), golden[f"{n}/G_stable"]) < tol, n
 
 
 def test_golden_vjp(golden, cuda):
@@ -100,6 +116,22 @@ def test_known_answer_1d(golden, cuda):
     np.testing.assert_allclose(got, expected, atol=1e-12)
 
 
+def test_conj_views_are_materialised(cuda, oracle_lib):
+    """Tensors carrying torch's lazy conjugation bit must reach the kernels conjugated."""
+    A, b, c = takagi(2, 0.6, 901)
+    shape = (6, 7)
+    G = oracle_lib.vanilla(shape, A, b, c)
+    g = cn(shape, 902)
+    ref = oracle_lib.vjp(G, c, g)
+    gt = torch.as_tensor(g.conj(), device=cuda).conj()  # conj view whose values equal g
+    assert gt.is_conj()
+    got = mm.vanilla_vjp_numba(torch.as_tensor(G, device=cuda), torch.tensor(c, device=cuda), gt)
+    assert rel(got[1], ref[1]) < VJP_TOL
+    bt = torch.as_tensor(b.conj(), device=cuda).conj()
+    Gd = mm.vanilla_numba(shape, torch.as_tensor(A, device=cuda), bt, torch.tensor(c, device=cuda))
+    assert rel(Gd, G) < FWD_TOL
+
+
 def test_stable_dgate_displacement(golden, cuda):
     G = mm.stable_numba((60, 60), golden["dgate/A"], golden["dgate/b"], golden["dgate/c"])
     assert np.allclose(G, golden["dgate/displacement"])
@@ -114,7 +146,9 @@ def test_stable_dgate_1000(cuda, oracle_lib):
     with mm.settings(STABLE_FOCK_CONVERSION=True):
         G = mm.hermite_renormalized(A, b, c, (1000, 1000))
     ref = oracle_lib.stable((1000, 1000), A, b, c)
-    assert rel(G, ref) < 1e-12
+    # the reference itself moves by ~2.7e-9 here under one-ulp changes of its division
+    tol = 10 * reference_sensitivity(oracle_lib, oracle_lib.stable, (1000, 1000), A, b, c)
+    assert rel(G, ref) < max(tol, 1e-12)
     r, phi = 4.0, 2.0
     A = np.array([[-np.exp(1j * phi) * np.tanh(r), 1 / np.cosh(r)], [1 / np.cosh(r), np.exp(-1j * phi) * np.tanh(r)]])
     with mm.settings(STABLE_FOCK_CONVERSION=True):
