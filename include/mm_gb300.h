@@ -116,6 +116,27 @@ MM_API int mm_hermite_vjp_batched(int64_t B, int D, const int64_t *shape, const 
                            const mm_c128 *dLdG, mm_c128 *dA, mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes,
                            mm_stream_t stream);
 
+/*
+ * mm_hermite_vjp without a workspace argument: the same kernels and results,
+ * for callers that cannot allocate device memory when they call (for example a
+ * custom-call handler inside another framework's runtime, which owns all
+ * device memory and the stream, so a cudaMalloc there would synchronise the
+ * device or escape the framework's memory accounting).  No counterpart in the
+ * reference.
+ *  - Scratch is a 2 MiB array in the library's device memory, held by every
+ *    GPU that loads the library until the process exits; shapes whose scratch
+ *    (sqrt tables + per-work-item partial sums) does not fit return
+ *    MM_ERR_TOO_LARGE.  Nothing is allocated by the call.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current); make that first call
+ *    before any stream capture.
+ *  - Every call uses the same array, so calls whose work overlaps on the GPU
+ *    (other streams, other host threads) race: issue them in order on one
+ *    stream.  The status word of the array is zeroed by each call.
+ */
+MM_API int mm_hermite_vjp_noalloc(int D, const int64_t *shape, const mm_c128 *G, const mm_c128 *c,
+                                  const mm_c128 *dLdG, mm_c128 *dA, mm_c128 *db, mm_c128 *dc, mm_stream_t stream);
+
 /* ------------------------------------------------------------ ragged batches */
 
 /*

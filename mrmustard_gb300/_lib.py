@@ -44,6 +44,7 @@ SIGNATURES = {
     "mm_hermite_fwd_batched": (I32, [I64, I32, P, P, P, P, I32, P, P, SZ, P]),
     "mm_hermite_vjp": (I32, [I32, P, P, P, P, P, P, P, P, SZ, P]),
     "mm_hermite_vjp_batched": (I32, [I64, I32, P, P, P, P, P, P, P, P, SZ, P]),
+    "mm_hermite_vjp_noalloc": (I32, [I32, P, P, P, P, P, P, P, P]),
     "mm_ragged_plan_create": (I32, [I64, P, P, ctypes.POINTER(P)]),
     "mm_ragged_plan_destroy": (None, [P]),
     "mm_ragged_plan_workspace_bytes": (SZ, [P]),

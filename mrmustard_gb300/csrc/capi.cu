@@ -592,6 +592,45 @@ int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c
   return launch_vjp_reduce(src, plan->B, partials, (double2*)dA, (double2*)db, (double2*)dc, st);
 }
 
+// ------------------------------------------------------- VJP without a workspace
+// Scratch of mm_hermite_vjp_noalloc: 2 MiB of device memory in this library's
+// module, present on every GPU that loads the library until the process exits.
+#define MM_NOALLOC_SCRATCH_BYTES (2u << 20)
+static __device__ __align__(256) unsigned char g_vjp_scratch[MM_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_vjp_scratch for the current device, looked up once per
+// device (cudaGetSymbolAddress, with that device current) and cached.
+static int noalloc_scratch(void** out) {
+  static std::mutex mu;
+  static void* addr[64] = {};
+  int dev = 0;
+  MM_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return MM_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(mu);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    MM_CUDA(cudaGetSymbolAddress(&p, g_vjp_scratch));
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return MM_OK;
+}
+
+int mm_hermite_vjp_noalloc(int D, const int64_t* shape, const mm_c128* G, const mm_c128* c, const mm_c128* dLdG,
+                           mm_c128* dA, mm_c128* db, mm_c128* dc, mm_stream_t stream) {
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  UniformPlan P;
+  if ((rc = plan_uniform(1, D, shape, P, di.sms))) return rc;
+  if (P.L.total > MM_NOALLOC_SCRATCH_BYTES) return MM_ERR_TOO_LARGE;
+  void* ws = nullptr;
+  if ((rc = noalloc_scratch(&ws))) return rc;
+  // the status word is the only scratch content read before it is written
+  MM_CUDA(cudaMemsetAsync(ws, 0, sizeof(WsHeader), (cudaStream_t)stream));
+  return mm_hermite_vjp(D, shape, G, c, dLdG, dA, db, dc, ws, MM_NOALLOC_SCRATCH_BYTES, stream);
+}
+
 // ---------------------------------------------------------------- diagnostics
 int mm_selftest(void* ws, size_t ws_bytes, mm_stream_t stream, int* nbad) {
   DevInfo di;
