@@ -34,7 +34,7 @@ N_INST = 4096
 
 
 # ------------------------------------------------------------------ workload
-def make_workload(base_seed: int, n: int = N_INST):
+def make_workload(base_seed: int, n: int = N_INST):  # noqa: C901
     """Per-instance seeded triples: (shapes, As, bs, cs)."""
     from scipy.stats import unitary_group
 
@@ -152,7 +152,7 @@ def run_reference(args, rank, world):
     import oracle
 
     oracle.build()
-    shapes, As, bs, cs = make_workload(20260000)
+    shapes, As, bs, cs = make_workload(20260000, args.instances)
     rh = oracle.RaggedHost(shapes)
     A = np.concatenate([a.ravel() for a in As])
     b = np.concatenate(bs)
@@ -179,14 +179,15 @@ def run_reference(args, rank, world):
         times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
     value = amps / t
-    sample = (f"{len(idx)} of {N_INST} instances ({amps} of {rh.total} amplitudes), fwd+VJP per step"
-              if len(idx) < N_INST else f"all {N_INST} instances ({amps} amplitudes), fwd+VJP per step")
+    sample = (f"{len(idx)} of {len(shapes)} instances ({amps} of {rh.total} amplitudes), fwd+VJP per step"
+              if len(idx) < len(shapes) else f"all {len(shapes)} instances ({amps} amplitudes), fwd+VJP per step")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": "ragged batch: 4096 triples, D~U{1..4}, cutoff~U{5..40}, Takagi A s~U(0,0.8), "
-                               "b sigma 0.3, c=1, fwd+VJP", "instances": N_INST, "amplitudes": int(rh.total)},
+        "config": {"workload": f"ragged batch: {len(shapes)} triples, D~U{{1..4}}, cutoff~U{{5..40}}, Takagi A "
+                               "s~U(0,0.8), b sigma 0.3, c=1, fwd+VJP", "instances": len(shapes),
+                   "amplitudes": int(rh.total)},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -214,7 +215,7 @@ def run_gb300(args, rank, local_rank, world):
     stream = torch.cuda.current_stream(dev)
 
     # --- workload (weak scaling: every rank its own 4096 triples)
-    shapes, As, bs, cs = make_workload(20260000 + rank * N_INST)
+    shapes, As, bs, cs = make_workload(20260000 + rank * N_INST, args.instances)
     rb = mm.RaggedBatch(shapes, device=dev)
     A, b, c = rb.pack(As, bs, cs)
     gen = torch.Generator(device=dev)
@@ -324,6 +325,55 @@ def run_gb300(args, rank, local_rank, world):
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get(dom)
 
+    extras = {}
+    if args.skip_extras:
+        e2e_ms, h2d, d2h, plain_value, cpu = float("nan"), 0, 0, float("nan"), None
+    else:
+        e2e_ms, h2d, d2h, plain_value, cpu, extras = run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads,
+                                                                shapes, As, bs, cs, time_eager)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": f"ragged batch: {len(shapes)} triples, D~U{{1..4}}, cutoff~U{{5..40}}, Takagi A "
+                                   "s~U(0,0.8), b sigma 0.3, c=1, fwd+VJP (one CUDA graph replay per step)",
+                       "instances": len(shapes), "amplitudes": total,
+                       "l2": "inputs larger than L2 (G, dLdG ~4.4 GB each)",
+                       "parallelism": f"replicas x{world} (instances independent)"},
+            "e2e": {"value": total * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": bytes_dom, "ms_per_launch": t_dom,
+                         "fp64": {"achieved_dfma_per_s": ops_dom / (t_dom * 1e-3), "peak_dfma_per_s": dfma_peak,
+                                  "frac": ops_dom / (t_dom * 1e-3) / dfma_peak,
+                                  "peak_kind": "measured (mm_probe_dfma)"}},
+            "kernels_ms": {"forward": t_fwd, "vjp": t_vjp},
+            "plain_loop": {"value": plain_value, "unit": UNIT, "sample": "256 instances, device_fwd + device_vjp per "
+                           "instance", "batched_over_plain": value / world / plain_value},
+            "max_rel_err_vs_oracle": max_err,
+            "clocks": clocks,
+        }
+        line.update(extras)
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs, cs, time_eager):
+    """e2e with host copies, the per-instance loop, the CPU oracle, single-instance and contraction figures."""
+    import torch
+
+    import mrmustard_gb300 as mm
+
+    stream = torch.cuda.current_stream(dev)
+    total = rb.total
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
     # --- e2e through the public API with pinned host buffers
     A_h = A.cpu().pin_memory()
     b_h = b.cpu().pin_memory()
@@ -365,7 +415,7 @@ def run_gb300(args, rank, local_rank, world):
 
     # --- plain per-instance GPU path on a sample of instances (scaled to amplitudes/s)
     rng = np.random.default_rng(11)
-    sample = rng.choice(len(shapes), 256, replace=False)
+    sample = rng.choice(len(shapes), min(256, len(shapes)), replace=False)
     dev_inputs = [(torch.as_tensor(As[k], device=dev), torch.as_tensor(bs[k], device=dev),
                    torch.tensor(cs[k], device=dev), g[rb.g_off[k]:rb.g_off[k] + rb.sizes[k]].reshape(shapes[k]))
                   for k in sample]
@@ -395,38 +445,61 @@ def run_gb300(args, rank, local_rank, world):
         oracle.vjp_ragged(rh, G_np, cs, g_np)
         tc = time.perf_counter() - t0
         cpu = {"value": total / tc, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-               "sample": f"all {N_INST} instances ({total} amplitudes), one fwd+VJP pass, {tc:.2f} s"}
+               "sample": f"all {len(shapes)} instances ({total} amplitudes), one fwd+VJP pass, {tc:.2f} s"}
 
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": "ragged batch: 4096 triples, D~U{1..4}, cutoff~U{5..40}, Takagi A s~U(0,0.8), "
-                                   "b sigma 0.3, c=1, fwd+VJP (one CUDA graph replay per step)",
-                       "instances": N_INST, "amplitudes": total, "l2": "inputs larger than L2 (G, dLdG ~4.4 GB each)",
-                       "parallelism": f"replicas x{world} (instances independent)"},
-            "e2e": {"value": total * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-            "gpu_launches": launches_per_step * args.steps,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": bytes_dom, "ms_per_launch": t_dom,
-                         "fp64": {"achieved_dfma_per_s": ops_dom / (t_dom * 1e-3), "peak_dfma_per_s": dfma_peak,
-                                  "frac": ops_dom / (t_dom * 1e-3) / dfma_peak,
-                                  "peak_kind": "measured (mm_probe_dfma)"}},
-            "kernels_ms": {"forward": t_fwd, "vjp": t_vjp},
-            "plain_loop": {"value": plain_value, "unit": UNIT, "sample": f"{len(sample)} instances, "
-                           "device_fwd + device_vjp per instance", "batched_over_plain": value / world / plain_value},
-            "max_rel_err_vs_oracle": max_err,
-            "clocks": clocks,
-        }
-        if cpu is not None:
-            line["cpu_baseline"] = cpu
-        print(json.dumps(line), flush=True)
-    if pg is not None:
-        pg.destroy_process_group()
-    return 0
+    extras = {}
+    # --- single large recurrences (4 modes at cutoff 40, pure; 4-index DM triple at cutoff 50): one
+    #     instance on the whole GPU
+    single = {}
+    for name, D, cut, kind in (("pure_4x40", 4, 40, "pure"), ("dm_4x50", 4, 50, "dm")):
+        rng = np.random.default_rng(4242 + cut)
+        if kind == "pure":
+            from scipy.stats import unitary_group
+
+            Q = unitary_group.rvs(D, random_state=rng)
+            A1 = (Q * rng.uniform(0, 0.85, D)) @ Q.T
+        else:
+            X1 = rng.standard_normal((D, D)) + 1j * rng.standard_normal((D, D))
+            A1 = X1 + X1.T
+            A1 *= 0.89 / np.linalg.norm(A1, 2)
+        b1 = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+        At, bt = torch.as_tensor(A1, device=dev), torch.as_tensor(b1, device=dev)
+        ct = torch.tensor(1.0 + 0j, device=dev)
+        out = torch.empty((cut,) * D, dtype=torch.complex128, device=dev)
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            t1 = time_eager(lambda: mm.device_fwd(At, bt, ct, (cut,) * D, out=out), reps=5)
+        n1 = cut ** D
+        single[name] = {"amplitudes": n1, "ms": t1, "amplitudes_per_s": n1 / (t1 * 1e-3),
+                        "hbm_gbs": 16.0 * n1 / (t1 * 1e-3) / 1e9}
+    extras["single_instance_forward"] = single
+
+    # --- Fock contraction: 2-mode gate tensor at cutoff 50 (2500 x 2500) on 256 kets
+    rng = np.random.default_rng(55)
+    X5 = rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))
+    A5 = X5 + X5.T
+    A5 *= 0.95 / np.linalg.norm(A5, 2)
+    b5 = 0.3 * (rng.standard_normal(4) + 1j * rng.standard_normal(4)) / np.sqrt(2)
+    U5 = mm.device_fwd(torch.as_tensor(A5, device=dev), torch.as_tensor(b5, device=dev),
+                       torch.tensor(1.0 + 0j, device=dev), (50, 50, 50, 50)).reshape(2500, 2500)
+    kets = torch.complex(torch.randn(256, 2500, dtype=torch.float64, device=dev),
+                         torch.randn(256, 2500, dtype=torch.float64, device=dev))
+    kets = kets / kets.abs().pow(2).sum(1, keepdim=True).sqrt()
+    Xk = kets.T.contiguous()
+    U5h, Xkh = U5.cpu().numpy(), Xk.cpu().numpy()
+    t0 = time.perf_counter()
+    ref5 = U5h @ Xkh
+    t_np = time.perf_counter() - t0
+    flops = 8.0 * 2500 * 256 * 2500
+    contraction = {"shape": "2500x2500 @ 2500x256 complex128", "flops": flops,
+                   "numpy_zgemm_ms": t_np * 1e3}
+    for mode in ("fp64", "ozaki"):
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            tm = time_eager(lambda: mm.fock_gemm(U5, Xk, mode), reps=5)
+        Y = mm.fock_gemm(U5, Xk, mode).cpu().numpy()
+        err = float(np.abs(Y - ref5).max() / np.abs(ref5).max())
+        contraction[mode] = {"ms": tm, "tflops": flops / (tm * 1e-3) / 1e12, "max_rel_err_vs_fp64_cpu": err}
+    extras["fock_contraction"] = contraction
+    return e2e_ms, h2d, d2h, plain_value, cpu, extras
 
 
 def rb_order_largest(rb, n):
@@ -440,6 +513,9 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-oracle baseline leg")
+    ap.add_argument("--instances", type=int, default=N_INST, help="triples in the ragged batch (profiling runs)")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="time only the headline step (no e2e, per-instance loop, contraction, CPU legs)")
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()

@@ -177,6 +177,27 @@ MM_API int mm_ragged_fwd(const mm_ragged_plan *plan, const mm_c128 *A, const mm_
 MM_API int mm_ragged_vjp(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG, mm_c128 *dA,
                   mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
 
+/* ------------------------------------------------------- Fock contraction */
+
+/*
+ * Y = U X for complex128 row-major U (M x K), X (K x N), Y (M x N): the dense
+ * Fock-space contraction after the recurrence, e.g. a 2-mode gate's Fock tensor
+ * reshaped to (c^2 x c^2) applied to a batch of kets stacked as columns.
+ * Replaces ArrayAnsatz.contract -> math.einsum -> opt_einsum -> numpy
+ * tensordot / BLAS zgemm (mrmustard/physics/ansatz/array_ansatz.py:159-226,
+ * mrmustard/math/backend_manager.py:526-548).
+ * mode MM_GEMM_FP64: native FP64 (DFMA).  mode MM_GEMM_OZAKI_BF16: FP64 values
+ * split into `slices` (2..9) signed 6-bit slices per row of U / column of X,
+ * slice products on the BF16 tensor cores with exact FP32 accumulation,
+ * recombined through 64-bit integer sums and one FP64 scaling per slice order;
+ * `slices` = 9 keeps 54 bits per operand.  ws: mm_fock_gemm_workspace_bytes
+ * (256 bytes for FP64).
+ */
+enum mm_gemm_mode { MM_GEMM_FP64 = 0, MM_GEMM_OZAKI_BF16 = 1 };
+MM_API size_t mm_fock_gemm_workspace_bytes(int mode, int64_t M, int64_t N, int64_t K, int slices);
+MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128 *U, const mm_c128 *X, mm_c128 *Y,
+                        int slices, void *ws, size_t ws_bytes, mm_stream_t stream);
+
 /* ------------------------------------------------------------- diagnostics */
 
 /*

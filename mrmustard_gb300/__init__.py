@@ -11,6 +11,7 @@ from __future__ import annotations
 from ._build_ext import build as build_library
 from .autograd import HermiteRenormalizedFn, hermite_renormalized_autograd
 from .backend import BackendGB300
+from .fock import apply_unitary, fock_gemm
 from .hermite import (
     device_fwd,
     device_vjp,
@@ -44,7 +45,9 @@ __all__ = [
     "BackendGB300",
     "HermiteRenormalizedFn",
     "RaggedBatch",
+    "apply_unitary",
     "build_library",
+    "fock_gemm",
     "device_fwd",
     "device_vjp",
     "hermite_renormalized",

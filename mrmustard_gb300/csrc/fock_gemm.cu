@@ -1,0 +1,378 @@
+// Fock-space contraction Y = U X (complex128, row-major), the dense step that
+// follows the recurrence when a gate tensor is applied to a batch of kets
+// (reference: ArrayAnsatz.contract, mrmustard/physics/ansatz/array_ansatz.py:159-226,
+// via math.einsum -> opt_einsum -> tensordot -> zgemm, backend_manager.py:526-548).
+//
+// Two paths:
+//  * MM_GEMM_FP64: complex DFMA GEMM (4 FP64 FMA per complex multiply-add).
+//  * MM_GEMM_OZAKI_BF16: Ozaki-style split.  Each real and imaginary part of U
+//    (per row) and of X (per column) is scaled by a power of two 2^E so that
+//    |x| < 2^E, truncated to a 54-bit integer a = floor(|x| 2^(54-E)) and cut
+//    into S signed 6-bit slices s_p (a = sum_p s_p 2^(54-6p)), each an integer
+//    in [-63, 63] and therefore exact in BF16.  Slice products accumulate on the
+//    tensor cores in FP32, exactly (|s_p s_q| <= 3969 < 2^12, so 4096 terms stay
+//    below 2^24), and are flushed into 64-bit integer sums every 4096 terms.
+//    All pairs (p, q) with the same p + q = d share a scale, so they add up in
+//    the same integer sum; each group d = 2 .. S+1 is then scaled once by
+//    2^(E_row + F_col - 6d) and added in FP64.  Pairs with p + q > S + 1 are
+//    dropped (the Ozaki truncation); the slicing itself truncates below
+//    2^(E-54).  The only FP64 work is one conversion and one FMA per element
+//    and group, which matters on a part whose FP64 rate is 1/1000 of BF16.
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace {
+
+using mm::cmk;
+
+// ---------------------------------------------------------------- FP64 path
+constexpr int FG_BM = 32, FG_BN = 32, FG_BK = 16;
+
+__global__ void __launch_bounds__(256) zgemm_fp64_kernel(const double2* __restrict__ U, const double2* __restrict__ X,
+                                                         double2* __restrict__ Y, int M, int N, int K) {
+  __shared__ double2 Us[FG_BK][FG_BM];
+  __shared__ double2 Xs[FG_BK][FG_BN];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = blockIdx.y * FG_BM, n0 = blockIdx.x * FG_BN;
+  double2 acc[2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) acc[i][j] = cmk(0.0, 0.0);
+  for (int k0 = 0; k0 < K; k0 += FG_BK) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + r * 256;
+      const int row = idx / FG_BK, kk = idx % FG_BK;
+      const int gm = m0 + row, gk = k0 + kk;
+      Us[kk][row] = (gm < M && gk < K) ? __ldg(U + (int64_t)gm * K + gk) : cmk(0.0, 0.0);
+      const int kx = idx / FG_BN, col = idx % FG_BN;
+      const int gk2 = k0 + kx, gn = n0 + col;
+      Xs[kx][col] = (gk2 < K && gn < N) ? __ldg(X + (int64_t)gk2 * N + gn) : cmk(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < FG_BK; ++kk) {
+      const double2 u0 = Us[kk][ty * 2], u1 = Us[kk][ty * 2 + 1];
+      const double2 x0 = Xs[kk][tx * 2], x1 = Xs[kk][tx * 2 + 1];
+      acc[0][0] = mm::cfma(u0, x0, acc[0][0]);
+      acc[0][1] = mm::cfma(u0, x1, acc[0][1]);
+      acc[1][0] = mm::cfma(u1, x0, acc[1][0]);
+      acc[1][1] = mm::cfma(u1, x1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int gm = m0 + ty * 2 + i, gn = n0 + tx * 2 + j;
+      if (gm < M && gn < N) Y[(int64_t)gm * N + gn] = acc[i][j];
+    }
+}
+
+// ---------------------------------------------------------------- Ozaki split
+constexpr int OZ_BETA = 6;       // bits per slice
+constexpr int OZ_MAX_SLICES = 9;  // 54 bits
+constexpr int OZ_FLUSH = 4096;    // exact FP32 accumulation length for |s| <= 63
+constexpr int OZ_BM = 64, OZ_BN = 32, OZ_BK = 32, OZ_PAD = 8;
+constexpr int OZ_KALIGN = 32;     // Kp: K padded to a multiple of this (zeros)
+
+// x = (-1)^neg * mant * 2^ex with mant < 2^53; returns the exponent bound E(x)
+// with |x| < 2^E(x) (or INT32_MIN for x == 0).
+__device__ __forceinline__ int exp_bound(double x) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  const uint64_t frac = bits & ((1ull << 52) - 1);
+  if (e == 0 && frac == 0) return INT32_MIN;
+  const int ex = e ? e - 1075 : -1074;
+  return ex + 53;
+}
+
+// Row exponents of U (M x K): E[r] = max over the row's re and im of exp_bound.
+__global__ void __launch_bounds__(256) row_exp_kernel(const double2* __restrict__ U, int M, int K, int* __restrict__ E) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= M) return;
+  int m = INT32_MIN;
+  for (int k = lane; k < K; k += 32) {
+    const double2 v = __ldg(U + (int64_t)warp * K + k);
+    m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) E[warp] = m;
+}
+
+// Column exponents of X (K x N): F[c] = max over the column.
+__global__ void __launch_bounds__(256) col_exp_kernel(const double2* __restrict__ X, int K, int N, int* __restrict__ F) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  int m = INT32_MIN;
+  for (int k = 0; k < K; ++k) {
+    const double2 v = __ldg(X + (int64_t)k * N + c);
+    m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
+  }
+  F[c] = m;
+}
+
+// Slices of one value against exponent bound E: out[p] for p < S.
+__device__ __forceinline__ void slice_value(double x, int E, int S, __nv_bfloat16* out, int64_t pstride) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  const uint64_t frac = bits & ((1ull << 52) - 1);
+  const bool neg = (bits >> 63) != 0;
+  uint64_t a = 0;
+  if (E != INT32_MIN && (e != 0 || frac != 0)) {
+    const uint64_t mant = e ? (frac | (1ull << 52)) : frac;
+    const int ex = e ? e - 1075 : -1074;
+    const int shift = ex + 54 - E;  // <= 1 because |x| < 2^E
+    if (shift >= 0) a = mant << shift;
+    else if (shift > -64) a = mant >> (-shift);
+  }
+  for (int p = 0; p < S; ++p) {
+    const int v = (int)((a >> (54 - OZ_BETA * (p + 1))) & ((1u << OZ_BETA) - 1));
+    out[p * pstride] = __float2bfloat16_rn((float)(neg ? -v : v));
+  }
+}
+
+// U (M x K) -> Us[p][comp][M][Kp] (comp 0 = re, 1 = im); zero padding for k >= K.
+__global__ void __launch_bounds__(256) split_u_kernel(const double2* __restrict__ U, int M, int K, int Kp, int S,
+                                                      const int* __restrict__ E, __nv_bfloat16* __restrict__ Us) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)M * Kp) return;
+  const int r = (int)(idx / Kp), k = (int)(idx - (int64_t)r * Kp);
+  const int64_t plane = (int64_t)M * Kp;  // one (p, comp) plane
+  double2 v = cmk(0.0, 0.0);
+  if (k < K) v = __ldg(U + (int64_t)r * K + k);
+  const int Er = E[r];
+  slice_value(v.x, Er, S, Us + idx, 2 * plane);
+  slice_value(v.y, Er, S, Us + plane + idx, 2 * plane);
+}
+
+// X (K x N) -> Xs[q][comp][N][Kp] (transposed: each column's K values contiguous).
+__global__ void __launch_bounds__(256) split_x_kernel(const double2* __restrict__ X, int K, int N, int Kp, int S,
+                                                      const int* __restrict__ F, __nv_bfloat16* __restrict__ Xs) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)N * Kp) return;
+  const int c = (int)(idx / Kp), k = (int)(idx - (int64_t)c * Kp);
+  const int64_t plane = (int64_t)N * Kp;
+  double2 v = cmk(0.0, 0.0);
+  if (k < K) v = __ldg(X + (int64_t)k * N + c);
+  const int Fc = F[c];
+  slice_value(v.x, Fc, S, Xs + idx, 2 * plane);
+  slice_value(v.y, Fc, S, Xs + plane + idx, 2 * plane);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ double pow2(int e) {
+  if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
+  return ldexp(1.0, e);
+}
+
+// One CTA: a 64 x 32 tile of Y, 4 warps each 32 x 16 (2 x 2 mma tiles of 16 x 8).
+// Per slice-order group d, all pairs (p, q = d - p) accumulate into int64 sums;
+// the group is then added to Y in FP64 (the first group stores).
+__global__ void __launch_bounds__(128) ozaki_mma_kernel(const __nv_bfloat16* __restrict__ Us,
+                                                        const __nv_bfloat16* __restrict__ Xs,
+                                                        const int* __restrict__ E, const int* __restrict__ F,
+                                                        double2* __restrict__ Y, int M, int N, int Kp, int S) {
+  __shared__ __align__(16) __nv_bfloat16 As[2][OZ_BM][OZ_BK + OZ_PAD];  // [comp][row][k]
+  __shared__ __align__(16) __nv_bfloat16 Bs[2][OZ_BN][OZ_BK + OZ_PAD];  // [comp][col][k]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 16;
+  const int m0 = blockIdx.y * OZ_BM, n0 = blockIdx.x * OZ_BN;
+  const int64_t uplane = (int64_t)M * Kp, xplane = (int64_t)N * Kp;
+
+  for (int d = 2; d <= S + 1; ++d) {
+    long long Tre[16], Tim[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) Tre[i] = Tim[i] = 0;
+    const int plo = d - S > 1 ? d - S : 1, phi = d - 1 < S ? d - 1 : S;
+    for (int p = plo; p <= phi; ++p) {
+      const int q = d - p;
+      const __nv_bfloat16* Up = Us + (int64_t)(p - 1) * 2 * uplane;
+      const __nv_bfloat16* Xq = Xs + (int64_t)(q - 1) * 2 * xplane;
+      float rr[16], ii[16], ri[16], ir[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) rr[i] = ii[i] = ri[i] = ir[i] = 0.f;
+      for (int k0 = 0; k0 < Kp; k0 += OZ_BK) {
+        // A: 2 comps x 64 rows x 32 k = 512 x 16-byte chunks; B: 2 x 32 x 32 = 256 chunks
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int ch = tid + r * 128;
+          const int comp = ch >> 8, row = (ch >> 2) & 63, kc = (ch & 3) * 8;
+          const int gm = m0 + row;
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (gm < M) v = __ldg(reinterpret_cast<const uint4*>(Up + comp * uplane + (int64_t)gm * Kp + k0 + kc));
+          *reinterpret_cast<uint4*>(&As[comp][row][kc]) = v;
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const int ch = tid + r * 128;
+          const int comp = ch >> 7, col = (ch >> 2) & 31, kc = (ch & 3) * 8;
+          const int gn = n0 + col;
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (gn < N) v = __ldg(reinterpret_cast<const uint4*>(Xq + comp * xplane + (int64_t)gn * Kp + k0 + kc));
+          *reinterpret_cast<uint4*>(&Bs[comp][col][kc]) = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < OZ_BK; kk += 16) {
+          uint32_t a[2][2][4], b[2][2][2];  // [comp][mtile][reg], [comp][ntile][reg]
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+              const int r0 = wm + mt * 16 + g;
+              a[c][mt][0] = *reinterpret_cast<const uint32_t*>(&As[c][r0][kk + t * 2]);
+              a[c][mt][1] = *reinterpret_cast<const uint32_t*>(&As[c][r0 + 8][kk + t * 2]);
+              a[c][mt][2] = *reinterpret_cast<const uint32_t*>(&As[c][r0][kk + 8 + t * 2]);
+              a[c][mt][3] = *reinterpret_cast<const uint32_t*>(&As[c][r0 + 8][kk + 8 + t * 2]);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) {
+              const int c0 = wn + nt * 8 + g;
+              b[c][nt][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][c0][kk + t * 2]);
+              b[c][nt][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][c0][kk + 8 + t * 2]);
+            }
+          }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) {
+              float* prr = rr + (mt * 2 + nt) * 4;
+              float* pii = ii + (mt * 2 + nt) * 4;
+              float* pri = ri + (mt * 2 + nt) * 4;
+              float* pir = ir + (mt * 2 + nt) * 4;
+              mma_bf16(*reinterpret_cast<float(*)[4]>(prr), a[0][mt], b[0][nt]);
+              mma_bf16(*reinterpret_cast<float(*)[4]>(pii), a[1][mt], b[1][nt]);
+              mma_bf16(*reinterpret_cast<float(*)[4]>(pri), a[0][mt], b[1][nt]);
+              mma_bf16(*reinterpret_cast<float(*)[4]>(pir), a[1][mt], b[0][nt]);
+            }
+        }
+        __syncthreads();
+        const int kdone = k0 + OZ_BK;
+        if ((kdone % OZ_FLUSH) == 0 || kdone >= Kp) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            Tre[i] += (long long)rr[i] - (long long)ii[i];
+            Tim[i] += (long long)ri[i] + (long long)ir[i];
+            rr[i] = ii[i] = ri[i] = ir[i] = 0.f;
+          }
+        }
+      }
+    }
+    // add group d in FP64
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int gm = m0 + wm + mt * 16 + g + (h >> 1) * 8;
+          const int gn = n0 + wn + nt * 8 + t * 2 + (h & 1);
+          if (gm < M && gn < N) {
+            const int i = (mt * 2 + nt) * 4 + h;
+            const int er = E[gm], fc = F[gn];
+            double2 y = cmk(0.0, 0.0);
+            if (er != INT32_MIN && fc != INT32_MIN) {
+              const double sc = pow2(er + fc - OZ_BETA * d);
+              y = cmk((double)Tre[i] * sc, (double)Tim[i] * sc);
+            }
+            double2* py = Y + (int64_t)gm * N + gn;
+            if (d == 2) {
+              *py = y;
+            } else {
+              const double2 o = *py;
+              *py = cmk(o.x + y.x, o.y + y.y);
+            }
+          }
+        }
+  }
+}
+
+}  // namespace
+
+namespace {
+int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+struct OzLayout {
+  int64_t Kp = 0;
+  size_t us = 0, xs = 0, e = 0, f = 0, total = 0;
+};
+
+OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int S) {
+  OzLayout L;
+  L.Kp = round_up(K, OZ_KALIGN);
+  size_t off = 0;
+  L.us = off;
+  off = round_up(off + (size_t)S * 2 * M * L.Kp * sizeof(__nv_bfloat16), 256);
+  L.xs = off;
+  off = round_up(off + (size_t)S * 2 * N * L.Kp * sizeof(__nv_bfloat16), 256);
+  L.e = off;
+  off = round_up(off + (size_t)M * sizeof(int), 256);
+  L.f = off;
+  off = round_up(off + (size_t)N * sizeof(int), 256);
+  L.total = off;
+  return L;
+}
+}  // namespace
+
+extern "C" {
+
+MM_API size_t mm_fock_gemm_workspace_bytes(int mode, int64_t M, int64_t N, int64_t K, int slices) {
+  if (M < 1 || N < 1 || K < 1) return 0;
+  if (mode == 0) return 256;
+  if (mode != 1 || slices < 2 || slices > OZ_MAX_SLICES) return 0;
+  return oz_layout(M, N, K, slices).total;
+}
+
+MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128* U, const mm_c128* X, mm_c128* Y,
+                        int slices, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return MM_ERR_NO_DEVICE;
+  }
+  if (M < 1 || N < 1 || K < 1 || !U || !X || !Y) return MM_ERR_INVALID_ARG;
+  if (M > INT32_MAX / 2 || N > INT32_MAX / 2 || K > INT32_MAX / 2) return MM_ERR_TOO_LARGE;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (mode == 0) {
+    dim3 grid((unsigned)((N + FG_BN - 1) / FG_BN), (unsigned)((M + FG_BM - 1) / FG_BM));
+    if (grid.y > 65535) return MM_ERR_TOO_LARGE;
+    zgemm_fp64_kernel<<<grid, 256, 0, st>>>((const double2*)U, (const double2*)X, (double2*)Y, (int)M, (int)N, (int)K);
+    return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
+  }
+  if (mode != 1) return MM_ERR_INVALID_ARG;
+  if (slices < 2 || slices > OZ_MAX_SLICES) return MM_ERR_INVALID_ARG;
+  const OzLayout L = oz_layout(M, N, K, slices);
+  if (ws == nullptr || ((uintptr_t)ws % 256) != 0 || ws_bytes < L.total) return MM_ERR_WORKSPACE;
+  char* w = static_cast<char*>(ws);
+  __nv_bfloat16* Us = reinterpret_cast<__nv_bfloat16*>(w + L.us);
+  __nv_bfloat16* Xs = reinterpret_cast<__nv_bfloat16*>(w + L.xs);
+  int* E = reinterpret_cast<int*>(w + L.e);
+  int* F = reinterpret_cast<int*>(w + L.f);
+  const int Kp = (int)L.Kp;
+  row_exp_kernel<<<(unsigned)((M * 32 + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, E);
+  col_exp_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, F);
+  split_u_kernel<<<(unsigned)((M * Kp + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, Us);
+  split_x_kernel<<<(unsigned)((N * Kp + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, Kp, slices, F, Xs);
+  dim3 grid((unsigned)((N + OZ_BN - 1) / OZ_BN), (unsigned)((M + OZ_BM - 1) / OZ_BM));
+  if (grid.y > 65535) return MM_ERR_TOO_LARGE;
+  ozaki_mma_kernel<<<grid, 128, 0, st>>>(Us, Xs, E, F, (double2*)Y, (int)M, (int)N, Kp, slices);
+  return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
+}
+
+}  // extern "C"
