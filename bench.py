@@ -464,7 +464,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
             A1 *= 0.89 / np.linalg.norm(A1, 2)
         b1 = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
         At, bt = torch.as_tensor(A1, device=dev), torch.as_tensor(b1, device=dev)
-        ct = torch.tensor(1.0 + 0j, device=dev)
+        ct = torch.tensor(1.0 + 0j, dtype=torch.complex128, device=dev)
         out = torch.empty((cut,) * D, dtype=torch.complex128, device=dev)
         with mm.settings(CHECK_DEVICE_STATUS=False):
             t1 = time_eager(lambda: mm.device_fwd(At, bt, ct, (cut,) * D, out=out), reps=5)
@@ -480,7 +480,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     A5 *= 0.95 / np.linalg.norm(A5, 2)
     b5 = 0.3 * (rng.standard_normal(4) + 1j * rng.standard_normal(4)) / np.sqrt(2)
     U5 = mm.device_fwd(torch.as_tensor(A5, device=dev), torch.as_tensor(b5, device=dev),
-                       torch.tensor(1.0 + 0j, device=dev), (50, 50, 50, 50)).reshape(2500, 2500)
+                       torch.tensor(1.0 + 0j, dtype=torch.complex128, device=dev), (50, 50, 50, 50)).reshape(2500, 2500)
     kets = torch.complex(torch.randn(256, 2500, dtype=torch.float64, device=dev),
                          torch.randn(256, 2500, dtype=torch.float64, device=dev))
     kets = kets / kets.abs().pow(2).sum(1, keepdim=True).sqrt()

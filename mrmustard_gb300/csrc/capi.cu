@@ -22,6 +22,7 @@ constexpr int64_t kGridMinAmps = 8192;     // single instances at least this lar
 constexpr uint32_t kSmallChunk = 256;      // grid kernel: chunks smaller than this run on CTA 0
 constexpr int kGridBlock = 512;            // threads per CTA of the cooperative grid kernel
 constexpr int64_t kVjpItemAmps = 65536;    // default amplitudes per VJP work item
+constexpr int kTeamCluster = 8;            // CTAs per cluster for the large instances of a ragged batch
 constexpr size_t kAlign = 256;
 
 int cuda_fail(cudaError_t e) {
@@ -124,7 +125,7 @@ void vjp_split(const Geom& g, int64_t target_amps, uint32_t& fpi, int64_t& items
 
 // Workspace regions shared by every entry point.
 struct Layout {
-  size_t tables = 0, coef = 0, partials = 0, desc = 0, order = 0, items = 0, total = 0;
+  size_t tables = 0, coef = 0, partials = 0, desc = 0, order = 0, big = 0, items = 0, total = 0;
   int64_t kmax = 0;
 };
 
@@ -141,6 +142,8 @@ Layout make_layout(int64_t kmax, int64_t coef_entries_total, int64_t n_items, in
   L.desc = off;
   off = align_up(off + (size_t)n_desc * sizeof(InstDesc));
   L.order = off;
+  off = align_up(off + (size_t)n_order * sizeof(int32_t));
+  L.big = off;
   off = align_up(off + (size_t)n_order * sizeof(int32_t));
   L.items = off;
   off = align_up(off + (size_t)n_items * sizeof(VjpItem));
@@ -307,6 +310,8 @@ struct mm_ragged_plan {
   int64_t B = 0;
   std::vector<InstDesc> desc;
   std::vector<int32_t> order;     // forward schedule: instances by decreasing cost
+  std::vector<int32_t> small;     // instances run by one CTA each (decreasing cost)
+  std::vector<int32_t> big;       // instances run by a cluster each (decreasing cost)
   std::vector<VjpItem> items;     // VJP items grouped by D, then instance
   std::vector<int64_t> d_item_begin, d_item_count;  // per D (index D)
   int maxD = 0;
@@ -321,6 +326,12 @@ struct mm_ragged_plan {
 namespace {
 int ragged_build(mm_ragged_plan* p) {
   const int64_t B = p->B;
+  // large instances (at least team_min_amps amplitudes) go to cluster teams
+  int64_t thr = p->team_min_amps;
+  if (thr == 0) thr = std::max<int64_t>(65536, p->total_amps / (4 * 152));  // about 1/4 of an SM's share
+  p->small.clear();
+  p->big.clear();
+  for (int32_t k : p->order) (p->desc[k].g.n >= thr ? p->big : p->small).push_back(k);
   // VJP items: grouped by D (one launch per D), instances by decreasing size
   std::vector<int32_t> byD(p->order);
   std::stable_sort(byD.begin(), byD.end(), [&](int32_t a, int32_t b) { return p->desc[a].g.D < p->desc[b].g.D; });
@@ -365,6 +376,43 @@ RaggedSrc ragged_src(const mm_ragged_plan* p, char* ws, const double2* A, const 
   s.coef = reinterpret_cast<double2*>(ws + p->L.coef);
   s.items = reinterpret_cast<const VjpItem*>(ws + p->L.items);
   return s;
+}
+}  // namespace
+
+namespace {
+template <int DHI>
+int launch_team_D(const mm_ragged_plan* p, const RaggedSrc& src, char* w, const double* rs, int stable,
+                  cudaStream_t st) {
+  auto kern = fwd_ragged_team_kernel<1, DHI>;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kTeamCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(MM_BLOCK);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(kTeamCluster);
+  int ncl = 0;
+  MM_CUDA(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg));
+  if (ncl < 1) return MM_ERR_UNSUPPORTED;
+  cfg.gridDim = dim3((unsigned)(ncl * kTeamCluster));
+  const int32_t* small = reinterpret_cast<const int32_t*>(w + p->L.big);
+  const int32_t* big = small + p->small.size();
+  WsHeader* h = reinterpret_cast<WsHeader*>(w);
+  MM_CUDA(cudaLaunchKernelEx(&cfg, kern, src, rs, stable, big, (int)p->big.size(), small, (int)p->small.size(), h));
+  g_launches.fetch_add(1);
+  return MM_OK;
+}
+
+int launch_ragged_team(const mm_ragged_plan* p, const RaggedSrc& src, char* w, const double* rs, int stable,
+                       cudaStream_t st) {
+  if (p->maxD <= 2) return launch_team_D<2>(p, src, w, rs, stable, st);
+  if (p->maxD <= 4) return launch_team_D<4>(p, src, w, rs, stable, st);
+  return launch_team_D<8>(p, src, w, rs, stable, st);
 }
 }  // namespace
 
@@ -538,6 +586,10 @@ int mm_ragged_plan_upload(const mm_ragged_plan* plan, void* ws, size_t ws_bytes,
                             cudaMemcpyHostToDevice, st));
     MM_CUDA(cudaMemcpyAsync(w + plan->L.order, plan->order.data(), plan->order.size() * sizeof(int32_t),
                             cudaMemcpyHostToDevice, st));
+    std::vector<int32_t> lists(plan->small);
+    lists.insert(lists.end(), plan->big.begin(), plan->big.end());
+    MM_CUDA(cudaMemcpyAsync(w + plan->L.big, lists.data(), lists.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                            st));
   }
   if (!plan->items.empty())
     MM_CUDA(cudaMemcpyAsync(w + plan->L.items, plan->items.data(), plan->items.size() * sizeof(VjpItem),
@@ -561,6 +613,7 @@ int mm_ragged_fwd(const mm_ragged_plan* plan, const mm_c128* A, const mm_c128* b
   if ((rc = reset_launch_state(w, st))) return rc;
   if ((rc = launch_setup(src, plan->B, w, plan->L, 1, st))) return rc;
   const double* rs = tables_of(w, plan->L).rs;
+  if (!plan->big.empty()) return launch_ragged_team(plan, src, w, rs, stable, st);
   const unsigned nb = (unsigned)plan->B;
   if (plan->maxD <= 2) fwd_cta_kernel<1, 2, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, rs, stable);
   else if (plan->maxD <= 4) fwd_cta_kernel<1, 4, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, rs, stable);

@@ -16,6 +16,17 @@
 #define MM_NV_MAX (1 + MM_MAXD + MM_MAXD * (MM_MAXD + 1) / 2)  // VJP accumulators per instance
 #define MM_BLOCK 256       // threads per CTA for the recurrence kernels
 
+// Shared-memory declarations of the kernels.  Under nvcc this is plain
+// __shared__; the host emulation of the kernels (MM_HOST_EMULATION) supplies
+// per-CTA storage instead, so several emulated CTAs can run at once.
+#if defined(MM_HOST_EMULATION) && !defined(__CUDA_ARCH__)
+template <class T>
+T& mm_emu_shared(int key);
+#define MM_SHARED(T, name) T& name = mm_emu_shared<T>(__LINE__)
+#else
+#define MM_SHARED(T, name) __shared__ T name
+#endif
+
 namespace mm {
 
 // ---------------------------------------------------------------- complex helpers
@@ -105,7 +116,8 @@ struct WsHeader {
   int32_t status;       // sticky error word (0 = ok), written with atomicCAS
   int32_t pad0[31];
   uint32_t barrier;     // grid-barrier arrival counter
-  uint32_t pad1[31];
+  uint32_t queue;       // work-queue head
+  uint32_t pad1[30];
   uint32_t heartbeat;   // bumped by CTAs that work while others wait (progress signal)
   uint32_t pad2[31];
   int32_t abort;        // set when any CTA of the launch gave up a wait
@@ -160,7 +172,7 @@ __device__ __forceinline__ void heartbeat(WsHeader* h) { atomicAdd(&h->heartbeat
 // CTA records MM_ERR_WAIT_TIMEOUT and the function returns false, so the kernel
 // returns instead of hanging the GPU.
 __device__ __forceinline__ bool grid_barrier(WsHeader* h, uint32_t epoch, uint64_t budget_ns, uint32_t extra) {
-  __shared__ int s_ok;
+  MM_SHARED(int, s_ok);
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;

@@ -334,7 +334,7 @@ __device__ void stable_instance_cta(const InstView& v, const double* rs) {
 // One CTA per instance, instances taken in schedule order (largest first).
 template <int DLO, int DHI, class Src>
 __global__ void __launch_bounds__(MM_BLOCK) fwd_cta_kernel(Src src, const double* __restrict__ rs, int stable) {
-  __shared__ InstView sv;
+  MM_SHARED(InstView, sv);
   const int64_t k = src.sched(blockIdx.x);
   if (threadIdx.x == 0) src.load(k, sv);
   __syncthreads();
@@ -358,6 +358,140 @@ __global__ void __launch_bounds__(MM_BLOCK) fwd_cta_kernel(Src src, const double
 #undef MM_FWD_CASE
 }
 
+// ------------------------------------------------ ragged batch with cluster teams
+// Thread-block cluster helpers (sm_90+ PTX special registers and barrier).
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_size() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_index() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_count() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// All threads of all CTAs of the cluster; release/acquire orders the chunk's
+// global writes before the next chunk's reads (which go through L2: ldG<true>).
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+#else  // host compilation of the device code (CPU emulation): provided by the emulator
+uint32_t cluster_rank();
+uint32_t cluster_size();
+uint32_t cluster_index();
+uint32_t cluster_count();
+void cluster_sync();
+#endif
+
+// One instance on a whole cluster: every chunk is split over the cluster's
+// CTAs in contiguous ranges, with a cluster barrier after it.  Control flow is
+// identical in every CTA of the cluster, so every barrier is reached by all.
+template <int D>
+__device__ void fwd_instance_team(const InstView& v, const double* rs, uint32_t rank, uint32_t nranks) {
+  if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
+  cluster_sync();
+  for (int i = D - 1; i >= 0; --i) {
+    const uint32_t si = (uint32_t)v.g.strides[i];
+    const uint32_t per = (si + nranks - 1) / nranks;
+    const uint32_t lo = min(si, per * rank), hi = min(si, lo + per);
+    for (int m = 1; m < (int)v.g.shape[i]; ++m) {
+      fwd_chunk<D, true>(v, rs, i, m, lo, hi, blockDim.x, threadIdx.x);
+      cluster_sync();
+    }
+  }
+}
+
+template <int D>
+__device__ void stable_instance_team(const InstView& v, const double* rs, uint32_t rank, uint32_t nranks) {
+  if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
+  cluster_sync();
+  int wmax = 0;
+  for (int i = 0; i < D; ++i) wmax += (int)v.g.shape[i] - 1;
+  const uint32_t P = (uint32_t)(v.g.n / v.g.shape[D - 1]);
+  const uint32_t per = (P + nranks - 1) / nranks;
+  const uint32_t lo = min(P, per * rank), hi = min(P, lo + per);
+  for (int w = 1; w <= wmax; ++w) {
+    stable_wave<D, true>(v, rs, w, lo, hi, blockDim.x, threadIdx.x);
+    cluster_sync();
+  }
+}
+
+// Persistent launch with cluster dimensions (CL, 1, 1).  Phase 1: cluster c
+// takes the large instances big[c], big[c + nclusters], ... (largest first) and
+// runs each on all its CTAs.  Phase 2: every CTA pulls the remaining instances
+// (largest first) one at a time from an atomic queue and runs each alone.
+// No CTA ever waits for another cluster, so the launch needs no co-residency
+// guarantee beyond the cluster's own.
+template <int DLO, int DHI>
+__global__ void __launch_bounds__(MM_BLOCK) fwd_ragged_team_kernel(RaggedSrc src, const double* __restrict__ rs,
+                                                                   int stable, const int32_t* __restrict__ big,
+                                                                   int n_big, const int32_t* __restrict__ small,
+                                                                   int n_small, WsHeader* h) {
+  MM_SHARED(InstView, sv);
+  MM_SHARED(int, s_next);
+  const uint32_t rank = cluster_rank(), nranks = cluster_size();
+  const uint32_t cid = cluster_index(), ncl = cluster_count();
+  for (int bi = (int)cid; bi < n_big; bi += (int)ncl) {
+    if (threadIdx.x == 0) src.load(big[bi], sv);
+    __syncthreads();
+    const int D = sv.g.D;
+#define MM_TEAM_CASE(DD)                                          \
+  if constexpr (DLO <= DD && DD <= DHI) {                         \
+    if (D == DD) {                                                \
+      if (stable) stable_instance_team<DD>(sv, rs, rank, nranks); \
+      else fwd_instance_team<DD>(sv, rs, rank, nranks);           \
+    }                                                             \
+  }
+    MM_TEAM_CASE(1)
+    MM_TEAM_CASE(2)
+    MM_TEAM_CASE(3)
+    MM_TEAM_CASE(4)
+    MM_TEAM_CASE(5)
+    MM_TEAM_CASE(6)
+    MM_TEAM_CASE(7)
+    MM_TEAM_CASE(8)
+#undef MM_TEAM_CASE
+    __syncthreads();
+  }
+  for (;;) {
+    if (threadIdx.x == 0) s_next = (int)atomicAdd(&h->queue, 1u);
+    __syncthreads();
+    const int idx = s_next;
+    if (idx >= n_small) break;
+    if (threadIdx.x == 0) src.load(small[idx], sv);
+    __syncthreads();
+    const int D = sv.g.D;
+#define MM_SOLO_CASE(DD)                                \
+  if constexpr (DLO <= DD && DD <= DHI) {               \
+    if (D == DD) {                                      \
+      if (stable) stable_instance_cta<DD>(sv, rs);      \
+      else fwd_instance_cta<DD>(sv, rs);                \
+    }                                                   \
+  }
+    MM_SOLO_CASE(1)
+    MM_SOLO_CASE(2)
+    MM_SOLO_CASE(3)
+    MM_SOLO_CASE(4)
+    MM_SOLO_CASE(5)
+    MM_SOLO_CASE(6)
+    MM_SOLO_CASE(7)
+    MM_SOLO_CASE(8)
+#undef MM_SOLO_CASE
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------ single large instance, whole grid
 // Cooperative launch (every CTA resident).  Levels whose chunks hold fewer than
 // `small_chunk` amplitudes run on CTA 0 alone; each larger chunk is split over
@@ -365,7 +499,7 @@ __global__ void __launch_bounds__(MM_BLOCK) fwd_cta_kernel(Src src, const double
 template <int D>
 __global__ void __launch_bounds__(512) fwd_grid_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
                                                        uint32_t small_chunk, uint64_t budget_ns, int stable) {
-  __shared__ InstView sv;
+  MM_SHARED(InstView, sv);
   if (threadIdx.x == 0) src.load(0, sv);
   __syncthreads();
   const Geom& g = sv.g;
@@ -416,7 +550,7 @@ __global__ void __launch_bounds__(512) fwd_grid_kernel(UniformSrc src, const dou
 // the host's expectation.  Only `src.c[k]` (a valid workspace address) is read.
 template <class Src>
 __global__ void view_selftest_kernel(Src src, int64_t k, const InstView* __restrict__ expect, int32_t* bad) {
-  __shared__ InstView sv;
+  MM_SHARED(InstView, sv);
   if (threadIdx.x == 0) src.load(k, sv);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -509,7 +643,8 @@ __device__ __forceinline__ void vjp_fibers(const InstView& v, const Tables& T, u
 // warps in order); thread 0..NV-1 end up writing out[s].
 template <int NV>
 __device__ __forceinline__ void block_reduce_write(double2 (&tot)[NV], double2* out) {
-  __shared__ double2 red[MM_BLOCK / 32][MM_NV_MAX];
+  typedef double2 RedT[MM_BLOCK / 32][MM_NV_MAX];
+  MM_SHARED(RedT, red);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int s = 0; s < NV; ++s) {
@@ -534,8 +669,9 @@ __device__ __forceinline__ void block_reduce_write(double2 (&tot)[NV], double2* 
 template <int DLO, int DHI, class Src>
 __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, double2* __restrict__ partials,
                                                              int64_t item_base) {
-  __shared__ InstView sv;
-  __shared__ uint32_t sq0, sq1;
+  MM_SHARED(InstView, sv);
+  MM_SHARED(uint32_t, sq0);
+  MM_SHARED(uint32_t, sq1);
   const int64_t item = item_base + blockIdx.x;
   if (threadIdx.x == 0) {
     int64_t k;

@@ -73,8 +73,10 @@ def ensure_device_ready(device) -> None:
 
 
 def raw(t: torch.Tensor) -> torch.Tensor:
-    """Materialised, contiguous storage of a tensor (torch's lazy conj/neg bits resolved),
-    so that its data pointer holds exactly its values."""
+    """Contiguous complex128 storage of a tensor (converted if needed, torch's lazy conj/neg bits
+    resolved), so that its data pointer holds exactly its values in the library's layout."""
+    if t.dtype != torch.complex128:
+        t = t.to(torch.complex128)
     return t.resolve_conj().resolve_neg().contiguous()
 
 

@@ -64,7 +64,8 @@ def test_cfg5_unitary_on_kets(cuda, oracle_lib):
     A *= 0.95 / np.linalg.norm(A, 2)
     b = 0.3 * (rng.standard_normal(4) + 1j * rng.standard_normal(4)) / np.sqrt(2)
     Ut = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
-                       torch.tensor(1.0 + 0j, device=cuda), (50, 50, 50, 50))
+                       torch.tensor(1.0 + 0j, device=cuda), (50, 50, 50, 50))  # complex64 c: converted
+    assert Ut[0, 0, 0, 0].item() == 1.0 and Ut.abs().max().item() >= 1.0
     kets = cn((256, 50, 50), 56)
     kets /= np.linalg.norm(kets.reshape(256, -1), axis=1)[:, None, None]
     kt = torch.as_tensor(kets, device=cuda)

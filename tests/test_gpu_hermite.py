@@ -281,6 +281,18 @@ def test_device_tensors_stay_on_device(cuda, oracle_lib):
     assert G2 is out and not torch.isnan(out).any()
 
 
+def test_device_api_converts_dtypes(cuda, oracle_lib):
+    """complex64 / real inputs to the device API are converted to complex128, not reinterpreted."""
+    A, b, _ = takagi(2, 0.6, 950)
+    G = mm.device_fwd(torch.as_tensor(A, device=cuda).to(torch.complex64).to(torch.complex128),
+                      torch.as_tensor(b, device=cuda), torch.tensor(0.5 + 0.25j, device=cuda), (5, 6))
+    ref = oracle_lib.vanilla((5, 6), A.astype(np.complex64).astype(complex), b, 0.5 + 0.25j)
+    assert rel(G, ref) < FWD_TOL
+    G2 = mm.device_fwd(torch.as_tensor(A.real, device=cuda), torch.as_tensor(b.real, device=cuda),
+                       torch.tensor(2.0, device=cuda), (4, 4))
+    assert rel(G2, oracle_lib.vanilla((4, 4), A.real, b.real, 2.0)) < FWD_TOL
+
+
 def test_poisoned_output_fully_overwritten(cuda, oracle_lib):
     for D, shape in [(1, (9,)), (2, (1, 6)), (3, (4, 1, 5)), (4, (3, 4, 2, 5))]:
         A, b, c = takagi(D, 0.7, 500 + D)
