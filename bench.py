@@ -387,16 +387,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     d2h = sum(t.numel() * 16 for t in (G_h, dA_h, db_h, dc_h))
 
     def e2e_step():
-        A.copy_(A_h, non_blocking=True)
-        b.copy_(b_h, non_blocking=True)
-        c.copy_(c_h, non_blocking=True)
-        g.copy_(g_h, non_blocking=True)
-        rb.forward(A, b, c, out=G)
-        rb.vjp(G, c, g, out=grads)
-        G_h.copy_(G, non_blocking=True)
-        dA_h.copy_(grads[0], non_blocking=True)
-        db_h.copy_(grads[1], non_blocking=True)
-        dc_h.copy_(grads[2], non_blocking=True)
+        rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h)
 
     e2e_steps = max(2, min(args.steps, 5))
     with mm.settings(CHECK_DEVICE_STATUS=False):

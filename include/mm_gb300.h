@@ -173,7 +173,8 @@ MM_API int mm_ragged_plan_upload(const mm_ragged_plan *plan, void *ws, size_t ws
 /* Forward of every instance of an uploaded plan (vanilla or stable). */
 MM_API int mm_ragged_fwd(const mm_ragged_plan *plan, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c, int stable,
                   mm_c128 *G, void *ws, size_t ws_bytes, mm_stream_t stream);
-/* VJP of every instance of an uploaded plan. */
+/* VJP of every instance of an uploaded plan.  G and dLdG may be any device-accessible
+ * addresses, including pinned host memory (read by the kernels over the host link). */
 MM_API int mm_ragged_vjp(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG, mm_c128 *dA,
                   mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
 

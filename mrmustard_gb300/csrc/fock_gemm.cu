@@ -19,7 +19,11 @@
 //    2^(E-54).  The only FP64 work is one conversion and one FMA per element
 //    and group, which matters on a part whose FP64 rate is 1/1000 of BF16.
 #include <cstdint>
+#include <cstdlib>
+#include <mutex>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -80,7 +84,7 @@ constexpr int OZ_BETA = 6;       // bits per slice
 constexpr int OZ_MAX_SLICES = 9;  // 54 bits
 constexpr int OZ_FLUSH = 4096;    // exact FP32 accumulation length for |s| <= 63
 constexpr int OZ_BM = 64, OZ_BN = 32, OZ_BK = 32, OZ_PAD = 8;
-constexpr int OZ_KALIGN = 32;     // Kp: K padded to a multiple of this (zeros)
+constexpr int OZ_KALIGN = 64;     // Kp: K padded to a multiple of this (zeros)
 
 // x = (-1)^neg * mant * 2^ex with mant < 2^53; returns the exponent bound E(x)
 // with |x| < 2^E(x) (or INT32_MIN for x == 0).
@@ -303,6 +307,354 @@ __global__ void __launch_bounds__(128) ozaki_mma_kernel(const __nv_bfloat16* __r
   }
 }
 
+
+// ---------------------------------------------------------------- tcgen05 path
+// Warp-specialised Blackwell kernel for the slice products.  One CTA owns a
+// 128-row x 32-complex-column tile of Y.  For every slice pair (p, q) and every
+// chunk of at most 4096 K values (one "unit"), the tensor cores compute two
+// M = 128, N = 64 products into TMEM:
+//     acc_r = U_re,p [X_re,q | X_im,q]   (columns 0..31: rr, 32..63: ri)
+//     acc_i = U_im,p [X_re,q | X_im,q]   (columns 0..31: ir, 32..63: ii)
+// with FP32 accumulation that is exact for 6-bit slices.  Roles:
+//   warp 0, lane 0: TMA producer (3-stage ring of [U_re | U_im | X_re ; X_im] K-blocks of 64),
+//   warp 1, lane 0: MMA issuer (tcgen05.mma, tcgen05.commit into mbarriers),
+//   warps 2..5:      epilogue (tcgen05.ld of a finished unit, exact integer sums per slice order,
+//                    one FP64 scaling per order into Y).
+// Accumulators are double-buffered (2 x 128 TMEM columns) so the epilogue of one
+// unit overlaps the MMAs of the next.  Every mbarrier wait is bounded; on a
+// timeout the CTA records MM_ERR_WAIT_TIMEOUT, lets its in-flight copies land,
+// frees its TMEM and returns.
+constexpr int TC_BM = 128;                                // Y rows per CTA (MMA M)
+constexpr int TC_NC = 32;                                 // Y complex columns per CTA (MMA N = 64)
+constexpr int TC_BK = 64;                                 // K per stage: one 128-byte swizzled row of BF16
+constexpr int TC_STAGES = 3;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;             // 16 KB per U component
+constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 8 KB ([X_re; X_im] rows)
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + TC_B_BYTES;  // 40 KB
+constexpr int TC_T_BYTES = 2 * TC_NC * TC_BM * 8;         // int64 slice-order sums, [comp][col][row]
+constexpr int TC_TMEM_COLS = 256;
+constexpr int TC_THREADS = 192;
+constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * TC_STAGE_BYTES + TC_T_BYTES + 256;
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 64, M = 128.
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                              ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false when another role gave up or the budget ran out (then records the error).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, mm::WsHeader* h,
+                                          uint64_t budget_ns) {
+  const uint64_t t0 = mm::globaltimer_ns();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63) == 63) {
+      if (*abort_flag) return false;
+      if (mm::globaltimer_ns() - t0 > budget_ns) {
+        *abort_flag = 1;
+        if (h) mm::set_status(h, MM_ERR_WAIT_TIMEOUT);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+// K-major, 128-byte swizzle smem descriptor (sm_100 format): start >> 4, LBO 16 B, SBO 1024 B, version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Units of a CTA, in order: slice order d = 2 .. S+1, p = max(1, d-S) .. min(S, d-1),
+// K chunks of at most 4096 (TC_FLUSH_BLOCKS K-blocks).  Every role walks the same sequence.
+struct UnitIter {
+  int S, nkb, chunk_kb;
+  int d, p, c;  // current unit
+  __device__ void start(int S_, int nkb_, int chunk_kb_) {
+    S = S_;
+    nkb = nkb_;
+    chunk_kb = chunk_kb_;
+    d = 2;
+    p = 1;
+    c = 0;
+  }
+  __device__ bool valid() const { return d <= S + 1; }
+  __device__ int q() const { return d - p; }
+  __device__ int kb_begin() const { return c * chunk_kb; }
+  __device__ int kb_end() const { return min(nkb, (c + 1) * chunk_kb); }
+  __device__ bool last_of_order() const {
+    const int phi = d - 1 < S ? d - 1 : S;
+    return p == phi && kb_end() >= nkb;
+  }
+  __device__ void next() {
+    if (kb_end() < nkb) {
+      ++c;
+      return;
+    }
+    c = 0;
+    const int phi = d - 1 < S ? d - 1 : S;
+    if (p < phi) {
+      ++p;
+      return;
+    }
+    ++d;
+    p = d - S > 1 ? d - S : 1;
+  }
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ CUtensorMap tmap_x,
+                    const int* __restrict__ E, const int* __restrict__ F, double2* __restrict__ Y, int M, int N,
+                    int Kp, int S, mm::WsHeader* h, uint64_t budget_ns) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* stages = smem;
+  long long* T = reinterpret_cast<long long*>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][TC_NC][TC_BM]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES + TC_T_BYTES);
+  // bars: full[STAGES], empty[STAGES], accf[2], acce[2], drain
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 5);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_NC;
+  const int nkb = Kp / TC_BK;
+  const int chunk_kb = 4096 / TC_BK;
+  auto full = [&](int s) { return smem_u32(bars + s); };
+  auto empty = [&](int s) { return smem_u32(bars + TC_STAGES + s); };
+  auto accf = [&](int b) { return smem_u32(bars + 2 * TC_STAGES + b); };
+  auto acce = [&](int b) { return smem_u32(bars + 2 * TC_STAGES + 2 + b); };
+  const uint32_t drain = smem_u32(bars + 2 * TC_STAGES + 4);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf(b), 1);
+      mbar_init(acce(b), 128);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // whole warp: TMEM allocation
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ------------------------------------------------------------ TMA producer
+    int stage = 0;
+    uint32_t phase = 0;
+    uint32_t armed_parity[TC_STAGES];
+    bool armed[TC_STAGES];
+    for (int s = 0; s < TC_STAGES; ++s) armed[s] = false;
+    UnitIter u;
+    u.start(S, nkb, chunk_kb);
+    bool ok = true;
+    for (; ok && u.valid(); u.next()) {
+      const int yu = (u.p - 1) * 2 * M + m0, yx = (u.q() - 1) * 2 * N + n0;
+      for (int kb = u.kb_begin(); kb < u.kb_end(); ++kb) {
+        if (!mbar_wait(empty(stage), phase ^ 1, abort_flag, h, budget_ns)) {
+          ok = false;
+          break;
+        }
+        unsigned char* st = stages + stage * TC_STAGE_BYTES;
+        mbar_expect_tx(full(stage), TC_STAGE_BYTES);
+        armed[stage] = true;
+        armed_parity[stage] = phase;
+        const int x = kb * TC_BK;
+        tma_load_2d(smem_u32(st), &tmap_u, x, yu, full(stage));
+        tma_load_2d(smem_u32(st + TC_A_BYTES), &tmap_u, x, yu + M, full(stage));
+        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), &tmap_x, x, yx, full(stage));
+        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + TC_B_BYTES / 2), &tmap_x, x, yx + N, full(stage));
+        if (++stage == TC_STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+    }
+    if (!ok) {  // let copies in flight land before the CTA's shared memory goes away
+      for (int s = 0; s < TC_STAGES; ++s)
+        if (armed[s]) {
+          const uint64_t t0 = mm::globaltimer_ns();
+          while (!mbar_try_wait(full(s), armed_parity[s]) && mm::globaltimer_ns() - t0 < budget_ns) {
+          }
+        }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ------------------------------------------------------------ MMA issuer
+    int stage = 0;
+    uint32_t phase = 0;
+    int abuf = 0;
+    uint32_t aphase = 0;
+    UnitIter u;
+    u.start(S, nkb, chunk_kb);
+    bool ok = true;
+    for (; ok && u.valid(); u.next()) {
+      if (!mbar_wait(acce(abuf), aphase ^ 1, abort_flag, h, budget_ns)) break;
+      tc_fence_after();
+      const uint32_t d_r = tmem + (uint32_t)(abuf * 128), d_i = d_r + 64;
+      for (int kb = u.kb_begin(); kb < u.kb_end(); ++kb) {
+        if (!mbar_wait(full(stage), phase, abort_flag, h, budget_ns)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t st = smem_u32(stages + stage * TC_STAGE_BYTES);
+#pragma unroll
+        for (int k16 = 0; k16 < TC_BK / 16; ++k16) {
+          const uint32_t koff = (uint32_t)k16 * 32;
+          const uint32_t acc = (kb > u.kb_begin() || k16 > 0) ? 1u : 0u;
+          const uint64_t bdesc = sw128_desc(st + 2 * TC_A_BYTES + koff);
+          tc_mma(d_r, sw128_desc(st + koff), bdesc, acc);
+          tc_mma(d_i, sw128_desc(st + TC_A_BYTES + koff), bdesc, acc);
+        }
+        tc_commit(empty(stage));  // frees the stage once these MMAs have read it
+        if (++stage == TC_STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+      if (!ok) break;
+      tc_commit(accf(abuf));  // the unit's accumulators are complete
+      if (++abuf == 2) {
+        abuf = 0;
+        aphase ^= 1;
+      }
+    }
+    // every MMA issued above has completed before TMEM can be freed
+    tc_commit(drain);
+    const uint64_t t0 = mm::globaltimer_ns();
+    while (!mbar_try_wait(drain, 0) && mm::globaltimer_ns() - t0 < budget_ns) {
+    }
+  } else if (warp >= 2) {
+    // ------------------------------------------------------------ epilogue
+    const int lane_base = 32 * (warp & 3);
+    const int row = lane_base + lane;
+    const int gm = m0 + row;
+    for (int c = 0; c < TC_NC; ++c) T[(0 * TC_NC + c) * TC_BM + row] = T[(1 * TC_NC + c) * TC_BM + row] = 0;
+    int abuf = 0;
+    uint32_t aphase = 0;
+    UnitIter u;
+    u.start(S, nkb, chunk_kb);
+    for (; u.valid(); u.next()) {
+      // one lane waits, the warp follows it, so the warp-wide tcgen05.ld stays convergent
+      int okw = lane == 0 ? (int)mbar_wait(accf(abuf), aphase, abort_flag, h, budget_ns) : 0;
+      okw = __shfl_sync(0xffffffffu, okw, 0);
+      if (!okw) break;
+      tc_fence_after();
+      const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(abuf * 128);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        uint32_t rr[16], ri[16], ir[16], ii[16];
+        tc_ld16(base + half * 16, rr);
+        tc_ld16(base + 32 + half * 16, ri);
+        tc_ld16(base + 64 + half * 16, ir);
+        tc_ld16(base + 96 + half * 16, ii);
+        tc_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c = half * 16 + j;
+          const long long re = (long long)__float2int_rn(__uint_as_float(rr[j])) -
+                               (long long)__float2int_rn(__uint_as_float(ii[j]));
+          const long long im = (long long)__float2int_rn(__uint_as_float(ri[j])) +
+                               (long long)__float2int_rn(__uint_as_float(ir[j]));
+          T[(0 * TC_NC + c) * TC_BM + row] += re;
+          T[(1 * TC_NC + c) * TC_BM + row] += im;
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(acce(abuf));
+      if (++abuf == 2) {
+        abuf = 0;
+        aphase ^= 1;
+      }
+      if (u.last_of_order()) {  // add this slice order's sums to Y in FP64
+        const int er = gm < M ? E[gm] : INT32_MIN;
+        for (int c = 0; c < TC_NC; ++c) {
+          const int gn = n0 + c;
+          long long& tre = T[(0 * TC_NC + c) * TC_BM + row];
+          long long& tim = T[(1 * TC_NC + c) * TC_BM + row];
+          if (gm < M && gn < N) {
+            const int fc = F[gn];
+            double2 y = cmk(0.0, 0.0);
+            if (er != INT32_MIN && fc != INT32_MIN) {
+              const double sc = pow2(er + fc - OZ_BETA * u.d);
+              y = cmk((double)tre * sc, (double)tim * sc);
+            }
+            double2* py = Y + (int64_t)gm * N + gn;
+            if (u.d == 2) {
+              *py = y;
+            } else {
+              const double2 o = *py;
+              *py = cmk(o.x + y.x, o.y + y.y);
+            }
+          }
+          tre = 0;
+          tim = 0;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -313,10 +665,11 @@ struct OzLayout {
   size_t us = 0, xs = 0, e = 0, f = 0, total = 0;
 };
 
+// Workspace: 512-byte status header, U slices, X slices, row / column exponents.
 OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int S) {
   OzLayout L;
   L.Kp = round_up(K, OZ_KALIGN);
-  size_t off = 0;
+  size_t off = sizeof(mm::WsHeader);
   L.us = off;
   off = round_up(off + (size_t)S * 2 * M * L.Kp * sizeof(__nv_bfloat16), 256);
   L.xs = off;
@@ -327,6 +680,49 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int S) {
   off = round_up(off + (size_t)N * sizeof(int), 256);
   L.total = off;
   return L;
+}
+// MM_OZAKI_LEGACY_MMA=1 selects the warp-level mma.sync kernel instead of tcgen05 (comparison only).
+bool mode_legacy_mma() {
+  static const bool v = [] {
+    const char* e = getenv("MM_OZAKI_LEGACY_MMA");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// 2-D BF16 tensor map over `rows` x `cols` (row-major, cols contiguous), box {64, box_rows}, 128-byte swizzle.
+bool make_map(CUtensorMap* map, void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {cols * 2};
+  const cuuint32_t box[2] = {64, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+uint64_t tc_budget_ns() {
+  static uint64_t v = [] {
+    const char* e = getenv("MM_WAIT_BUDGET_NS");
+    return e ? strtoull(e, nullptr, 10) : 2000000000ull;
+  }();
+  return v;
 }
 }  // namespace
 
@@ -369,9 +765,24 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
   col_exp_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, F);
   split_u_kernel<<<(unsigned)((M * Kp + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, Us);
   split_x_kernel<<<(unsigned)((N * Kp + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, Kp, slices, F, Xs);
-  dim3 grid((unsigned)((N + OZ_BN - 1) / OZ_BN), (unsigned)((M + OZ_BM - 1) / OZ_BM));
+  if (mode_legacy_mma()) {
+    dim3 grid((unsigned)((N + OZ_BN - 1) / OZ_BN), (unsigned)((M + OZ_BM - 1) / OZ_BM));
+    if (grid.y > 65535) return MM_ERR_TOO_LARGE;
+    ozaki_mma_kernel<<<grid, 128, 0, st>>>(Us, Xs, E, F, (double2*)Y, (int)M, (int)N, Kp, slices);
+    return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
+  }
+  CUtensorMap tu, tx;
+  if (!make_map(&tu, Us, (uint64_t)slices * 2 * M, (uint64_t)Kp, TC_BM) ||
+      !make_map(&tx, Xs, (uint64_t)slices * 2 * N, (uint64_t)Kp, TC_NC))
+    return MM_ERR_UNSUPPORTED;
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
+  });
+  dim3 grid((unsigned)((N + TC_NC - 1) / TC_NC), (unsigned)((M + TC_BM - 1) / TC_BM));
   if (grid.y > 65535) return MM_ERR_TOO_LARGE;
-  ozaki_mma_kernel<<<grid, 128, 0, st>>>(Us, Xs, E, F, (double2*)Y, (int)M, (int)N, Kp, slices);
+  ozaki_tc_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices,
+                                                           reinterpret_cast<mm::WsHeader*>(w), tc_budget_ns());
   return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
 }
 

@@ -96,7 +96,9 @@ class RaggedBatch:
         return G
 
     def vjp(self, G, c, dLdG, out=None):
-        """(dA_flat, db_flat, dc) of every instance (holomorphic VJP, as vanilla_vjp_numba)."""
+        """(dA_flat, db_flat, dc) of every instance (holomorphic VJP, as vanilla_vjp_numba).
+
+        ``dLdG`` may be a pinned host tensor: the kernels then read it through the host link."""
         lib = _lib.load()
         G, c, dLdG = raw(G), raw(c), raw(dLdG)
         if out is None:
@@ -110,6 +112,41 @@ class RaggedBatch:
                    "mm_ragged_vjp")
         self._check("ragged vjp")
         return dA, db, dc
+
+    def step_host(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable: bool = False):
+        """One forward + VJP step with every input and output in pinned host memory.
+
+        A, b, c (small) are copied to the device; the forward writes G in device memory; G is
+        copied back on a second stream while the VJP runs; the VJP reads dL/dG straight from the
+        pinned host buffer through the host link (the GPU addresses pinned host memory directly),
+        so the 2 x |G| bytes of traffic overlap the FP64-bound compute instead of preceding and
+        following it.  Enqueued asynchronously on the current stream; synchronise (or record an
+        event) before reading the outputs.
+        """
+        cur = torch.cuda.current_stream(self.device)
+        if getattr(self, "_dev_bufs", None) is None:
+            mk = lambda n: torch.empty(n, dtype=torch.complex128, device=self.device)  # noqa: E731
+            self._dev_bufs = (mk(self.n_a), mk(self.n_b), mk(self.B), mk(self.total),
+                              (mk(self.n_a), mk(self.n_b), mk(self.B)))
+            self._copy_stream = torch.cuda.Stream(device=self.device)
+        A, b, c, G, grads = self._dev_bufs
+        for h in (dLdG_h, G_h):
+            if h.is_cuda or not h.is_pinned():
+                raise ValueError("dLdG_h and G_h must be pinned host tensors")
+        A.copy_(A_h, non_blocking=True)
+        b.copy_(b_h, non_blocking=True)
+        c.copy_(c_h, non_blocking=True)
+        self.forward(A, b, c, stable, out=G)
+        cs = self._copy_stream
+        cs.wait_stream(cur)
+        with torch.cuda.stream(cs):
+            G_h.copy_(G, non_blocking=True)
+        self.vjp(G, c, dLdG_h, out=grads)
+        dA_h.copy_(grads[0], non_blocking=True)
+        db_h.copy_(grads[1], non_blocking=True)
+        dc_h.copy_(grads[2], non_blocking=True)
+        cur.wait_stream(cs)
+        return G_h, (dA_h, db_h, dc_h)
 
     def capture(self, A, b, c, dLdG, stable: bool = False, warmup: int = 1):
         """Capture forward + VJP on static buffers into one CUDA graph.

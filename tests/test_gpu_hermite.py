@@ -439,3 +439,24 @@ def test_launch_count_increments(cuda):
     n0 = mm.launch_count()
     mm.vanilla_numba((4, 4), np.eye(2) * 0.1, np.ones(2) * 0.2, 1.0)
     assert mm.launch_count() >= n0 + 2
+
+
+def test_ragged_step_host_matches_device(cuda, oracle_lib):
+    """The host-buffer step (cotangent read from pinned host memory, G copied back while the
+    VJP runs) gives the same bits as the device-resident forward + VJP."""
+    shapes, As, bs, cs = _ragged_case(48, 21, cmax=9)
+    rb = mm.RaggedBatch(shapes)
+    A, b, c = rb.pack(As, bs, cs)
+    g = torch.as_tensor(cn(rb.total, 22), device=cuda)
+    G_ref = rb.forward(A, b, c).clone()
+    ref = [t.clone() for t in rb.vjp(G_ref, c, g)]
+    pin = lambda t: t.cpu().pin_memory()  # noqa: E731
+    A_h, b_h, c_h, g_h = pin(A), pin(b), pin(c), pin(g)
+    G_h = torch.empty(rb.total, dtype=torch.complex128).pin_memory()
+    outs = [torch.empty(n, dtype=torch.complex128).pin_memory() for n in (rb.n_a, rb.n_b, rb.B)]
+    for _ in range(2):
+        rb.step_host(A_h, b_h, c_h, g_h, G_h, *outs)
+        torch.cuda.synchronize()
+        assert torch.equal(G_h, G_ref.cpu())
+        for o, r in zip(outs, ref):
+            assert torch.equal(o, r.cpu())
