@@ -31,6 +31,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Fock amplitudes/s fwd+VJP (c128, <=1e-12 rel) batched vs plain, 1 GB300"
 UNIT = "amplitudes/s"
 N_INST = 4096
+VJP_DRAM_BYTES_PER_AMP = 50.3  # dram read + write per amplitude, ncu capture of the VJP items kernel
 
 
 # ------------------------------------------------------------------ workload
@@ -320,10 +321,9 @@ def run_gb300(args, rank, local_rank, world):
     else:
         dom, t_dom, bytes_dom, ops_dom = "fwd_cta_kernel", t_fwd, 16.0 * total, fwd_ops
     achieved_gbs = bytes_dom / (t_dom * 1e-3) / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get(dom)
+    # DRAM bytes per launch from one ncu capture of the VJP on a 1024-triple batch
+    # (profiles/ncu_vjp_items_d4_ragged1024.md: 50.3 B per amplitude), scaled by amplitudes
+    traffic = VJP_DRAM_BYTES_PER_AMP * total if dom == "vjp_items_kernel" else None
 
     extras = {}
     if args.skip_extras:

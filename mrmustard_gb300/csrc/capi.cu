@@ -332,13 +332,12 @@ int ragged_build(mm_ragged_plan* p) {
   p->small.clear();
   p->big.clear();
   for (int32_t k : p->order) (p->desc[k].g.n >= thr ? p->big : p->small).push_back(k);
-  // VJP items: grouped by D (one launch per D), instances by decreasing size
-  std::vector<int32_t> byD(p->order);
-  std::stable_sort(byD.begin(), byD.end(), [&](int32_t a, int32_t b) { return p->desc[a].g.D < p->desc[b].g.D; });
+  // VJP items: one launch over every item; instances by decreasing cost, so the
+  // largest items are scheduled first (longest-processing-time order)
   p->items.clear();
   p->d_item_begin.assign(MM_MAXD + 1, 0);
   p->d_item_count.assign(MM_MAXD + 1, 0);
-  for (int32_t k : byD) {
+  for (int32_t k : p->order) {
     InstDesc& d = p->desc[k];
     uint32_t fpi;
     int64_t nit;
@@ -346,7 +345,6 @@ int ragged_build(mm_ragged_plan* p) {
     d.item_begin = (int64_t)p->items.size();
     d.n_items = nit;
     d.fibers_per_item = fpi;
-    if (p->d_item_count[d.g.D] == 0) p->d_item_begin[d.g.D] = d.item_begin;
     p->d_item_count[d.g.D] += nit;
     for (int64_t r = 0; r < nit; ++r) {
       VjpItem it;
@@ -638,9 +636,14 @@ int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c
   if ((rc = launch_setup(src, plan->B, w, plan->L, 0, st))) return rc;
   double2* partials = reinterpret_cast<double2*>(w + plan->L.partials);
   Tables T = tables_of(w, plan->L);
-  for (int D = 1; D <= MM_MAXD; ++D) {
-    if (plan->d_item_count[D] == 0) continue;
-    if ((rc = launch_vjp_items(D, src, T, partials, plan->d_item_begin[D], plan->d_item_count[D], st))) return rc;
+  const int64_t n_items = (int64_t)plan->items.size();
+  for (int64_t done = 0; done < n_items;) {
+    const unsigned nb = (unsigned)std::min<int64_t>(n_items - done, INT32_MAX);
+    if (plan->maxD <= 2) vjp_items_kernel<1, 2, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+    else if (plan->maxD <= 4) vjp_items_kernel<1, 4, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+    else vjp_items_kernel<1, 8, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+    MM_LAUNCHED();
+    done += nb;
   }
   return launch_vjp_reduce(src, plan->B, partials, (double2*)dA, (double2*)db, (double2*)dc, st);
 }

@@ -111,16 +111,24 @@ __global__ void __launch_bounds__(256) row_exp_kernel(const double2* __restrict_
   if (lane == 0) E[warp] = m;
 }
 
-// Column exponents of X (K x N): F[c] = max over the column.
+// Column exponents of X (K x N): F[c] = max over the column.  A CTA of 256
+// threads covers 32 columns: 8 row strides x 32 columns, coalesced along the row.
 __global__ void __launch_bounds__(256) col_exp_kernel(const double2* __restrict__ X, int K, int N, int* __restrict__ F) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= N) return;
+  __shared__ int part[8][32];
+  const int cl = threadIdx.x & 31, rl = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + cl;
   int m = INT32_MIN;
-  for (int k = 0; k < K; ++k) {
-    const double2 v = __ldg(X + (int64_t)k * N + c);
-    m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
+  if (c < N)
+    for (int k = rl; k < K; k += 8) {
+      const double2 v = __ldg(X + (int64_t)k * N + c);
+      m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
+    }
+  part[rl][cl] = m;
+  __syncthreads();
+  if (rl == 0 && c < N) {
+    for (int r = 1; r < 8; ++r) m = max(m, part[r][cl]);
+    F[c] = m;
   }
-  F[c] = m;
 }
 
 // Slices of one value against exponent bound E: out[p] for p < S.
@@ -762,7 +770,7 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
   int* F = reinterpret_cast<int*>(w + L.f);
   const int Kp = (int)L.Kp;
   row_exp_kernel<<<(unsigned)((M * 32 + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, E);
-  col_exp_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, F);
+  col_exp_kernel<<<(unsigned)((N + 31) / 32), 256, 0, st>>>((const double2*)X, (int)K, (int)N, F);
   split_u_kernel<<<(unsigned)((M * Kp + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, Us);
   split_x_kernel<<<(unsigned)((N * Kp + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, Kp, slices, F, Xs);
   if (mode_legacy_mma()) {
