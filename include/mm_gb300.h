@@ -167,6 +167,8 @@ MM_API int mm_ragged_plan_offsets(const mm_ragged_plan *plan, int64_t *g_off, in
  *   vjp_item_amps:  target amplitudes per VJP work item.
  */
 MM_API int mm_ragged_plan_set_tuning(mm_ragged_plan *plan, int64_t team_min_amps, int64_t vjp_item_amps);
+/* CTAs per cluster team for the large instances: 1 (no teams), 2, 4, 8 (default) or 16. */
+MM_API int mm_ragged_plan_set_team_size(mm_ragged_plan *plan, int cluster_ctas);
 /* Copy the plan's descriptors and work queues into ws (blocks the host until copied). */
 MM_API int mm_ragged_plan_upload(const mm_ragged_plan *plan, void *ws, size_t ws_bytes, mm_stream_t stream);
 

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 from ._build_ext import build as build_library
 from .autograd import HermiteRenormalizedFn, hermite_renormalized_autograd
+from .autotune import autotune
 from .backend import BackendGB300
 from .fock import apply_unitary, fock_gemm
 from .hermite import (
@@ -46,6 +47,7 @@ __all__ = [
     "HermiteRenormalizedFn",
     "RaggedBatch",
     "apply_unitary",
+    "autotune",
     "build_library",
     "fock_gemm",
     "device_fwd",

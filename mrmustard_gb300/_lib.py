@@ -51,6 +51,7 @@ SIGNATURES = {
     "mm_ragged_plan_amplitudes": (I64, [P]),
     "mm_ragged_plan_offsets": (I32, [P, P, P, P]),
     "mm_ragged_plan_set_tuning": (I32, [P, I64, I64]),
+    "mm_ragged_plan_set_team_size": (I32, [P, I32]),
     "mm_ragged_plan_upload": (I32, [P, P, SZ, P]),
     "mm_ragged_fwd": (I32, [P, P, P, P, I32, P, P, SZ, P]),
     "mm_ragged_vjp": (I32, [P, P, P, P, P, P, P, P, SZ, P]),

@@ -319,6 +319,7 @@ struct mm_ragged_plan {
   int64_t total_amps = 0;
   int64_t total_coef = 0;
   int64_t team_min_amps = 0;
+  int team_cluster = kTeamCluster;  // CTAs per cluster team (1 = no teams)
   int64_t vjp_item_amps = kVjpItemAmps;
   Layout L;
 };
@@ -331,7 +332,8 @@ int ragged_build(mm_ragged_plan* p) {
   if (thr == 0) thr = std::max<int64_t>(65536, p->total_amps / (4 * 152));  // about 1/4 of an SM's share
   p->small.clear();
   p->big.clear();
-  for (int32_t k : p->order) (p->desc[k].g.n >= thr ? p->big : p->small).push_back(k);
+  for (int32_t k : p->order)
+    (p->team_cluster > 1 && p->desc[k].g.n >= thr ? p->big : p->small).push_back(k);
   // VJP items: one launch over every item; instances by decreasing cost, so the
   // largest items are scheduled first (longest-processing-time order)
   p->items.clear();
@@ -382,10 +384,12 @@ template <int DHI>
 int launch_team_D(const mm_ragged_plan* p, const RaggedSrc& src, char* w, const double* rs, int stable,
                   cudaStream_t st) {
   auto kern = fwd_ragged_team_kernel<1, DHI>;
+  const int cl = p->team_cluster;
+  if (cl > 8) MM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kTeamCluster;
+  attr[0].val.clusterDim.x = cl;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(MM_BLOCK);
@@ -393,11 +397,11 @@ int launch_team_D(const mm_ragged_plan* p, const RaggedSrc& src, char* w, const 
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cfg.gridDim = dim3(kTeamCluster);
+  cfg.gridDim = dim3(cl);
   int ncl = 0;
   MM_CUDA(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg));
   if (ncl < 1) return MM_ERR_UNSUPPORTED;
-  cfg.gridDim = dim3((unsigned)(ncl * kTeamCluster));
+  cfg.gridDim = dim3((unsigned)(ncl * cl));
   const int32_t* small = reinterpret_cast<const int32_t*>(w + p->L.big);
   const int32_t* big = small + p->small.size();
   WsHeader* h = reinterpret_cast<WsHeader*>(w);
@@ -568,6 +572,14 @@ int mm_ragged_plan_set_tuning(mm_ragged_plan* plan, int64_t team_min_amps, int64
   if (!plan || team_min_amps < 0 || vjp_item_amps < 1) return MM_ERR_INVALID_ARG;
   plan->team_min_amps = team_min_amps;
   plan->vjp_item_amps = vjp_item_amps;
+  return ragged_build(plan);
+}
+
+int mm_ragged_plan_set_team_size(mm_ragged_plan* plan, int cluster_ctas) {
+  if (!plan || (cluster_ctas != 1 && cluster_ctas != 2 && cluster_ctas != 4 && cluster_ctas != 8 &&
+                cluster_ctas != 16))
+    return MM_ERR_INVALID_ARG;
+  plan->team_cluster = cluster_ctas;
   return ragged_build(plan);
 }
 

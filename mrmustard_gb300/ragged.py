@@ -50,8 +50,35 @@ class RaggedBatch:
         self.total = int(lib.mm_ragged_plan_amplitudes(plan))
         self.n_a = int((self.D.astype(np.int64) ** 2).sum())
         self.n_b = int(self.D.sum())
-        self.ws = Workspace(lib.mm_ragged_plan_workspace_bytes(plan), self.device)
-        _lib.check(lib.mm_ragged_plan_upload(plan, self.ws.ptr, self.ws.nbytes, _stream()), "mm_ragged_plan_upload")
+        self.tuning = {"team_min_amps": int(team_min_amps or 0), "vjp_item_amps": int(vjp_item_amps or 65536),
+                       "team_cluster": 8}
+        self._upload()
+
+    def _upload(self):
+        lib = _lib.load()
+        self.ws = Workspace(lib.mm_ragged_plan_workspace_bytes(self._plan), self.device)
+        _lib.check(lib.mm_ragged_plan_upload(self._plan, self.ws.ptr, self.ws.nbytes, _stream()),
+                   "mm_ragged_plan_upload")
+
+    def retune(self, team_min_amps: int | None = None, vjp_item_amps: int | None = None,
+               team_cluster: int | None = None):
+        """Re-plan with new schedule settings (see mm_ragged_plan_set_tuning / _set_team_size)
+        and upload the new plan; results are unchanged, only the work split differs."""
+        lib = _lib.load()
+        t = dict(self.tuning)
+        if team_min_amps is not None:
+            t["team_min_amps"] = int(team_min_amps)
+        if vjp_item_amps is not None:
+            t["vjp_item_amps"] = int(vjp_item_amps)
+        if team_cluster is not None:
+            t["team_cluster"] = int(team_cluster)
+        _lib.check(lib.mm_ragged_plan_set_tuning(self._plan, t["team_min_amps"], t["vjp_item_amps"]),
+                   "mm_ragged_plan_set_tuning")
+        _lib.check(lib.mm_ragged_plan_set_team_size(self._plan, t["team_cluster"]), "mm_ragged_plan_set_team_size")
+        self.tuning = t
+        torch.cuda.synchronize(self.device)
+        self._upload()
+        return t
 
     def __del__(self):
         plan = getattr(self, "_plan", None)

@@ -460,3 +460,101 @@ def test_ragged_step_host_matches_device(cuda, oracle_lib):
         assert torch.equal(G_h, G_ref.cpu())
         for o, r in zip(outs, ref):
             assert torch.equal(o, r.cpu())
+
+
+def test_ragged_schedules_agree(cuda, oracle_lib):
+    """Every schedule (cluster teams of 1..16 CTAs, thresholds, VJP item sizes) gives the same
+    forward bits and a VJP within tolerance of the oracle; the autotuner picks one of them."""
+    shapes, As, bs, cs = _ragged_case(40, 31, cmax=16)
+    rb = mm.RaggedBatch(shapes)
+    A, b, c = rb.pack(As, bs, cs)
+    g = torch.as_tensor(cn(rb.total, 32), device=cuda)
+    G0 = rb.forward(A, b, c).clone()
+    for cl, tm in ((1, 0), (2, 64), (4, 256), (8, 1000), (16, 500)):
+        try:
+            rb.retune(team_min_amps=tm, team_cluster=cl)
+        except _lib.MMError:
+            continue
+        assert torch.equal(rb.forward(A, b, c), G0), (cl, tm)
+    Gs, gs = rb.unpack(G0.cpu().numpy()), rb.unpack(g.cpu().numpy())
+    for it in (256, 4096, 1 << 16):
+        rb.retune(vjp_item_amps=it)
+        dA, db, dc = rb.vjp(G0, c, g)
+        dAs, dbs = rb.unpack_grads(dA.cpu().numpy(), db.cpu().numpy())
+        for k in range(0, len(shapes), 7):
+            rA, rbb, _ = oracle_lib.vjp(Gs[k], cs[k], gs[k])
+            assert rel(dAs[k], rA) < VJP_TOL and rel(dbs[k], rbb) < VJP_TOL
+    choice = mm.autotune(rb, A, b, c, g, reps=1, use_cache=False)
+    assert choice["team_cluster"] in (4, 8, 16) and choice["vjp_item_amps"] > 0
+    assert torch.equal(rb.forward(A, b, c), G0)
+
+
+def test_cfg4_gradient_d4_cutoff30(cuda, oracle_lib):
+    """4-mode triple at cutoff 30: dA, db, dc vs central differences (h = 1e-6, real
+    perturbations, holomorphic) of L = sum(dLdG * G) and vs the oracle's vanilla_vjp."""
+    A, b, c = takagi(4, 0.8, 1401)
+    c = 0.9 - 0.2j
+    shape = (30,) * 4
+    g = cn(shape, 1402)
+    At, bt = torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda)
+    ct = torch.tensor(c, dtype=torch.complex128, device=cuda)
+    gt = torch.as_tensor(g, device=cuda)
+    G = mm.device_fwd(At, bt, ct, shape)
+    dA, db, dc = (x.cpu().numpy() for x in mm.device_vjp(G, ct, gt, batched=False))
+    rA, rb_, rc = oracle_lib.vjp(G.cpu().numpy(), c, g)
+    assert rel(dA, rA) < VJP_TOL and rel(db, rb_) < VJP_TOL and abs(dc - rc) <= VJP_TOL * abs(rc)
+
+    def L(A_, b_, c_):
+        Gx = mm.device_fwd(torch.as_tensor(A_, device=cuda), torch.as_tensor(b_, device=cuda),
+                           torch.tensor(c_, dtype=torch.complex128, device=cuda), shape)
+        return complex((gt * Gx).sum().item())
+
+    h = 1e-6
+    scale = max(np.abs(dA).max(), np.abs(db).max())
+    for i in range(4):
+        e = np.zeros(4)
+        e[i] = h
+        fd = (L(A, b + e, c) - L(A, b - e, c)) / (2 * h)
+        assert abs(fd - db[i]) < 1e-6 * scale
+        j = (i + 1) % 4
+        E = np.zeros((4, 4))
+        E[i, j] = E[j, i] = h
+        fd = (L(A + E, b, c) - L(A - E, b, c)) / (2 * h)  # symmetric perturbation = dA_ij + dA_ji
+        assert abs(fd - 2 * dA[i, j]) < 1e-6 * scale
+    fd = (L(A, b, c + h) - L(A, b, c - h)) / (2 * h)
+    assert abs(fd - dc) < 1e-6 * max(1.0, abs(dc))
+
+
+def test_cfg4_batched_fidelity_step(cuda):
+    """64-instance batched gradient step: loss = sum_k 1 - |<T, G_k>|^2 / <G_k, G_k> with a fixed
+    random normalised target T; autograd gradients vs central differences on sampled entries."""
+    B, shape = 64, (30,) * 4
+    trip = [takagi(4, 0.8, 1500 + k) for k in range(B)]
+    A = torch.as_tensor(np.stack([t[0] for t in trip]), device=cuda).requires_grad_(True)
+    b = torch.as_tensor(np.stack([t[1] for t in trip]), device=cuda).requires_grad_(True)
+    c = torch.ones(B, dtype=torch.complex128, device=cuda, requires_grad=True)
+    T = torch.as_tensor(cn(shape, 1600), device=cuda)
+    T = T / T.abs().pow(2).sum().sqrt()
+
+    def loss(A_, b_, c_):
+        G = mm.hermite_renormalized_autograd(A_, b_, c_, shape)  # (B, 30, 30, 30, 30)
+        ov = (T.conj() * G).sum(dim=(1, 2, 3, 4))
+        return (1 - ov.abs() ** 2 / G.abs().pow(2).sum(dim=(1, 2, 3, 4))).sum()
+
+    l0 = loss(A, b, c)
+    l0.backward()
+    assert torch.isfinite(A.grad).all() and torch.isfinite(b.grad).all()
+    h = 1e-6
+    with torch.no_grad():
+        for k, i in ((0, 0), (17, 2), (63, 3)):
+            for part in (1.0, 1j):
+                e = torch.zeros_like(b)
+                e[k, i] = h * part
+                fd = (loss(A, b + e, c) - loss(A, b - e, c)).item() / (2 * h)
+                got = b.grad[k, i].real if part == 1.0 else b.grad[k, i].imag
+                assert abs(fd - got.item()) < 1e-6
+            j = (i + 1) % 4
+            E = torch.zeros_like(A)
+            E[k, i, j] = E[k, j, i] = h
+            fd = (loss(A + E, b, c) - loss(A - E, b, c)).item() / (2 * h)
+            assert abs(fd - (A.grad[k, i, j] + A.grad[k, j, i]).real.item()) < 1e-6
