@@ -391,22 +391,23 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     h2d = sum(t.numel() * 16 for t in (A_h, b_h, c_h, g_h))
     d2h = sum(t.numel() * 16 for t in (G_h, dA_h, db_h, dc_h))
 
-    def e2e_step():
-        rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h)
-
     e2e_steps = max(2, min(args.steps, 5))
-    with mm.settings(CHECK_DEVICE_STATUS=False):
-        e2e_step()
-        torch.cuda.synchronize()
-        barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(e2e_steps):
-            e2e_step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_modes = {}
+    for mode in ("prefetch", "zero_copy"):
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode)
+            torch.cuda.synchronize()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(e2e_steps):
+                rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+        e2e_modes[mode] = e0.elapsed_time(e1) / e2e_steps
+    e2e_mode = min(e2e_modes, key=e2e_modes.get)
+    e2e_ms = e2e_modes[e2e_mode]
     rb.ws.check_status("e2e")
 
     # --- plain per-instance GPU path on a sample of instances (scaled to amplitudes/s)
@@ -443,7 +444,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
         cpu = {"value": total / tc, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
                "sample": f"all {len(shapes)} instances ({total} amplitudes), one fwd+VJP pass, {tc:.2f} s"}
 
-    extras = {}
+    extras = {"e2e_cotangent_ms": e2e_modes, "e2e_cotangent_path": e2e_mode}
     # --- single large recurrences (4 modes at cutoff 40, pure; 4-index DM triple at cutoff 50): one
     #     instance on the whole GPU
     single = {}
@@ -469,7 +470,17 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
                         "hbm_gbs": 16.0 * n1 / (t1 * 1e-3) / 1e9}
     extras["single_instance_forward"] = single
 
-    # --- Fock contraction: 2-mode gate tensor at cutoff 50 (2500 x 2500) on 256 kets
+    extras["fock_contraction"] = run_contraction(dev, time_eager)
+    return e2e_ms, h2d, d2h, plain_value, cpu, extras
+
+
+def run_contraction(dev, time_eager):
+    """Gate tensor at cutoff 50 (2500 x 2500, built by the recurrence) applied to 256 kets: FP64 and
+    Ozaki tensor-core paths, timed with CUDA events, error against numpy's zgemm on the host."""
+    import torch
+
+    import mrmustard_gb300 as mm
+
     rng = np.random.default_rng(55)
     X5 = rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))
     A5 = X5 + X5.T
@@ -486,16 +497,14 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     ref5 = U5h @ Xkh
     t_np = time.perf_counter() - t0
     flops = 8.0 * 2500 * 256 * 2500
-    contraction = {"shape": "2500x2500 @ 2500x256 complex128", "flops": flops,
-                   "numpy_zgemm_ms": t_np * 1e3}
+    contraction = {"shape": "2500x2500 @ 2500x256 complex128", "flops": flops, "numpy_zgemm_ms": t_np * 1e3}
     for mode in ("fp64", "ozaki"):
         with mm.settings(CHECK_DEVICE_STATUS=False):
             tm = time_eager(lambda: mm.fock_gemm(U5, Xk, mode), reps=5)
         Y = mm.fock_gemm(U5, Xk, mode).cpu().numpy()
         err = float(np.abs(Y - ref5).max() / np.abs(ref5).max())
         contraction[mode] = {"ms": tm, "tflops": flops / (tm * 1e-3) / 1e12, "max_rel_err_vs_fp64_cpu": err}
-    extras["fock_contraction"] = contraction
-    return e2e_ms, h2d, d2h, plain_value, cpu, extras
+    return contraction
 
 
 def rb_order_largest(rb, n):
@@ -511,11 +520,32 @@ def main(argv=None):
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-oracle baseline leg")
     ap.add_argument("--instances", type=int, default=N_INST, help="triples in the ragged batch (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's default schedule")
+    ap.add_argument("--only-contraction", action="store_true",
+                    help="run only the Fock-contraction leg (gate tensor on 256 kets) and print its figures")
     ap.add_argument("--skip-extras", action="store_true",
                     help="time only the headline step (no e2e, per-instance loop, contraction, CPU legs)")
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()
+    if args.only_contraction:
+        import torch
+
+        dev = torch.device("cuda", local_rank)
+        torch.cuda.set_device(dev)
+
+        def time_eager(fn, reps=3):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        print(json.dumps({"fock_contraction": run_contraction(dev, time_eager)}), flush=True)
+        return 0
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_gb300(args, rank, local_rank, world)

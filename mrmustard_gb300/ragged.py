@@ -140,35 +140,56 @@ class RaggedBatch:
         self._check("ragged vjp")
         return dA, db, dc
 
-    def step_host(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable: bool = False):
+    def step_host(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable: bool = False,
+                  cotangent: str = "prefetch"):
         """One forward + VJP step with every input and output in pinned host memory.
 
-        A, b, c (small) are copied to the device; the forward writes G in device memory; G is
-        copied back on a second stream while the VJP runs; the VJP reads dL/dG straight from the
-        pinned host buffer through the host link (the GPU addresses pinned host memory directly),
-        so the 2 x |G| bytes of traffic overlap the FP64-bound compute instead of preceding and
-        following it.  Enqueued asynchronously on the current stream; synchronise (or record an
-        event) before reading the outputs.
+        A, b, c (small) are copied to the device and the forward writes G in device memory; G is
+        copied back on a second stream while the VJP runs.  The cotangent dL/dG reaches the VJP in
+        one of two ways, both overlapped with compute:
+
+        * ``"prefetch"``: copied into device memory on the second stream while the forward runs;
+        * ``"zero_copy"``: read by the VJP kernels straight from the pinned host buffer over the
+          host link (the GPU addresses pinned host memory directly; no device copy is kept).
+
+        Enqueued asynchronously on the current stream; synchronise before reading the outputs.
         """
+        if cotangent not in ("prefetch", "zero_copy"):
+            raise ValueError("cotangent must be 'prefetch' or 'zero_copy'")
         cur = torch.cuda.current_stream(self.device)
         if getattr(self, "_dev_bufs", None) is None:
             mk = lambda n: torch.empty(n, dtype=torch.complex128, device=self.device)  # noqa: E731
             self._dev_bufs = (mk(self.n_a), mk(self.n_b), mk(self.B), mk(self.total),
                               (mk(self.n_a), mk(self.n_b), mk(self.B)))
             self._copy_stream = torch.cuda.Stream(device=self.device)
+        if cotangent == "prefetch" and getattr(self, "_g_dev", None) is None:
+            self._g_dev = torch.empty(self.total, dtype=torch.complex128, device=self.device)
         A, b, c, G, grads = self._dev_bufs
-        for h in (dLdG_h, G_h):
-            if h.is_cuda or not h.is_pinned():
+        for hbuf in (dLdG_h, G_h):
+            if hbuf.is_cuda or not hbuf.is_pinned():
                 raise ValueError("dLdG_h and G_h must be pinned host tensors")
+        cs = self._copy_stream
+        cs.wait_stream(cur)  # the previous step's readers of G and of the cotangent buffer are done
+        if cotangent == "prefetch":
+            with torch.cuda.stream(cs):
+                self._g_dev.copy_(dLdG_h, non_blocking=True)
+                g_ready = torch.cuda.Event()
+                g_ready.record(cs)
         A.copy_(A_h, non_blocking=True)
         b.copy_(b_h, non_blocking=True)
         c.copy_(c_h, non_blocking=True)
         self.forward(A, b, c, stable, out=G)
-        cs = self._copy_stream
-        cs.wait_stream(cur)
+        fwd_done = torch.cuda.Event()
+        fwd_done.record(cur)
         with torch.cuda.stream(cs):
+            cs.wait_event(fwd_done)
             G_h.copy_(G, non_blocking=True)
-        self.vjp(G, c, dLdG_h, out=grads)
+        if cotangent == "prefetch":
+            cur.wait_event(g_ready)
+            g = self._g_dev
+        else:
+            g = dLdG_h
+        self.vjp(G, c, g, out=grads)
         dA_h.copy_(grads[0], non_blocking=True)
         db_h.copy_(grads[1], non_blocking=True)
         dc_h.copy_(grads[2], non_blocking=True)

@@ -454,8 +454,8 @@ def test_ragged_step_host_matches_device(cuda, oracle_lib):
     A_h, b_h, c_h, g_h = pin(A), pin(b), pin(c), pin(g)
     G_h = torch.empty(rb.total, dtype=torch.complex128).pin_memory()
     outs = [torch.empty(n, dtype=torch.complex128).pin_memory() for n in (rb.n_a, rb.n_b, rb.B)]
-    for _ in range(2):
-        rb.step_host(A_h, b_h, c_h, g_h, G_h, *outs)
+    for mode in ("prefetch", "zero_copy", "prefetch"):
+        rb.step_host(A_h, b_h, c_h, g_h, G_h, *outs, cotangent=mode)
         torch.cuda.synchronize()
         assert torch.equal(G_h, G_ref.cpu())
         for o, r in zip(outs, ref):
