@@ -19,8 +19,11 @@ thread_local char g_last_cuda_error[256] = "";
 std::atomic<int64_t> g_launches{0};
 
 constexpr int64_t kGridMinAmps = 8192;     // single instances at least this large use the whole grid
-constexpr uint32_t kSmallChunk = 256;      // grid kernel: chunks smaller than this run on CTA 0
-constexpr int kGridBlock = 512;            // threads per CTA of the cooperative grid kernel
+constexpr int kGridBlock = 512;            // threads per CTA of the cooperative stable kernel
+constexpr int kFlowBlock = 256;            // dataflow forward: threads per CTA
+constexpr int kFlowPerSm = 2;              // dataflow forward: CTAs per SM (capped by occupancy)
+constexpr int kFlowMaxPerSm = 8;           // bound used to size the progress words
+constexpr uint32_t kFlowMinAmps = 128;     // dataflow forward: fewest amplitudes of a chunk per CTA
 constexpr int64_t kVjpItemAmps = 65536;    // default amplitudes per VJP work item
 constexpr int kTeamCluster = 8;            // CTAs per cluster for the large instances of a ragged batch
 constexpr size_t kAlign = 256;
@@ -125,13 +128,15 @@ void vjp_split(const Geom& g, int64_t target_amps, uint32_t& fpi, int64_t& items
 
 // Workspace regions shared by every entry point.
 struct Layout {
-  size_t tables = 0, coef = 0, partials = 0, desc = 0, order = 0, big = 0, items = 0, total = 0;
-  int64_t kmax = 0;
+  size_t tables = 0, coef = 0, partials = 0, desc = 0, order = 0, big = 0, items = 0, flags = 0, total = 0;
+  int64_t kmax = 0, n_flags = 0;
 };
 
-Layout make_layout(int64_t kmax, int64_t coef_entries_total, int64_t n_items, int64_t n_desc, int64_t n_order) {
+Layout make_layout(int64_t kmax, int64_t coef_entries_total, int64_t n_items, int64_t n_desc, int64_t n_order,
+                   int64_t n_flags = 0) {
   Layout L;
   L.kmax = kmax;
+  L.n_flags = n_flags;
   size_t off = sizeof(WsHeader);
   L.tables = off;
   off = align_up(off + 3 * (size_t)kmax * sizeof(double));
@@ -147,6 +152,8 @@ Layout make_layout(int64_t kmax, int64_t coef_entries_total, int64_t n_items, in
   off = align_up(off + (size_t)n_order * sizeof(int32_t));
   L.items = off;
   off = align_up(off + (size_t)n_items * sizeof(VjpItem));
+  L.flags = off;
+  off = align_up(off + (size_t)n_flags * sizeof(uint32_t));
   L.total = off;
   return L;
 }
@@ -160,7 +167,9 @@ struct UniformPlan {
   Layout L;
 };
 
-int plan_uniform(int64_t B, int D, const int64_t* shape, UniformPlan& P, int sms) {
+// `fwd`: the plan includes the progress words of the dataflow forward (the last
+// workspace region, which the VJP does not use).
+int plan_uniform(int64_t B, int D, const int64_t* shape, UniformPlan& P, int sms, bool fwd = true) {
   int rc = make_geom(D, shape, P.g);
   if (rc) return rc;
   if (B < 0) return MM_ERR_INVALID_ARG;
@@ -171,7 +180,12 @@ int plan_uniform(int64_t B, int D, const int64_t* shape, UniformPlan& P, int sms
   int64_t per_inst = std::max<int64_t>(1, (want_items + std::max<int64_t>(B, 1) - 1) / std::max<int64_t>(B, 1));
   int64_t target = std::max<int64_t>(1, P.g.n / per_inst);
   vjp_split(P.g, target, P.fpi, P.items_per_inst);
-  P.L = make_layout(P.g.maxC + 1, B * coef_entries(P.g), B * P.items_per_inst, 0, 0);
+  // progress words of the dataflow forward (one large instance)
+  const int64_t n_flags =
+      (fwd && B == 1 && P.g.n >= kGridMinAmps)
+          ? 1 + (int64_t)MM_MAXD * kFlowMaxPerSm * std::max(sms, 1) + (int64_t)kFlowMaxSmid
+          : 0;
+  P.L = make_layout(P.g.maxC + 1, B * coef_entries(P.g), B * P.items_per_inst, 0, 0, n_flags);
   return MM_OK;
 }
 
@@ -222,20 +236,58 @@ int launch_setup(const Src& src, int64_t n_inst, char* ws, const Layout& L, int 
   return MM_OK;
 }
 
+// Tuning of the dataflow forward; MM_FLOW_BLOCK, MM_FLOW_PER_SM, MM_FLOW_MIN_AMPS
+// and MM_FLOW_EXCLUSIVE in the environment override the defaults.
+struct FlowTuning {
+  int block = kFlowBlock, per_sm = kFlowPerSm, exclusive = 1;
+  uint32_t min_amps = kFlowMinAmps;
+};
+
+FlowTuning flow_tuning() {
+  static FlowTuning t = [] {
+    FlowTuning r;
+    if (const char* e = getenv("MM_FLOW_BLOCK")) r.block = std::min(256, std::max(32, atoi(e)) / 32 * 32);
+    if (const char* e = getenv("MM_FLOW_PER_SM")) r.per_sm = std::min(kFlowMaxPerSm, std::max(1, atoi(e)));
+    if (const char* e = getenv("MM_FLOW_MIN_AMPS")) r.min_amps = (uint32_t)std::max(2, atoi(e));
+    if (const char* e = getenv("MM_FLOW_EXCLUSIVE")) r.exclusive = atoi(e) != 0;
+    return r;
+  }();
+  return t;
+}
+
 template <int D>
 int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, int stable, const DevInfo& di,
                          cudaStream_t st) {
   const double* rs = tables_of(ws, P.L).rs;
-  if (P.B == 1 && P.g.n >= kGridMinAmps && di.coop) {
+  WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+  if (P.B == 1 && P.g.n >= kGridMinAmps && di.coop && stable) {
     int per_sm = 0;
-    MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_grid_kernel<D>, kGridBlock, 0));
+    MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stable_grid_kernel<D>, kGridBlock, 0));
     if (per_sm >= 1) {
-      WsHeader* h = reinterpret_cast<WsHeader*>(ws);
-      uint32_t small = kSmallChunk;
       uint64_t budget = wait_budget_ns();
       UniformSrc s = src;
-      void* args[] = {&s, (void*)&rs, &h, &small, &budget, &stable};
-      MM_CUDA(cudaLaunchCooperativeKernel((void*)fwd_grid_kernel<D>, dim3(di.sms), dim3(kGridBlock), args, 0, st));
+      void* args[] = {&s, (void*)&rs, &h, &budget};
+      MM_CUDA(cudaLaunchCooperativeKernel((void*)stable_grid_kernel<D>, dim3(di.sms), dim3(kGridBlock), args, 0, st));
+      g_launches.fetch_add(1);
+      return MM_OK;
+    }
+  }
+  if (P.B == 1 && P.g.n >= kGridMinAmps && di.coop && !stable) {
+    const FlowTuning t = flow_tuning();
+    int occ = 0;
+    MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_flow_kernel<D>, t.block, 0));
+    if (occ >= 1) {
+      const int per_sm = std::min(occ, t.per_sm);
+      FlowPlan fp;
+      const int64_t n_flags = flow_plan(P.g, di.sms, per_sm, t.min_amps, t.exclusive, wait_budget_ns(), fp);
+      // progress words, then the SM registration words
+      if (n_flags + (int64_t)kFlowMaxSmid > P.L.n_flags) return MM_ERR_WORKSPACE;
+      uint32_t* prog = reinterpret_cast<uint32_t*>(ws + P.L.flags);
+      MM_CUDA(cudaMemsetAsync(prog, 0, (size_t)(n_flags + kFlowMaxSmid) * sizeof(uint32_t), st));
+      UniformSrc s = src;
+      void* args[] = {&s, (void*)&rs, &h, &prog, &fp};
+      MM_CUDA(cudaLaunchCooperativeKernel((void*)fwd_flow_kernel<D>, dim3(per_sm * di.sms), dim3(t.block), args, 0,
+                                          st));
       g_launches.fetch_add(1);
       return MM_OK;
     }
@@ -492,7 +544,7 @@ int mm_hermite_vjp_batched(int64_t B, int D, const int64_t* shape, const mm_c128
   int rc = common_checks(ws, stream, di);
   if (rc) return rc;
   UniformPlan P;
-  if ((rc = plan_uniform(B, D, shape, P, di.sms))) return rc;
+  if ((rc = plan_uniform(B, D, shape, P, di.sms, false))) return rc;
   if (B == 0) return MM_OK;
   if (!G || !c || !dLdG || !dA || !db || !dc) return MM_ERR_INVALID_ARG;
   if ((rc = check_ws(ws, ws_bytes, P.L.total))) return rc;
@@ -690,7 +742,7 @@ int mm_hermite_vjp_noalloc(int D, const int64_t* shape, const mm_c128* G, const 
   int rc = device_info(di);
   if (rc) return rc;
   UniformPlan P;
-  if ((rc = plan_uniform(1, D, shape, P, di.sms))) return rc;
+  if ((rc = plan_uniform(1, D, shape, P, di.sms, false))) return rc;
   if (P.L.total > MM_NOALLOC_SCRATCH_BYTES) return MM_ERR_TOO_LARGE;
   void* ws = nullptr;
   if ((rc = noalloc_scratch(&ws))) return rc;

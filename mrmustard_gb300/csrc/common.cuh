@@ -154,11 +154,15 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 #else  // host compilation of the device code (CPU emulation of the kernels' indexing)
 __device__ __forceinline__ uint64_t globaltimer_ns() { return 0; }
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
 __device__ __forceinline__ int32_t ld_relaxed_i32(const int32_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) { __atomic_store_n(p, v, __ATOMIC_RELEASE); }
 #endif
 
 // Progress signal for waits: a CTA that works alone while the others wait at a

@@ -16,6 +16,11 @@
 //   exactly; the final division by sqrt(m) becomes a multiply by 1/sqrt(m)
 //   and products are fused (DFMA), so results agree to rounding.
 //   Writes are contiguous (one chunk = one slab of the row-major tensor).
+//   One large instance on the whole GPU (fwd_flow_kernel) drops the per-chunk
+//   grid barrier: ranges of a chunk wait only for the ranges they read
+//   (progress words), the smallest levels run in one CTA's shared memory, and
+//   latency-bound chains split each amplitude's real and imaginary parts over
+//   a lane pair (same terms, products rounded per part).
 // stable (core.py:127-213).  Every valid pivot is averaged, so an amplitude also
 //   reads amplitudes of its own chunk; the schedule is the |k| anti-diagonal
 //   wavefront (all reads sit on wavefronts |k|-1 and |k|-2).
@@ -25,6 +30,9 @@
 //   the fiber and are applied once per fiber; the axis-0 weights are folded
 //   into the cotangent once per amplitude.
 #pragma once
+
+#include <algorithm>
+#include <cstring>
 
 #include "common.cuh"
 
@@ -493,54 +501,474 @@ __global__ void __launch_bounds__(MM_BLOCK) fwd_ragged_team_kernel(RaggedSrc src
 }
 
 // ------------------------------------------------ single large instance, whole grid
-// Cooperative launch (every CTA resident).  Levels whose chunks hold fewer than
-// `small_chunk` amplitudes run on CTA 0 alone; each larger chunk is split over
-// all CTAs in contiguous ranges with a bounded grid barrier after it.
+// Stable recurrence of one large instance: every anti-diagonal |k| = w is split
+// over all CTAs (cooperative launch) with a bounded grid barrier after it.
 template <int D>
-__global__ void __launch_bounds__(512) fwd_grid_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
-                                                       uint32_t small_chunk, uint64_t budget_ns, int stable) {
+__global__ void __launch_bounds__(512) stable_grid_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
+                                                          uint64_t budget_ns) {
   MM_SHARED(InstView, sv);
   if (threadIdx.x == 0) src.load(0, sv);
   __syncthreads();
   const Geom& g = sv.g;
   uint32_t epoch = 0;
-  if (!stable) {
-    int lvl_big = -1;  // levels 0..lvl_big use the whole grid
-    for (int i = 0; i < D; ++i)
-      if ((uint32_t)g.strides[i] >= small_chunk) lvl_big = i;
-    if (blockIdx.x == 0) {
-      if (threadIdx.x == 0) sv.G[0] = sv.c;
-      __syncthreads();
-      for (int i = D - 1; i > lvl_big; --i) {
-        const uint32_t si = (uint32_t)g.strides[i];
-        for (int m = 1; m < (int)g.shape[i]; ++m) {
-          fwd_chunk<D, false>(sv, rs, i, m, 0u, si, blockDim.x, threadIdx.x);
-          if (threadIdx.x == 0 && (m & 63) == 0) heartbeat(h);
-          __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) sv.G[0] = sv.c;
+  if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+  int wmax = 0;
+  for (int i = 0; i < D; ++i) wmax += (int)g.shape[i] - 1;
+  const uint32_t P = (uint32_t)(g.n / g.shape[D - 1]);
+  const uint32_t per = (P + gridDim.x - 1) / gridDim.x;
+  const uint32_t lo = min(P, per * blockIdx.x), hi = min(P, lo + per);
+  for (int w = 1; w <= wmax; ++w) {
+    stable_wave<D, true>(sv, rs, w, lo, hi, blockDim.x, threadIdx.x);
+    if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+  }
+}
+
+// ------------------------------------------------ dataflow forward of one large instance
+// Level i's chunk m (the slab k_0..k_{i-1} = 0, k_i = m) is split into ctas[i]
+// contiguous ranges of per[i] amplitudes; range v is computed by one CTA, which
+// then publishes prog[flag0[i] + v] = m.  Amplitude q of chunk m reads chunk
+// m-1 at q and at q - strides[j] (j > i), and chunk m-2 at q, so before chunk
+// m >= 2 a CTA waits only for the ranges of chunk m-1 that overlap
+// [lo - strides[i+1], hi); before chunk 1 it waits until the lower levels hold
+// every amplitude below its `hi`.  There is no grid-wide barrier per chunk.
+//
+// Levels >= small_lvl (positions [0, small_amps)) are latency-bound chains of
+// tiny chunks: one CTA computes them in shared memory, writes them out and
+// publishes them at once.  Levels 1 .. small_lvl-1 run on `face` CTAs, one per
+// SM; level 0 runs on the rest.  Roles come from the SM each CTA landed on
+// (%smid, registered once with one grid barrier): with `exclusive`, the other
+// CTAs on a face CTA's SM stay idle so the face's latency-bound chain owns its
+// SM's FP64 pipes, the face CTAs take the last level-0 ranges (they finish the
+// face last), and consecutive level-0 ranges go to different SMs so the ranges
+// that start last (after the face) run one per SM.
+struct FlowPlan {
+  uint32_t ctas[MM_MAXD];
+  uint32_t per[MM_MAXD];
+  uint32_t flag0[MM_MAXD];
+  uint32_t face;        // CTAs holding the ranges of levels 1 .. small_lvl-1 (at least 1)
+  uint32_t sms;         // SMs of the device
+  uint32_t per_sm;      // CTAs per SM of the launch (gridDim.x = per_sm * sms)
+  uint32_t exclusive;   // see above
+  uint32_t small_lvl;   // levels >= small_lvl live in shared memory (D: none)
+  uint32_t small_amps;  // strides[small_lvl - 1]: amplitudes of that region
+  uint64_t budget_ns;
+};
+
+constexpr uint32_t kFlowSmemAmps = 2560;  // shared-memory region of the small levels (40 KiB)
+constexpr uint32_t kFlowMaxSmid = 1024;   // SM-id registration words after the progress words
+constexpr uint32_t kFlowNone = 0xffffffffu;
+
+// Host planning.  min_amps: fewest amplitudes of a range (>= 2).  Returns the
+// number of progress words (word 0 = the shared-memory region or G[0]).
+inline int64_t flow_plan(const Geom& g, int sms, int per_sm, uint32_t min_amps, int exclusive, uint64_t budget,
+                         FlowPlan& fp) {
+  memset(&fp, 0, sizeof(fp));
+  fp.sms = (uint32_t)sms;
+  fp.per_sm = (uint32_t)per_sm;
+  fp.budget_ns = budget;
+  const int D = g.D;
+  int L = D;
+  while (L > 1 && (uint64_t)g.strides[L - 2] <= kFlowSmemAmps) --L;
+  fp.small_lvl = (uint32_t)L;
+  fp.small_amps = (L < D) ? (uint32_t)g.strides[L - 1] : 0u;
+  auto split = [&](uint32_t s, uint32_t cap, uint32_t& P, uint32_t& per) {
+    P = std::max(1u, std::min(cap, (s + min_amps - 1) / min_amps));
+    per = (s + P - 1) / P;
+    P = (s + per - 1) / per;
+  };
+  uint32_t flag = 1, F = 1;
+  for (int i = D - 1; i >= 1; --i) {
+    if (i >= L) {
+      fp.ctas[i] = 1;
+      fp.per[i] = (uint32_t)g.strides[i];
+    } else {
+      split((uint32_t)g.strides[i], (uint32_t)sms, fp.ctas[i], fp.per[i]);
+    }
+    fp.flag0[i] = flag;
+    flag += fp.ctas[i];
+    F = std::max(F, fp.ctas[i]);
+  }
+  fp.face = F;
+  fp.exclusive = (exclusive && F <= (uint32_t)sms / 2) ? 1u : 0u;
+  const uint32_t total = (uint32_t)(per_sm * sms);
+  const uint32_t avail = fp.exclusive ? (uint32_t)per_sm * ((uint32_t)sms - F) + F : total;
+  split((uint32_t)g.strides[0], avail, fp.ctas[0], fp.per[0]);
+  fp.flag0[0] = flag;
+  flag += fp.ctas[0];
+  return flag;
+}
+
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ uint32_t sm_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t sm_id_count() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nsmid;" : "=r"(r));
+  return r;
+}
+#else  // provided by the emulator
+uint32_t sm_id();
+uint32_t sm_id_count();
+#endif
+
+struct FlowSmem {
+  double2 g[kFlowSmemAmps];
+};
+// flow_level's double buffer (2 chunks of at most 2 amplitudes per thread, 256 threads) reuses it
+static_assert(2 * 2 * 256 <= kFlowSmemAmps, "flow_level buffer");
+
+struct FlowRole {
+  uint32_t smid, slot, below, present, odd;
+  uint32_t face_v;  // range of levels 1 .. small_lvl-1 (kFlowNone: none)
+  uint32_t v0;      // level-0 range (kFlowNone: none)
+};
+
+// Role of this CTA.  Every CTA registers its SM (reg[smid] counts the CTAs of
+// that SM; the slot is the CTA's arrival order on it), one grid barrier, then
+// each CTA ranks its SM among the SMs present.  If the launch did not land as
+// per_sm CTAs on each of `sms` SMs (or an SM id is out of range), every CTA
+// falls back to the same blockIdx-based mapping.
+__device__ bool flow_roles(const FlowPlan& fp, WsHeader* h, uint32_t* reg, FlowRole& r) {
+  const uint32_t b = blockIdx.x;
+  const uint32_t nsm = sm_id_count();
+  if (threadIdx.x == 0) {
+    r.smid = sm_id();
+    r.slot = (nsm <= kFlowMaxSmid && r.smid < kFlowMaxSmid) ? atomicAdd(reg + r.smid, 1u) : kFlowNone;
+    r.below = r.present = r.odd = 0;
+  }
+  if (!grid_barrier(h, 1, fp.budget_ns, 0)) return false;
+  if (nsm <= kFlowMaxSmid) {
+    uint32_t below = 0, present = 0, odd = 0;
+    for (uint32_t s = threadIdx.x; s < nsm; s += blockDim.x) {
+      const uint32_t c = ld_relaxed_u32(reg + s);
+      if (c) {
+        ++present;
+        below += (s < r.smid);
+        odd += (c != fp.per_sm);
+      }
+    }
+    if (present) atomicAdd(&r.present, present);
+    if (below) atomicAdd(&r.below, below);
+    if (odd) atomicAdd(&r.odd, odd);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t F = fp.face, S = fp.sms, total = fp.per_sm * S;
+    uint32_t fv = kFlowNone, v0 = kFlowNone;
+    if (!fp.exclusive) {  // face CTAs b < F take the last ranges
+      fv = b < F ? b : kFlowNone;
+      v0 = b >= F ? b - F : total - F + b;
+    } else if (nsm > kFlowMaxSmid || r.odd != 0 || r.present != S) {  // blockIdx-based: b and b + S share an SM
+      const uint32_t sm = b % S, slot = b / S;
+      if (sm < F) {
+        if (slot == 0) {
+          fv = sm;
+          v0 = fp.per_sm * (S - F) + sm;
+        }
+      } else {
+        v0 = slot * (S - F) + (sm - F);
+      }
+    } else if (r.below < F) {
+      if (r.slot == 0) {
+        fv = r.below;
+        v0 = fp.per_sm * (S - F) + r.below;
+      }
+    } else {
+      v0 = r.slot * (S - F) + (r.below - F);
+    }
+    r.face_v = fv;
+    r.v0 = v0 < fp.ctas[0] ? v0 : kFlowNone;
+  }
+  __syncthreads();
+  return true;
+}
+
+// Bounded wait until prog[w] >= target for all w in [w_lo, w_hi) except
+// `skip`, the CTA's threads polling the words in parallel.  A word that does
+// not move for budget_ns records MM_ERR_WAIT_TIMEOUT; any CTA that gives up
+// sets the abort word, which ends every other wait.  Returns false on give-up.
+__device__ __forceinline__ bool flow_wait(WsHeader* h, const uint32_t* prog, uint32_t w_lo, uint32_t w_hi,
+                                          uint32_t skip, uint32_t target, uint64_t budget_ns, int* s_fail) {
+  bool fail = false;
+  for (uint32_t w = w_lo + threadIdx.x; w < w_hi && !fail; w += blockDim.x) {
+    if (w == skip) continue;
+    uint32_t v = ld_acquire_u32(prog + w);
+    if (v >= target) continue;
+    uint64_t t0 = globaltimer_ns();
+    uint32_t last = v;
+    while (v < target) {
+      if (ld_relaxed_i32(&h->abort) != 0) {
+        fail = true;
+        break;
+      }
+      const uint64_t now = globaltimer_ns();
+      if (v != last) {
+        last = v;
+        t0 = now;
+      } else if (now - t0 > budget_ns) {
+        set_status(h, MM_ERR_WAIT_TIMEOUT);
+        fail = true;
+        break;
+      }
+      v = ld_acquire_u32(prog + w);
+    }
+  }
+  if (fail) *s_fail = 1;
+  __syncthreads();
+  return *s_fail == 0;
+}
+
+// Chunk (i, m) of the shared-memory region Gs, on lane pairs: lane 2a
+// computes the real part and lane 2a+1 the imaginary part of amplitude a, as
+// one chain of FMAs per part.  A GB300 FP64 warp instruction costs the same
+// for 1 or 32 active lanes, so this halves the FP64 instructions on the
+// latency-bound chain of the small levels.  The terms are those of fwd_chunk
+// (b_i G_p, A_ii sqrt(m-1) G_pp, A_ij sqrt(k_j) G_{p-1_j}, then the 1/sqrt(m)
+// scale); only the rounding of the complex products differs.
+__device__ __forceinline__ double flip_sign_if(double x, bool neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ull : 0ll));
+}
+// acc + (re or im part of x*y): re = x.x y.x - x.y y.y, im = x.x y.y + x.y y.x
+__device__ __forceinline__ double part_fma(double2 x, double2 y, bool im, double acc) {
+  return fma(x.x, im ? y.y : y.x, fma(flip_sign_if(x.y, !im), im ? y.x : y.y, acc));
+}
+
+template <int D>
+__device__ __forceinline__ void fwd_chunk_smem(const InstView& v, const double* __restrict__ rs, int i, int m,
+                                               double2* Gs) {
+  const Geom& g = v.g;
+  const uint32_t si = (uint32_t)g.strides[i];
+  const bool im = (threadIdx.x & 1u) != 0;
+  const double2 bi = __ldg(v.b + i);
+  const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
+  const double2 cd = (m >= 2) ? crow[g.prefC[i] + m] : cmk(0.0, 0.0);
+  const double rsm = rs[m];
+  const uint32_t base = (uint32_t)m * si;
+  double* Gd = reinterpret_cast<double*>(Gs);
+  for (uint32_t a = threadIdx.x >> 1; a < si; a += blockDim.x >> 1) {
+    int32_t k[D];
+    decompose<D>(a, i + 1, g, k);
+    const uint32_t f = base + a, p = f - si;
+    double acc = part_fma(bi, Gs[p], im, 0.0);
+    if (m >= 2) acc = part_fma(cd, Gs[p - si], im, acc);
+#pragma unroll
+    for (int j = 1; j < D; ++j) {
+      if (j > i && k[j] > 0) acc = part_fma(crow[g.prefC[j] + k[j]], Gs[p - (uint32_t)g.strides[j]], im, acc);
+    }
+    Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
+  }
+}
+
+// One CTA's range [lo, hi) of a shared level i (ctas[i] > 1) through chunks
+// 1..C_i-1, on lane pairs as in fwd_chunk_smem: pair a of the CTA holds
+// amplitudes lo + a + u*(blockDim/2) (u < A), lane 2a their real parts and
+// lane 2a+1 their imaginary parts.  Each lane keeps its part of the last two
+// chunks in registers (gp: m-1, gpp: m-2; the partner's part comes by
+// shuffle), and chunk m-1 of the whole range sits in shared memory S
+// (double-buffered) for the in-range neighbours q - strides[j].  The terms
+// whose inputs lie in the range are summed before the wait for the
+// neighbouring ranges; only the halo terms (inputs in another CTA's range) are
+// read from global memory after it.
+template <int D, int A>
+__device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsHeader* h, uint32_t* prog,
+                           const FlowPlan& fp, int i, uint32_t vr, uint32_t fv, double2* S, int* s_fail) {
+  const Geom& g = v.g;
+  const uint32_t si = (uint32_t)g.strides[i], per = fp.per[i];
+  const uint32_t lo = min(si, per * vr), hi = min(si, lo + per);
+  const uint32_t snext = (i + 1 < D) ? (uint32_t)g.strides[i + 1] : 0u;
+  const int Ci = (int)g.shape[i];
+  const bool im = (threadIdx.x & 1u) != 0;
+  const uint32_t pairs = blockDim.x >> 1, a0 = threadIdx.x >> 1;
+  const double2 bi = __ldg(v.b + i);
+  const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
+  double2* G = v.G;
+  double* Gd = reinterpret_cast<double*>(G);
+  double* Sd = reinterpret_cast<double*>(S);
+  uint32_t* my = prog + fp.flag0[i] + vr;
+  double gp[A], gpp[A];
+  int32_t k[A][D];
+#pragma unroll
+  for (int u = 0; u < A; ++u) {
+    const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+    decompose<D>(q < hi ? q : lo, i + 1, g, k[u]);
+    gp[u] = gpp[u] = 0.0;
+  }
+  if (Ci < 2) return true;
+  {  // chunk 1: every input is an amplitude of the lower levels
+    const uint32_t pos = hi - 1;
+    int l = i + 1;
+    while (l < D && pos / (uint32_t)g.strides[l] == 0) ++l;
+    uint32_t w_lo = 0, w_hi = (fv == 0) ? 0u : 1u, target = 1u, skip = kFlowNone;
+    if (l < D) {
+      target = pos / (uint32_t)g.strides[l];
+      w_lo = fp.flag0[l];
+      w_hi = w_lo + fp.ctas[l];
+      if (fv < fp.ctas[l]) skip = w_lo + fv;
+    }
+    if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, skip, target, fp.budget_ns, s_fail)) return false;
+    const double rs1 = rs[1];
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+      const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+      if (q < hi) {
+        const double2 g0 = __ldcg(G + q);
+        double acc = part_fma(bi, g0, im, 0.0);
+#pragma unroll
+        for (int j = 1; j < D; ++j)
+          if (j > i && k[u][j] > 0)
+            acc = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + q - (uint32_t)g.strides[j]), im, acc);
+        const double val = rs1 * acc;
+        Gd[2 * ((int64_t)si + q) + im] = val;
+        Sd[2 * (per + (q - lo)) + im] = val;
+        gpp[u] = im ? g0.y : g0.x;
+        gp[u] = val;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) st_release_u32(my, 1u);
+  }
+  const uint32_t w_lo = fp.flag0[i] + (lo >= snext ? lo - snext : 0u) / per, w_hi = fp.flag0[i] + vr;
+  for (int m = 2; m < Ci; ++m) {
+    const double2 cd = crow[g.prefC[i] + m];
+    const double rsm = rs[m];
+    const double2* Sp = S + ((m - 1) & 1) * per;
+    double* Sn = Sd + 2 * (m & 1) * per;
+    double acc[A];
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+      const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+      const double op = __shfl_xor_sync(0xffffffffu, gp[u], 1), opp = __shfl_xor_sync(0xffffffffu, gpp[u], 1);
+      const double2 Gp = im ? cmk(op, gp[u]) : cmk(gp[u], op);
+      const double2 Gpp = im ? cmk(opp, gpp[u]) : cmk(gpp[u], opp);
+      acc[u] = part_fma(cd, Gpp, im, part_fma(bi, Gp, im, 0.0));
+      if (q < hi) {
+#pragma unroll
+        for (int j = 1; j < D; ++j) {
+          const uint32_t sj = (uint32_t)g.strides[j];
+          if (j > i && k[u][j] > 0 && q - sj >= lo)
+            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], Sp[q - sj - lo], im, acc[u]);
         }
       }
     }
-    if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
-    for (int i = lvl_big; i >= 0; --i) {
-      const uint32_t si = (uint32_t)g.strides[i];
-      const uint32_t per = (si + gridDim.x - 1) / gridDim.x;
-      const uint32_t lo = min(si, per * blockIdx.x), hi = min(si, lo + per);
-      for (int m = 1; m < (int)g.shape[i]; ++m) {
-        fwd_chunk<D, true>(sv, rs, i, m, lo, hi, blockDim.x, threadIdx.x);
-        if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+    if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, kFlowNone, (uint32_t)(m - 1), fp.budget_ns, s_fail))
+      return false;
+    const int64_t prev = (int64_t)(m - 1) * si;
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+      const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+      if (q < hi) {
+#pragma unroll
+        for (int j = 1; j < D; ++j) {
+          const uint32_t sj = (uint32_t)g.strides[j];
+          if (j > i && k[u][j] > 0 && q - sj < lo)
+            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + prev + (q - sj)), im, acc[u]);
+        }
+        const double val = rsm * acc[u];
+        Gd[2 * ((int64_t)m * si + q) + im] = val;
+        Sn[2 * (q - lo) + im] = val;
+        gpp[u] = gp[u];
+        gp[u] = val;
       }
     }
-  } else {
-    if (blockIdx.x == 0 && threadIdx.x == 0) sv.G[0] = sv.c;
-    if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
-    int wmax = 0;
-    for (int i = 0; i < D; ++i) wmax += (int)g.shape[i] - 1;
-    const uint32_t P = (uint32_t)(g.n / g.shape[D - 1]);
-    const uint32_t per = (P + gridDim.x - 1) / gridDim.x;
-    const uint32_t lo = min(P, per * blockIdx.x), hi = min(P, lo + per);
-    for (int w = 1; w <= wmax; ++w) {
-      stable_wave<D, true>(sv, rs, w, lo, hi, blockDim.x, threadIdx.x);
-      if (!grid_barrier(h, ++epoch, budget_ns, 0)) return;
+    __syncthreads();
+    if (threadIdx.x == 0) st_release_u32(my, (uint32_t)m);
+  }
+  return true;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) fwd_flow_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
+                                                       uint32_t* prog, FlowPlan fp) {
+  MM_SHARED(InstView, sv);
+  MM_SHARED(int, s_fail);
+  MM_SHARED(FlowRole, role);
+  MM_SHARED(FlowSmem, smem);
+  double2* Gs = smem.g;
+  if (threadIdx.x == 0) {
+    src.load(0, sv);
+    s_fail = 0;
+  }
+  if (!flow_roles(fp, h, prog + (fp.flag0[0] + fp.ctas[0]), role)) return;
+  const Geom& g = sv.g;
+  const uint32_t fv = role.face_v;
+  const int L = (int)fp.small_lvl;
+  if (fv == 0) {
+    if (L < D) {  // the small levels, in shared memory, then written out at once
+      if (threadIdx.x == 0) Gs[0] = sv.c;
+      __syncthreads();
+      for (int i = D - 1; i >= L; --i) {
+        for (int m = 1; m < (int)g.shape[i]; ++m) {
+          fwd_chunk_smem<D>(sv, rs, i, m, Gs);
+          __syncthreads();
+        }
+      }
+      for (uint32_t f = threadIdx.x; f < fp.small_amps; f += blockDim.x) stG(sv, f, Gs[f], 7);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        st_release_u32(prog, 1u);
+        for (int l = L; l < D; ++l) st_release_u32(prog + fp.flag0[l], (uint32_t)g.shape[l] - 1u);
+      }
+    } else {
+      if (threadIdx.x == 0) {
+        stG(sv, 0, sv.c, 7);
+        st_release_u32(prog, 1u);
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = min(L, D) - 1; i >= 0; --i) {
+    const uint32_t P = fp.ctas[i];
+    const uint32_t v = (i > 0) ? fv : role.v0;
+    if (v >= P) continue;
+    const uint32_t si = (uint32_t)g.strides[i];
+    const uint32_t per = fp.per[i];
+    const uint32_t lo = min(si, per * v), hi = min(si, lo + per);
+    const uint32_t snext = (i + 1 < D) ? (uint32_t)g.strides[i + 1] : 0u;
+    const int Ci = (int)g.shape[i];
+    if (P > 1 && per <= 2u * blockDim.x) {  // register/shared-memory form on lane pairs
+      const uint32_t pairs = blockDim.x >> 1;
+      const bool ok = (per <= pairs)       ? flow_level<D, 1>(sv, rs, h, prog, fp, i, v, fv, Gs, &s_fail)
+                      : (per <= 2 * pairs) ? flow_level<D, 2>(sv, rs, h, prog, fp, i, v, fv, Gs, &s_fail)
+                                           : flow_level<D, 4>(sv, rs, h, prog, fp, i, v, fv, Gs, &s_fail);
+      if (!ok) return;
+      continue;
+    }
+    const bool publish_each = P > 1 || (i > 0 && fp.ctas[i - 1] > 1);
+    for (int m = 1; m < Ci; ++m) {
+      uint32_t w_lo, w_hi, skip = kFlowNone, target;
+      if (m >= 2) {
+        target = (uint32_t)(m - 1);
+        w_lo = fp.flag0[i] + (lo >= snext ? lo - snext : 0u) / per;
+        w_hi = fp.flag0[i] + v;
+      } else {
+        const uint32_t pos = hi - 1;
+        int l = i + 1;
+        while (l < D && pos / (uint32_t)g.strides[l] == 0) ++l;
+        if (l < D) {
+          target = pos / (uint32_t)g.strides[l];
+          w_lo = fp.flag0[l];
+          w_hi = w_lo + fp.ctas[l];
+          if (fv < fp.ctas[l]) skip = w_lo + fv;
+        } else {  // only G[0] lies below hi
+          target = 1u;
+          w_lo = 0u;
+          w_hi = (fv == 0) ? 0u : 1u;
+        }
+      }
+      if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, skip, target, fp.budget_ns, &s_fail)) return;
+      // L1-cached loads only where every amplitude read was written by this CTA
+      // (a one-range level >= 1 and everything below it belong to face CTA 0)
+      if (i > 0 && P == 1)
+        fwd_chunk<D, false>(sv, rs, i, m, lo, hi, blockDim.x, threadIdx.x);
+      else
+        fwd_chunk<D, true>(sv, rs, i, m, lo, hi, blockDim.x, threadIdx.x);
+      __syncthreads();
+      // the CTA barrier orders every thread's stores before thread 0's release
+      if (threadIdx.x == 0 && (publish_each || m == Ci - 1)) st_release_u32(prog + fp.flag0[i] + v, (uint32_t)m);
     }
   }
 }
