@@ -318,33 +318,37 @@ __global__ void __launch_bounds__(128) ozaki_mma_kernel(const __nv_bfloat16* __r
 
 // ---------------------------------------------------------------- tcgen05 path
 // Warp-specialised Blackwell kernel for the slice products.  One CTA owns a
-// 128-row x 32-complex-column tile of Y.  For every slice pair (p, q) and every
-// chunk of at most 4096 K values (one "unit"), the tensor cores compute two
-// M = 128, N = 64 products into TMEM:
-//     acc_r = U_re,p [X_re,q | X_im,q]   (columns 0..31: rr, 32..63: ri)
-//     acc_i = U_im,p [X_re,q | X_im,q]   (columns 0..31: ir, 32..63: ii)
+// 128-row x 40-complex-column tile of Y (a 2500 x 256 product is 20 x 7 = 140
+// tiles: one wave on 152 SMs).  For every slice pair (p, q) and every chunk of
+// at most 4096 K values (one "unit"), the tensor cores compute two M = 128,
+// N = 80 products into TMEM:
+//     acc_r = U_re,p [X_re,q | X_im,q]   (columns 0..39: rr, 40..79: ri)
+//     acc_i = U_im,p [X_re,q | X_im,q]   (columns 0..39: ir, 40..79: ii)
 // with FP32 accumulation that is exact for 6-bit slices.  Roles:
 //   warp 0, lane 0: TMA producer (3-stage ring of [U_re | U_im | X_re ; X_im] K-blocks of 64),
 //   warp 1, lane 0: MMA issuer (tcgen05.mma, tcgen05.commit into mbarriers),
 //   warps 2..5:      epilogue (tcgen05.ld of a finished unit, exact integer sums per slice order,
 //                    one FP64 scaling per order into Y).
-// Accumulators are double-buffered (2 x 128 TMEM columns) so the epilogue of one
+// Accumulators are double-buffered (TMEM columns 0 and 256) so the epilogue of one
 // unit overlaps the MMAs of the next.  Every mbarrier wait is bounded; on a
 // timeout the CTA records MM_ERR_WAIT_TIMEOUT, lets its in-flight copies land,
 // frees its TMEM and returns.
 constexpr int TC_BM = 128;                                // Y rows per CTA (MMA M)
-constexpr int TC_NC = 32;                                 // Y complex columns per CTA (MMA N = 64)
+constexpr int TC_NC = 40;                                 // Y complex columns per CTA (MMA N = 80)
 constexpr int TC_BK = 64;                                 // K per stage: one 128-byte swizzled row of BF16
 constexpr int TC_STAGES = 3;
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;             // 16 KB per U component
-constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 8 KB ([X_re; X_im] rows)
-constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + TC_B_BYTES;  // 40 KB
+constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 10 KB ([X_re; X_im] rows)
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + TC_B_BYTES;  // 42 KB (a multiple of 1 KB: swizzle atoms stay aligned)
 constexpr int TC_T_BYTES = 2 * TC_NC * TC_BM * 8;         // int64 slice-order sums, [comp][col][row]
-constexpr int TC_TMEM_COLS = 256;
+constexpr int TC_TMEM_COLS = 512;
+constexpr int TC_ACC_STRIDE = 256;                        // TMEM columns between the two accumulator buffers
+static_assert(TC_NC % 8 == 0 && 4 * TC_NC <= TC_ACC_STRIDE, "accumulator layout");
+static_assert(TC_STAGE_BYTES % 1024 == 0 && (TC_B_BYTES / 2) % 1024 == 0, "swizzle atoms");
 constexpr int TC_THREADS = 192;
 constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * TC_STAGE_BYTES + TC_T_BYTES + 256;
-// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 64, M = 128.
-constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 2 * TC_NC, M = 128.
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)((2 * TC_NC) >> 3) << 17) |
                               ((uint32_t)(128 >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -407,12 +411,10 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -552,7 +554,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (; ok && u.valid(); u.next()) {
       if (!mbar_wait(acce(abuf), aphase ^ 1, abort_flag, h, budget_ns)) break;
       tc_fence_after();
-      const uint32_t d_r = tmem + (uint32_t)(abuf * 128), d_i = d_r + 64;
+      const uint32_t d_r = tmem + (uint32_t)(abuf * TC_ACC_STRIDE), d_i = d_r + 2 * TC_NC;
       for (int kb = u.kb_begin(); kb < u.kb_end(); ++kb) {
         if (!mbar_wait(full(stage), phase, abort_flag, h, budget_ns)) {
           ok = false;
@@ -602,18 +604,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       okw = __shfl_sync(0xffffffffu, okw, 0);
       if (!okw) break;
       tc_fence_after();
-      const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(abuf * 128);
+      const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(abuf * TC_ACC_STRIDE);
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        uint32_t rr[16], ri[16], ir[16], ii[16];
-        tc_ld16(base + half * 16, rr);
-        tc_ld16(base + 32 + half * 16, ri);
-        tc_ld16(base + 64 + half * 16, ir);
-        tc_ld16(base + 96 + half * 16, ii);
+      for (int c8 = 0; c8 < TC_NC / 8; ++c8) {
+        uint32_t rr[8], ri[8], ir[8], ii[8];
+        tc_ld8(base + c8 * 8, rr);
+        tc_ld8(base + TC_NC + c8 * 8, ri);
+        tc_ld8(base + 2 * TC_NC + c8 * 8, ir);
+        tc_ld8(base + 3 * TC_NC + c8 * 8, ii);
         tc_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int c = half * 16 + j;
+        for (int j = 0; j < 8; ++j) {
+          const int c = c8 * 8 + j;
           const long long re = (long long)__float2int_rn(__uint_as_float(rr[j])) -
                                (long long)__float2int_rn(__uint_as_float(ii[j]));
           const long long im = (long long)__float2int_rn(__uint_as_float(ri[j])) +
