@@ -98,8 +98,12 @@ __device__ __forceinline__ int exp_bound(double x) {
 }
 
 // Row exponents of U (M x K): E[r] = max over the row's re and im of exp_bound.
-__global__ void __launch_bounds__(256) row_exp_kernel(const double2* __restrict__ U, int M, int K, int* __restrict__ E) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+// Also sets every column exponent F[c] to INT32_MIN for col_exp_kernel's atomicMax.
+__global__ void __launch_bounds__(256) row_exp_kernel(const double2* __restrict__ U, int M, int K, int* __restrict__ E,
+                                                      int N, int* __restrict__ F) {
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int c = gtid; c < N; c += gridDim.x * blockDim.x) F[c] = INT32_MIN;
+  const int warp = gtid >> 5, lane = threadIdx.x & 31;
   if (warp >= M) return;
   int m = INT32_MIN;
   for (int k = lane; k < K; k += 32) {
@@ -111,15 +115,18 @@ __global__ void __launch_bounds__(256) row_exp_kernel(const double2* __restrict_
   if (lane == 0) E[warp] = m;
 }
 
-// Column exponents of X (K x N): F[c] = max over the column.  A CTA of 256
-// threads covers 32 columns: 8 row strides x 32 columns, coalesced along the row.
+// Column exponents of X (K x N): F[c] = max over the column.  CTA (x, y) covers
+// 32 columns and rows [y * COL_EXP_ROWS, +COL_EXP_ROWS): 8 row strides x 32
+// columns, coalesced along the row, merged into F with atomicMax.
+constexpr int COL_EXP_ROWS = 128;
 __global__ void __launch_bounds__(256) col_exp_kernel(const double2* __restrict__ X, int K, int N, int* __restrict__ F) {
   __shared__ int part[8][32];
   const int cl = threadIdx.x & 31, rl = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + cl;
+  const int k0 = blockIdx.y * COL_EXP_ROWS, k1 = min(K, k0 + COL_EXP_ROWS);
   int m = INT32_MIN;
   if (c < N)
-    for (int k = rl; k < K; k += 8) {
+    for (int k = k0 + rl; k < k1; k += 8) {
       const double2 v = __ldg(X + (int64_t)k * N + c);
       m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
     }
@@ -127,7 +134,7 @@ __global__ void __launch_bounds__(256) col_exp_kernel(const double2* __restrict_
   __syncthreads();
   if (rl == 0 && c < N) {
     for (int r = 1; r < 8; ++r) m = max(m, part[r][cl]);
-    F[c] = m;
+    if (m != INT32_MIN) atomicMax(F + c, m);
   }
 }
 
@@ -324,6 +331,9 @@ __global__ void __launch_bounds__(128) ozaki_mma_kernel(const __nv_bfloat16* __r
 // N = 80 products into TMEM:
 //     acc_r = U_re,p [X_re,q | X_im,q]   (columns 0..39: rr, 40..79: ri)
 //     acc_i = U_im,p [X_re,q | X_im,q]   (columns 0..39: ir, 40..79: ii)
+// The kernel is bound by the latency of its TMA ring (bytes in flight per SM),
+// not by L2 bandwidth: sharing the U tiles of a row of CTAs through cluster
+// multicast was measured and gained nothing, so every CTA loads its own.
 // with FP32 accumulation that is exact for 6-bit slices.  Roles:
 //   warp 0, lane 0: TMA producer (3-stage ring of [U_re | U_im | X_re ; X_im] K-blocks of 64),
 //   warp 1, lane 0: MMA issuer (tcgen05.mma, tcgen05.commit into mbarriers),
@@ -336,17 +346,20 @@ __global__ void __launch_bounds__(128) ozaki_mma_kernel(const __nv_bfloat16* __r
 constexpr int TC_BM = 128;                                // Y rows per CTA (MMA M)
 constexpr int TC_NC = 40;                                 // Y complex columns per CTA (MMA N = 80)
 constexpr int TC_BK = 64;                                 // K per stage: one 128-byte swizzled row of BF16
-constexpr int TC_STAGES = 3;
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;             // 16 KB per U component
 constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 10 KB ([X_re; X_im] rows)
 constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + TC_B_BYTES;  // 42 KB (a multiple of 1 KB: swizzle atoms stay aligned)
-constexpr int TC_T_BYTES = 2 * TC_NC * TC_BM * 8;         // int64 slice-order sums, [comp][col][row]
+// Slice-order sums [comp][col][row]: int32 while 9 pairs x Kp x 2 x 63^2 < 2^31
+// (then four stages fit), int64 beyond (three stages).
+constexpr int TC_KP_INT32_MAX = 30000;
+constexpr int tc_smem_bytes(int tbytes, int stages) {
+  return 1024 + stages * TC_STAGE_BYTES + 2 * TC_NC * TC_BM * tbytes + 256;
+}
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_ACC_STRIDE = 256;                        // TMEM columns between the two accumulator buffers
 static_assert(TC_NC % 8 == 0 && 4 * TC_NC <= TC_ACC_STRIDE, "accumulator layout");
 static_assert(TC_STAGE_BYTES % 1024 == 0 && (TC_B_BYTES / 2) % 1024 == 0, "swizzle atoms");
 constexpr int TC_THREADS = 192;
-constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * TC_STAGE_BYTES + TC_T_BYTES + 256;
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 2 * TC_NC, M = 128.
 constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)((2 * TC_NC) >> 3) << 17) |
                               ((uint32_t)(128 >> 4) << 24);
@@ -418,11 +431,16 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Units of a CTA, in order: slice order d = 2 .. S+1, p = max(1, d-S) .. min(S, d-1),
-// K chunks of at most 4096 (TC_FLUSH_BLOCKS K-blocks).  Every role walks the same sequence.
+// Units of a CTA, in order: slice order d = 2 .. S+1; within an order the
+// pairs p in [max(1, d-S), min(S, d-1)], ascending for even d and descending
+// for odd d (consecutive units then reuse the U slices still in L2); K chunks
+// of at most 4096.  Every role walks the same sequence.
 struct UnitIter {
   int S, nkb, chunk_kb;
   int d, p, c;  // current unit
+  __device__ int plo() const { return d - S > 1 ? d - S : 1; }
+  __device__ int phi() const { return d - 1 < S ? d - 1 : S; }
+  __device__ bool desc() const { return (d & 1) != 0; }
   __device__ void start(int S_, int nkb_, int chunk_kb_) {
     S = S_;
     nkb = nkb_;
@@ -435,26 +453,23 @@ struct UnitIter {
   __device__ int q() const { return d - p; }
   __device__ int kb_begin() const { return c * chunk_kb; }
   __device__ int kb_end() const { return min(nkb, (c + 1) * chunk_kb); }
-  __device__ bool last_of_order() const {
-    const int phi = d - 1 < S ? d - 1 : S;
-    return p == phi && kb_end() >= nkb;
-  }
+  __device__ bool last_of_order() const { return p == (desc() ? plo() : phi()) && kb_end() >= nkb; }
   __device__ void next() {
     if (kb_end() < nkb) {
       ++c;
       return;
     }
     c = 0;
-    const int phi = d - 1 < S ? d - 1 : S;
-    if (p < phi) {
-      ++p;
+    if (desc() ? p > plo() : p < phi()) {
+      p += desc() ? -1 : 1;
       return;
     }
     ++d;
-    p = d - S > 1 ? d - S : 1;
+    p = desc() ? phi() : plo();
   }
 };
 
+template <typename TT, int TC_STAGES>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ CUtensorMap tmap_x,
                     const int* __restrict__ E, const int* __restrict__ F, double2* __restrict__ Y, int M, int N,
@@ -462,8 +477,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* stages = smem;
-  long long* T = reinterpret_cast<long long*>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][TC_NC][TC_BM]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES + TC_T_BYTES);
+  TT* T = reinterpret_cast<TT*>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][TC_NC][TC_BM]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES + 2 * TC_NC * TC_BM * sizeof(TT));
   // bars: full[STAGES], empty[STAGES], accf[2], acce[2], drain
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -616,10 +631,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int c = c8 * 8 + j;
-          const long long re = (long long)__float2int_rn(__uint_as_float(rr[j])) -
-                               (long long)__float2int_rn(__uint_as_float(ii[j]));
-          const long long im = (long long)__float2int_rn(__uint_as_float(ri[j])) +
-                               (long long)__float2int_rn(__uint_as_float(ir[j]));
+          const TT re = (TT)__float2int_rn(__uint_as_float(rr[j])) - (TT)__float2int_rn(__uint_as_float(ii[j]));
+          const TT im = (TT)__float2int_rn(__uint_as_float(ri[j])) + (TT)__float2int_rn(__uint_as_float(ir[j]));
           T[(0 * TC_NC + c) * TC_BM + row] += re;
           T[(1 * TC_NC + c) * TC_BM + row] += im;
         }
@@ -634,8 +647,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int er = gm < M ? E[gm] : INT32_MIN;
         for (int c = 0; c < TC_NC; ++c) {
           const int gn = n0 + c;
-          long long& tre = T[(0 * TC_NC + c) * TC_BM + row];
-          long long& tim = T[(1 * TC_NC + c) * TC_BM + row];
+          TT& tre = T[(0 * TC_NC + c) * TC_BM + row];
+          TT& tim = T[(1 * TC_NC + c) * TC_BM + row];
           if (gm < M && gn < N) {
             const int fc = F[gn];
             double2 y = cmk(0.0, 0.0);
@@ -771,8 +784,9 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
   int* E = reinterpret_cast<int*>(w + L.e);
   int* F = reinterpret_cast<int*>(w + L.f);
   const int Kp = (int)L.Kp;
-  row_exp_kernel<<<(unsigned)((M * 32 + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, E);
-  col_exp_kernel<<<(unsigned)((N + 31) / 32), 256, 0, st>>>((const double2*)X, (int)K, (int)N, F);
+  row_exp_kernel<<<(unsigned)((M * 32 + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, E, (int)N, F);
+  col_exp_kernel<<<dim3((unsigned)((N + 31) / 32), (unsigned)((K + COL_EXP_ROWS - 1) / COL_EXP_ROWS)), 256, 0, st>>>(
+      (const double2*)X, (int)K, (int)N, F);
   split_u_kernel<<<(unsigned)((M * Kp + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, Us);
   split_x_kernel<<<(unsigned)((N * Kp + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, Kp, slices, F, Xs);
   if (mode_legacy_mma()) {
@@ -787,12 +801,19 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
     return MM_ERR_UNSUPPORTED;
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
+    cudaFuncSetAttribute(ozaki_tc_kernel<int, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes(4, 4));
+    cudaFuncSetAttribute(ozaki_tc_kernel<long long, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         tc_smem_bytes(8, 3));
   });
   dim3 grid((unsigned)((N + TC_NC - 1) / TC_NC), (unsigned)((M + TC_BM - 1) / TC_BM));
   if (grid.y > 65535) return MM_ERR_TOO_LARGE;
-  ozaki_tc_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices,
-                                                           reinterpret_cast<mm::WsHeader*>(w), tc_budget_ns());
+  mm::WsHeader* h = reinterpret_cast<mm::WsHeader*>(w);
+  if (Kp <= TC_KP_INT32_MAX)
+    ozaki_tc_kernel<int, 4><<<grid, TC_THREADS, tc_smem_bytes(4, 4), st>>>(tu, tx, E, F, (double2*)Y, (int)M, (int)N,
+                                                                         Kp, slices, h, tc_budget_ns());
+  else
+    ozaki_tc_kernel<long long, 3><<<grid, TC_THREADS, tc_smem_bytes(8, 3), st>>>(tu, tx, E, F, (double2*)Y, (int)M,
+                                                                               (int)N, Kp, slices, h, tc_budget_ns());
   return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
 }
 

@@ -26,7 +26,10 @@ def cn(shape, seed):
     return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
 
 
-@pytest.mark.parametrize("M,N,K", [(1, 1, 1), (37, 5, 300), (300, 64, 200), (129, 33, 4200)])
+# (40, 300, 64): N spans several 40-column tiles with a ragged last one; K = 30100 takes the int64
+# slice-order sums (K padded beyond 30000), every other case the int32 ones.
+@pytest.mark.parametrize("M,N,K", [(1, 1, 1), (37, 5, 300), (300, 64, 200), (129, 33, 4200), (40, 300, 64),
+                                   (24, 12, 30100)])
 def test_gemm_random(cuda, oracle_lib, M, N, K):
     U, X = cn((M, K), M + K), cn((K, N), N)
     ref = oracle_lib.fock_gemm(U, X)
