@@ -349,15 +349,18 @@ constexpr int TC_BK = 64;                                 // K per stage: one 12
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;             // 16 KB per U component
 constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 10 KB ([X_re; X_im] rows)
 constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + TC_B_BYTES;  // 42 KB (a multiple of 1 KB: swizzle atoms stay aligned)
-// Slice-order sums [comp][col][row]: int32 while 9 pairs x Kp x 2 x 63^2 < 2^31
-// (then four stages fit), int64 beyond (three stages).
+// Slice-order sums [comp][col][row]: int32 while 9 pairs x Kp x 2 x 63^2 < 2^31,
+// held in TMEM columns TC_T_COL.. (free between the two accumulator buffers), so
+// five stages fit in shared memory; int64 beyond, in shared memory (three stages).
 constexpr int TC_KP_INT32_MAX = 30000;
+// tbytes: bytes per shared-memory order sum (0: sums in TMEM)
 constexpr int tc_smem_bytes(int tbytes, int stages) {
   return 1024 + stages * TC_STAGE_BYTES + 2 * TC_NC * TC_BM * tbytes + 256;
 }
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_ACC_STRIDE = 256;                        // TMEM columns between the two accumulator buffers
-static_assert(TC_NC % 8 == 0 && 4 * TC_NC <= TC_ACC_STRIDE, "accumulator layout");
+constexpr int TC_T_COL = 4 * TC_NC;                       // int32 order sums: [re cols | im cols] after buffer 0
+static_assert(TC_NC % 8 == 0 && 6 * TC_NC <= TC_ACC_STRIDE, "accumulator and order-sum layout");
 static_assert(TC_STAGE_BYTES % 1024 == 0 && (TC_B_BYTES / 2) % 1024 == 0, "swizzle atoms");
 constexpr int TC_THREADS = 192;
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 2 * TC_NC, M = 128.
@@ -429,6 +432,12 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t (&r)[8]) {
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                : "r"(taddr));
 }
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Units of a CTA, in order: slice order d = 2 .. S+1; within an order the
@@ -469,7 +478,8 @@ struct UnitIter {
   }
 };
 
-template <typename TT, int TC_STAGES>
+// TT: type of the slice-order sums; TMEM_T: they live in TMEM (int32 only).
+template <typename TT, int TC_STAGES, bool TMEM_T>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ CUtensorMap tmap_x,
                     const int* __restrict__ E, const int* __restrict__ F, double2* __restrict__ Y, int M, int N,
@@ -477,8 +487,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* stages = smem;
-  TT* T = reinterpret_cast<TT*>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][TC_NC][TC_BM]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES + 2 * TC_NC * TC_BM * sizeof(TT));
+  static_assert(!TMEM_T || sizeof(TT) == 4, "TMEM sums are 32-bit");
+  constexpr int t_bytes = TMEM_T ? 0 : 2 * TC_NC * TC_BM * (int)sizeof(TT);
+  TT* T = reinterpret_cast<TT*>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][TC_NC][TC_BM] (shared-memory sums)
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES + t_bytes);
   // bars: full[STAGES], empty[STAGES], accf[2], acce[2], drain
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -608,7 +620,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int lane_base = 32 * (warp & 3);
     const int row = lane_base + lane;
     const int gm = m0 + row;
-    for (int c = 0; c < TC_NC; ++c) T[(0 * TC_NC + c) * TC_BM + row] = T[(1 * TC_NC + c) * TC_BM + row] = 0;
+    const uint32_t trow = tmem + ((uint32_t)lane_base << 16);  // this warp's 32 TMEM lanes
+    const uint32_t zeros[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    if constexpr (TMEM_T) {
+#pragma unroll
+      for (int c8 = 0; c8 < 2 * TC_NC / 8; ++c8) tc_st8(trow + TC_T_COL + c8 * 8, zeros);
+      tc_wait_st();
+    } else {
+      for (int c = 0; c < TC_NC; ++c) T[(0 * TC_NC + c) * TC_BM + row] = T[(1 * TC_NC + c) * TC_BM + row] = 0;
+    }
     int abuf = 0;
     uint32_t aphase = 0;
     UnitIter u;
@@ -619,54 +639,93 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       okw = __shfl_sync(0xffffffffu, okw, 0);
       if (!okw) break;
       tc_fence_after();
-      const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(abuf * TC_ACC_STRIDE);
+      const uint32_t base = trow + (uint32_t)(abuf * TC_ACC_STRIDE);
 #pragma unroll
       for (int c8 = 0; c8 < TC_NC / 8; ++c8) {
-        uint32_t rr[8], ri[8], ir[8], ii[8];
+        uint32_t rr[8], ri[8], ir[8], ii[8], tr[8], ti[8];
         tc_ld8(base + c8 * 8, rr);
         tc_ld8(base + TC_NC + c8 * 8, ri);
         tc_ld8(base + 2 * TC_NC + c8 * 8, ir);
         tc_ld8(base + 3 * TC_NC + c8 * 8, ii);
+        if constexpr (TMEM_T) {
+          tc_ld8(trow + TC_T_COL + c8 * 8, tr);
+          tc_ld8(trow + TC_T_COL + TC_NC + c8 * 8, ti);
+        }
         tc_wait_ld();
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int c = c8 * 8 + j;
           const TT re = (TT)__float2int_rn(__uint_as_float(rr[j])) - (TT)__float2int_rn(__uint_as_float(ii[j]));
           const TT im = (TT)__float2int_rn(__uint_as_float(ri[j])) + (TT)__float2int_rn(__uint_as_float(ir[j]));
-          T[(0 * TC_NC + c) * TC_BM + row] += re;
-          T[(1 * TC_NC + c) * TC_BM + row] += im;
+          if constexpr (TMEM_T) {
+            tr[j] = (uint32_t)((int)tr[j] + (int)re);
+            ti[j] = (uint32_t)((int)ti[j] + (int)im);
+          } else {
+            T[(0 * TC_NC + c) * TC_BM + row] += re;
+            T[(1 * TC_NC + c) * TC_BM + row] += im;
+          }
+        }
+        if constexpr (TMEM_T) {
+          tc_st8(trow + TC_T_COL + c8 * 8, tr);
+          tc_st8(trow + TC_T_COL + TC_NC + c8 * 8, ti);
         }
       }
+      if constexpr (TMEM_T) tc_wait_st();
       tc_fence_before();
       mbar_arrive(acce(abuf));
       if (++abuf == 2) {
         abuf = 0;
         aphase ^= 1;
       }
-      if (u.last_of_order()) {  // add this slice order's sums to Y in FP64
+      if (u.last_of_order()) {  // add this slice order's sums to Y in FP64, then clear them
         const int er = gm < M ? E[gm] : INT32_MIN;
-        for (int c = 0; c < TC_NC; ++c) {
-          const int gn = n0 + c;
-          TT& tre = T[(0 * TC_NC + c) * TC_BM + row];
-          TT& tim = T[(1 * TC_NC + c) * TC_BM + row];
-          if (gm < M && gn < N) {
-            const int fc = F[gn];
-            double2 y = cmk(0.0, 0.0);
-            if (er != INT32_MIN && fc != INT32_MIN) {
-              const double sc = pow2(er + fc - OZ_BETA * u.d);
-              y = cmk((double)tre * sc, (double)tim * sc);
+#pragma unroll
+        for (int c8 = 0; c8 < TC_NC / 8; ++c8) {
+          long long vre[8], vim[8];
+          if constexpr (TMEM_T) {
+            uint32_t tr[8], ti[8];
+            tc_ld8(trow + TC_T_COL + c8 * 8, tr);
+            tc_ld8(trow + TC_T_COL + TC_NC + c8 * 8, ti);
+            tc_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              vre[j] = (int)tr[j];
+              vim[j] = (int)ti[j];
             }
-            double2* py = Y + (int64_t)gm * N + gn;
-            if (u.d == 2) {
-              *py = y;
-            } else {
-              const double2 o = *py;
-              *py = cmk(o.x + y.x, o.y + y.y);
+            tc_st8(trow + TC_T_COL + c8 * 8, zeros);
+            tc_st8(trow + TC_T_COL + TC_NC + c8 * 8, zeros);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              TT& tre = T[(0 * TC_NC + c8 * 8 + j) * TC_BM + row];
+              TT& tim = T[(1 * TC_NC + c8 * 8 + j) * TC_BM + row];
+              vre[j] = (long long)tre;
+              vim[j] = (long long)tim;
+              tre = 0;
+              tim = 0;
             }
           }
-          tre = 0;
-          tim = 0;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int gn = n0 + c8 * 8 + j;
+            if (gm < M && gn < N) {
+              const int fc = F[gn];
+              double2 y = cmk(0.0, 0.0);
+              if (er != INT32_MIN && fc != INT32_MIN) {
+                const double sc = pow2(er + fc - OZ_BETA * u.d);
+                y = cmk((double)vre[j] * sc, (double)vim[j] * sc);
+              }
+              double2* py = Y + (int64_t)gm * N + gn;
+              if (u.d == 2) {
+                *py = y;
+              } else {
+                const double2 o = *py;
+                *py = cmk(o.x + y.x, o.y + y.y);
+              }
+            }
+          }
         }
+        if constexpr (TMEM_T) tc_wait_st();
       }
     }
   }
@@ -801,19 +860,20 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
     return MM_ERR_UNSUPPORTED;
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(ozaki_tc_kernel<int, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes(4, 4));
-    cudaFuncSetAttribute(ozaki_tc_kernel<long long, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ozaki_tc_kernel<int, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         tc_smem_bytes(0, 5));
+    cudaFuncSetAttribute(ozaki_tc_kernel<long long, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          tc_smem_bytes(8, 3));
   });
   dim3 grid((unsigned)((N + TC_NC - 1) / TC_NC), (unsigned)((M + TC_BM - 1) / TC_BM));
   if (grid.y > 65535) return MM_ERR_TOO_LARGE;
   mm::WsHeader* h = reinterpret_cast<mm::WsHeader*>(w);
   if (Kp <= TC_KP_INT32_MAX)
-    ozaki_tc_kernel<int, 4><<<grid, TC_THREADS, tc_smem_bytes(4, 4), st>>>(tu, tx, E, F, (double2*)Y, (int)M, (int)N,
-                                                                         Kp, slices, h, tc_budget_ns());
+    ozaki_tc_kernel<int, 5, true><<<grid, TC_THREADS, tc_smem_bytes(0, 5), st>>>(
+        tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices, h, tc_budget_ns());
   else
-    ozaki_tc_kernel<long long, 3><<<grid, TC_THREADS, tc_smem_bytes(8, 3), st>>>(tu, tx, E, F, (double2*)Y, (int)M,
-                                                                               (int)N, Kp, slices, h, tc_budget_ns());
+    ozaki_tc_kernel<long long, 3, false><<<grid, TC_THREADS, tc_smem_bytes(8, 3), st>>>(
+        tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices, h, tc_budget_ns());
   return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
 }
 
