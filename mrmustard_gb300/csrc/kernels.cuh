@@ -722,11 +722,10 @@ __device__ __forceinline__ bool flow_wait(WsHeader* h, const uint32_t* prog, uin
   return *s_fail == 0;
 }
 
-// Chunk (i, m) of the shared-memory region Gs, on lane pairs: lane 2a
-// computes the real part and lane 2a+1 the imaginary part of amplitude a, as
-// one chain of FMAs per part.  A GB300 FP64 warp instruction costs the same
-// for 1 or 32 active lanes, so this halves the FP64 instructions on the
-// latency-bound chain of the small levels.  The terms are those of fwd_chunk
+// Lane pairs: lane 2a computes the real part and lane 2a+1 the imaginary part
+// of amplitude a, as one chain of FMAs per part.  A GB300 FP64 warp
+// instruction costs the same for 1 or 32 active lanes, so this halves the FP64
+// instructions on the latency-bound chains.  The terms are those of fwd_chunk
 // (b_i G_p, A_ii sqrt(m-1) G_pp, A_ij sqrt(k_j) G_{p-1_j}, then the 1/sqrt(m)
 // scale); only the rounding of the complex products differs.
 __device__ __forceinline__ double flip_sign_if(double x, bool neg) {
@@ -737,34 +736,76 @@ __device__ __forceinline__ double part_fma(double2 x, double2 y, bool im, double
   return fma(x.x, im ? y.y : y.x, fma(flip_sign_if(x.y, !im), im ? y.x : y.y, acc));
 }
 
+// Barrier over the first n threads of the CTA (n a multiple of 32), id != 0.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ void bar_sync_n(uint32_t id, uint32_t n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+#else  // provided by the emulator
+void bar_sync_n(uint32_t id, uint32_t n);
+#endif
+
+// Small level i of the shared-memory region, all its chunks, on the first
+// `lanes` threads (lane pairs, see part_fma), synchronised by a named
+// barrier over those threads only.  With one amplitude per lane pair its
+// indices and coefficients are loaded once; the per-chunk coefficients
+// (A_ii sqrt(m), 1/sqrt(m)) are fetched one chunk ahead.
 template <int D>
-__device__ __forceinline__ void fwd_chunk_smem(const InstView& v, const double* __restrict__ rs, int i, int m,
-                                               double2* Gs) {
+__device__ void small_level(const InstView& v, const double* __restrict__ rs, int i, double2* Gs, uint32_t lanes) {
   const Geom& g = v.g;
   const uint32_t si = (uint32_t)g.strides[i];
+  const int Ci = (int)g.shape[i];
   const bool im = (threadIdx.x & 1u) != 0;
+  const uint32_t pairs = lanes >> 1, a0 = threadIdx.x >> 1;
   const double2 bi = __ldg(v.b + i);
   const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
-  const double2 cd = (m >= 2) ? crow[g.prefC[i] + m] : cmk(0.0, 0.0);
-  const double rsm = rs[m];
-  const uint32_t base = (uint32_t)m * si;
+  const int32_t pci = g.prefC[i];
   double* Gd = reinterpret_cast<double*>(Gs);
-  for (uint32_t a = threadIdx.x >> 1; a < si; a += blockDim.x >> 1) {
-    int32_t k[D];
-    decompose<D>(a, i + 1, g, k);
-    const uint32_t f = base + a, p = f - si;
-    double acc = part_fma(bi, Gs[p], im, 0.0);
-    if (m >= 2) acc = part_fma(cd, Gs[p - si], im, acc);
+  const bool one = si <= pairs;
+  int32_t k1[D];
+  double2 w1[D];
+  decompose<D>(a0 < si ? a0 : 0u, i + 1, g, k1);
 #pragma unroll
-    for (int j = 1; j < D; ++j) {
-      if (j > i && k[j] > 0) acc = part_fma(crow[g.prefC[j] + k[j]], Gs[p - (uint32_t)g.strides[j]], im, acc);
+  for (int j = 0; j < D; ++j) w1[j] = (one && j > i && k1[j] > 0) ? crow[g.prefC[j] + k1[j]] : cmk(0.0, 0.0);
+  double rs_c = rs[1];
+  double2 cd_c = cmk(0.0, 0.0);
+  for (int m = 1; m < Ci; ++m) {
+    const double rsm = rs_c;
+    const double2 cd = cd_c;
+    if (m + 1 < Ci) {
+      rs_c = rs[m + 1];
+      cd_c = crow[pci + m + 1];
     }
-    Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
+    const uint32_t base = (uint32_t)m * si;
+    if (one) {
+      if (a0 < si) {
+        const uint32_t f = base + a0, p = f - si;
+        double acc = part_fma(bi, Gs[p], im, 0.0);
+        if (m >= 2) acc = part_fma(cd, Gs[p - si], im, acc);
+#pragma unroll
+        for (int j = 1; j < D; ++j)
+          if (j > i && k1[j] > 0) acc = part_fma(w1[j], Gs[p - (uint32_t)g.strides[j]], im, acc);
+        Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
+      }
+    } else {
+      for (uint32_t a = a0; a < si; a += pairs) {
+        int32_t k[D];
+        decompose<D>(a, i + 1, g, k);
+        const uint32_t f = base + a, p = f - si;
+        double acc = part_fma(bi, Gs[p], im, 0.0);
+        if (m >= 2) acc = part_fma(cd, Gs[p - si], im, acc);
+#pragma unroll
+        for (int j = 1; j < D; ++j)
+          if (j > i && k[j] > 0) acc = part_fma(crow[g.prefC[j] + k[j]], Gs[p - (uint32_t)g.strides[j]], im, acc);
+        Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
+      }
+    }
+    bar_sync_n(1, lanes);
   }
 }
 
 // One CTA's range [lo, hi) of a shared level i (ctas[i] > 1) through chunks
-// 1..C_i-1, on lane pairs as in fwd_chunk_smem: pair a of the CTA holds
+// 1..C_i-1, on lane pairs (see part_fma): pair a of the CTA holds
 // amplitudes lo + a + u*(blockDim/2) (u < A), lane 2a their real parts and
 // lane 2a+1 their imaginary parts.  Each lane keeps its part of the last two
 // chunks in registers (gp: m-1, gpp: m-2; the partner's part comes by
@@ -901,10 +942,9 @@ __global__ void __launch_bounds__(256) fwd_flow_kernel(UniformSrc src, const dou
       if (threadIdx.x == 0) Gs[0] = sv.c;
       __syncthreads();
       for (int i = D - 1; i >= L; --i) {
-        for (int m = 1; m < (int)g.shape[i]; ++m) {
-          fwd_chunk_smem<D>(sv, rs, i, m, Gs);
-          __syncthreads();
-        }
+        const uint32_t lanes = min((2u * (uint32_t)g.strides[i] + 31u) / 32u * 32u, blockDim.x);
+        if (threadIdx.x < lanes) small_level<D>(sv, rs, i, Gs, lanes);
+        __syncthreads();
       }
       for (uint32_t f = threadIdx.x; f < fp.small_amps; f += blockDim.x) stG(sv, f, Gs[f], 7);
       __syncthreads();
