@@ -201,6 +201,28 @@ MM_API size_t mm_fock_gemm_workspace_bytes(int mode, int64_t M, int64_t N, int64
 MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128 *U, const mm_c128 *X, mm_c128 *Y,
                         int slices, void *ws, size_t ws_bytes, mm_stream_t stream);
 
+/* ------------------------------------------------------------- autoshape */
+
+/*
+ * Per-mode Fock cutoffs of B Gaussian density-matrix triples with M modes each.
+ * Replaces autoshape_numba(A, b, c, max_prob, max_shape, min_shape)
+ * (mrmustard/math/lattice/autoshape.py:23-154), which State.auto_shape
+ * (mrmustard/lab/states/base.py:383-430) calls on the triple of
+ * `ansatz.conj & ansatz` with the settings AUTOSHAPE_PROBABILITY (0.99999),
+ * AUTOSHAPE_MAX (50) and AUTOSHAPE_MIN (1).
+ * A (B, 2M, 2M), b (B, 2M), c (B,): device complex128, variables ordered bra
+ * copy then ket copy, as the reference reshapes them ((2, M, 2, M)).
+ * shapes (B, M): device int64 output, shapes[s * M + m] = clip(k, min_shape,
+ * max_shape) where k is the number of recurrence steps taken for mode m; a
+ * state whose reduction is singular (the reference raises LinAlgError) gets -1
+ * in every mode.  1 <= M <= 8; max_shape <= 99998 (the reference's sqrt table
+ * ends at 99999; larger values return MM_ERR_TOO_LARGE).  No workspace;
+ * asynchronous on `stream`.
+ */
+MM_API int mm_autoshape_batched(int64_t B, int M, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c,
+                                double max_prob, int64_t max_shape, int64_t min_shape, int64_t *shapes,
+                                mm_stream_t stream);
+
 /* ------------------------------------------------------------- diagnostics */
 
 /*

@@ -1,7 +1,8 @@
 """GB300-native Gaussian->Fock hot path of MrMustard.
 
 The renormalised multidimensional Hermite recurrence (``vanilla`` / ``stable`` /
-batched / VJP) and the Fock contraction after it, computed by hand-written sm_103a CUDA
+batched / VJP), the Fock contraction after it and the autoshape cutoffs before it, computed by
+hand-written sm_103a CUDA
 kernels in ``libmm_gb300.so`` behind a C ABI (include/mm_gb300.h).  The Python layer mirrors
 the reference's interface for this path; it has no CPU compute path.
 """
@@ -10,6 +11,7 @@ from __future__ import annotations
 
 from ._build_ext import build as build_library
 from .autograd import HermiteRenormalizedFn, hermite_renormalized_autograd
+from .autoshape import autoshape_batched, autoshape_numba, ket_dm_triple
 from .autotune import autotune
 from .backend import BackendGB300
 from .fock import apply_unitary, fock_gemm
@@ -47,6 +49,8 @@ __all__ = [
     "HermiteRenormalizedFn",
     "RaggedBatch",
     "apply_unitary",
+    "autoshape_batched",
+    "autoshape_numba",
     "autotune",
     "build_library",
     "fock_gemm",
@@ -55,6 +59,7 @@ __all__ = [
     "hermite_renormalized",
     "hermite_renormalized_autograd",
     "hermite_renormalized_batched",
+    "ket_dm_triple",
     "launch_count",
     "settings",
     "stable",

@@ -60,6 +60,7 @@ SIGNATURES = {
     "mm_selftest": (I32, [P, SZ, P, ctypes.POINTER(I32)]),
     "mm_fock_gemm_workspace_bytes": (SZ, [I32, I64, I64, I64, I32]),
     "mm_fock_gemm": (I32, [I32, I64, I64, I64, P, P, P, I32, P, SZ, P]),
+    "mm_autoshape_batched": (I32, [I64, I32, P, P, P, ctypes.c_double, I64, I64, P, P]),
 }
 
 

@@ -470,6 +470,8 @@ int launch_ragged_team(const mm_ragged_plan* p, const RaggedSrc& src, char* w, c
 }
 }  // namespace
 
+void mm::note_launches(int64_t n) { g_launches.fetch_add(n); }
+
 extern "C" {
 
 const char* mm_status_string(int status) {

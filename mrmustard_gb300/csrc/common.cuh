@@ -29,6 +29,9 @@ T& mm_emu_shared(int key);
 
 namespace mm {
 
+// Adds n to the library's launch counter (mm_launch_count); defined in capi.cu.
+void note_launches(int64_t n);
+
 // ---------------------------------------------------------------- complex helpers
 __device__ __forceinline__ double2 cmk(double r, double i) { return make_double2(r, i); }
 // a * b

@@ -831,6 +831,7 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
     dim3 grid((unsigned)((N + FG_BN - 1) / FG_BN), (unsigned)((M + FG_BM - 1) / FG_BM));
     if (grid.y > 65535) return MM_ERR_TOO_LARGE;
     zgemm_fp64_kernel<<<grid, 256, 0, st>>>((const double2*)U, (const double2*)X, (double2*)Y, (int)M, (int)N, (int)K);
+    mm::note_launches(1);
     return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
   }
   if (mode != 1) return MM_ERR_INVALID_ARG;
@@ -852,6 +853,7 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
     dim3 grid((unsigned)((N + OZ_BN - 1) / OZ_BN), (unsigned)((M + OZ_BM - 1) / OZ_BM));
     if (grid.y > 65535) return MM_ERR_TOO_LARGE;
     ozaki_mma_kernel<<<grid, 128, 0, st>>>(Us, Xs, E, F, (double2*)Y, (int)M, (int)N, Kp, slices);
+    mm::note_launches(5);
     return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
   }
   CUtensorMap tu, tx;
@@ -874,6 +876,7 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
   else
     ozaki_tc_kernel<long long, 3, false><<<grid, TC_THREADS, tc_smem_bytes(8, 3), st>>>(
         tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices, h, tc_budget_ns());
+  mm::note_launches(5);  // exponents, slices, products
   return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
 }
 

@@ -5,6 +5,10 @@
 (all-pivot average) recurrence even if ``stable=False`` is passed
 (mrmustard/math/backend_manager.py:682).
 
+``AUTOSHAPE_PROBABILITY``, ``AUTOSHAPE_MAX``, ``AUTOSHAPE_MIN`` mirror the reference's autoshape
+defaults (mrmustard/utils/settings.py:67-74): the probability mass to capture per mode and the
+clip range of the cutoffs, used when ``autoshape_numba``'s arguments are None.
+
 ``CHECK_DEVICE_STATUS``: after each call, synchronise and read the workspace status word, so a
 bounded inter-CTA wait that gave up raises at the call that caused it.  Benchmarks switch it
 off inside timed loops and check once afterwards.
@@ -19,6 +23,9 @@ class _Settings:
     def __init__(self):
         self.STABLE_FOCK_CONVERSION = False
         self.CHECK_DEVICE_STATUS = True
+        self.AUTOSHAPE_PROBABILITY = 0.99999
+        self.AUTOSHAPE_MAX = 50
+        self.AUTOSHAPE_MIN = 1
 
     @contextmanager
     def __call__(self, **kwargs):

@@ -29,6 +29,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "hermite_oracle.c"
+SOURCES = (SRC, HERE / "autoshape_oracle.c")
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
 
@@ -38,9 +39,11 @@ _lib = None
 def build(force: bool = False) -> Path:
     """Compile the C restatement into ``oracle/_build/liboracle.so`` (OpenMP when available)."""
     BUILD_DIR.mkdir(exist_ok=True)
-    if LIB_PATH.exists() and not force and LIB_PATH.stat().st_mtime >= SRC.stat().st_mtime:
+    if (LIB_PATH.exists() and not force
+            and all(LIB_PATH.stat().st_mtime >= src.stat().st_mtime for src in SOURCES)):
         return LIB_PATH
-    base = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", str(SRC)]
+    base = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+            *map(str, SOURCES)]
     tmp = BUILD_DIR / f"liboracle.{os.getpid()}.so"
     try:
         subprocess.run(base + ["-fopenmp", "-o", str(tmp), "-lm"], check=True, capture_output=True)
@@ -66,6 +69,8 @@ def lib():
             "oracle_vjp_batch": [I64, I32, P, P, P, P, P, P, P],
             "oracle_fwd_ragged": [I64, P, P, P, P, P, P, P, P, I32, P, P, P],
             "oracle_vjp_ragged": [I64, P, P, P, P, P, P, P, P, P, P, P, P, P],
+            "oracle_autoshape": [I32, P, P, P, D, I64, I64, P],
+            "oracle_autoshape_ragged": [I64, P, P, P, P, P, P, P, D, I64, I64, P],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -73,7 +78,6 @@ def lib():
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_set_numpy_division.argtypes = [ctypes.c_int]
         L.oracle_set_numpy_division.restype = None
-        del D
         _lib = L
     return _lib
 
@@ -208,6 +212,40 @@ def vjp_ragged(rh: RaggedHost, G, c, dLdG, indices=None):
     if rc:
         raise ValueError(f"oracle_vjp_ragged failed ({rc})")
     return dA, db, dc
+
+
+def autoshape(A, b, c, max_prob, max_shape, min_shape) -> np.ndarray:
+    """``autoshape_numba(A, b, c, max_prob, max_shape, min_shape)`` (autoshape.py:23-154) of one
+    density-matrix triple (A 2M x 2M, b 2M, c scalar) -> int64 shape of M cutoffs."""
+    A, b = _cc(A), _cc(b)
+    M = b.shape[0] // 2
+    if A.shape != (2 * M, 2 * M) or b.shape != (2 * M,):
+        raise ValueError("autoshape needs A (2M, 2M) and b (2M,)")
+    c = np.array([complex(np.asarray(c).reshape(-1)[0])], np.complex128)
+    out = np.zeros(M, np.int64)
+    rc = lib().oracle_autoshape(M, _ptr(A), _ptr(b), _ptr(c), float(max_prob), int(max_shape), int(min_shape),
+                                _ptr(out))
+    if rc:
+        raise ValueError(f"oracle_autoshape failed ({rc})")
+    return out
+
+
+def autoshape_ragged(As, bs, cs, max_prob, max_shape, min_shape):
+    """``autoshape`` of many triples with their own mode counts (OpenMP over states); returns the
+    list of shapes."""
+    Ms = np.array([len(b) // 2 for b in bs], np.int32)
+    a_off = np.concatenate([[0], np.cumsum(4 * Ms.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+    b_off = np.concatenate([[0], np.cumsum(2 * Ms.astype(np.int64))[:-1]]).astype(np.int64)
+    s_off = np.concatenate([[0], np.cumsum(Ms.astype(np.int64))[:-1]]).astype(np.int64)
+    A = _cc(np.concatenate([np.asarray(a).ravel() for a in As]))
+    b = _cc(np.concatenate([np.asarray(x).ravel() for x in bs]))
+    c = _cc(np.asarray(cs).ravel())
+    out = np.zeros(int(Ms.sum()), np.int64)
+    rc = lib().oracle_autoshape_ragged(len(Ms), _ptr(Ms), _ptr(a_off), _ptr(b_off), _ptr(s_off), _ptr(A), _ptr(b),
+                                       _ptr(c), float(max_prob), int(max_shape), int(min_shape), _ptr(out))
+    if rc:
+        raise ValueError(f"oracle_autoshape_ragged failed ({rc})")
+    return [out[o:o + m] for o, m in zip(s_off, Ms)]
 
 
 def fock_gemm(U, B):

@@ -54,6 +54,7 @@ static inline cplx cadd(cplx a, cplx b) { return CMPLX(creal(a) + creal(b), cima
  */
 static int g_numpy_div = 0;
 void oracle_set_numpy_division(int on) { g_numpy_div = on; }
+int oracle_numpy_division(void) { return g_numpy_div; }
 static inline cplx cdivr(cplx a, double d) {
   double ar = creal(a), ai = cimag(a);
   if (g_numpy_div) {

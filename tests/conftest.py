@@ -15,6 +15,7 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = ROOT / "tests" / "golden" / "hermite_golden.npz"
+AUTOSHAPE_GOLDEN = ROOT / "tests" / "golden" / "autoshape_golden.npz"
 
 
 def pytest_configure(config):
@@ -25,6 +26,12 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def golden():
     return dict(np.load(GOLDEN))
+
+
+@pytest.fixture(scope="session")
+def autoshape_golden():
+    z = np.load(AUTOSHAPE_GOLDEN)
+    return {k: z[k] for k in z.files}
 
 
 def golden_cases(z, need=("G",)):

@@ -100,3 +100,31 @@ def test_ragged_oracle_equals_per_instance(golden):
         assert np.array_equal(dA[rh.a_off[k]:rh.a_off[k] + D * D].reshape(D, D), rA)
         assert np.array_equal(db[rh.b_off[k]:rh.b_off[k] + D], rb)
         assert dc[k] == rc
+
+
+# ---------------------------------------------------------------- autoshape
+def test_autoshape_oracle_matches_reference(autoshape_golden):
+    """The C restatement of autoshape_numba (autoshape.py:23-154) gives the reference source's
+    shapes on every fixture case (tests/golden/make_autoshape_golden.py), with either lowering of
+    the reference's complex/real division.  Includes the reference's own known answers:
+    Coherent(alpha=1) -> (8,) (test_ket.py:98-100) and the vacuum -> (1,) (test_coherent.py:74-75)."""
+    g = autoshape_golden
+    assert tuple(g["coh1/shape"]) == (8,) and tuple(g["vac/shape"]) == (1,)
+    try:
+        for numpy_div in (True, False):
+            oracle.set_numpy_division(numpy_div)
+            for n in g["names"]:
+                p, hi, lo = g[f"{n}/params"]
+                got = oracle.autoshape(g[f"{n}/A"], g[f"{n}/b"], g[f"{n}/c"], p, int(hi), int(lo))
+                assert np.array_equal(got, g[f"{n}/shape"]), (n, numpy_div, got, g[f"{n}/shape"])
+    finally:
+        oracle.set_numpy_division(False)
+
+
+def test_autoshape_oracle_ragged_equals_single(autoshape_golden):
+    g = autoshape_golden
+    names = list(g["names"])
+    shapes = oracle.autoshape_ragged([g[f"{n}/A"] for n in names], [g[f"{n}/b"] for n in names],
+                                     [g[f"{n}/c"] for n in names], 0.999, 40, 2)
+    for n, s in zip(names, shapes):
+        assert np.array_equal(s, oracle.autoshape(g[f"{n}/A"], g[f"{n}/b"], g[f"{n}/c"], 0.999, 40, 2))
