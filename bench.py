@@ -444,9 +444,57 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     if cpu is not None:
         extras["max_rel_err_vs_oracle"] = extras_err
     extras["single_instance_forward"] = run_single(dev, time_eager, dfma_peak)
+    extras["autoshape"] = run_autoshape(dev, time_eager, As, bs,
+                                        with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
 
     extras["fock_contraction"] = run_contraction(dev, time_eager)
     return e2e_ms, h2d, d2h, plain_value, cpu, extras
+
+
+def run_autoshape(dev, time_eager, As, bs, with_cpu=True):
+    """autoshape (per-mode cutoffs, the reference's defaults 0.99999 / 50 / 1) of every state of the
+    workload as a normalised density-matrix triple, one launch per mode count; the C oracle with
+    OpenMP is the CPU baseline and the exact-match check.  Normalisation: the trace of a
+    density-matrix triple is |c exp(-b (A - X)^-1 b / 2) / sqrt(det(A - X))|, X = [[0, I], [I, 0]]."""
+    import torch
+
+    import mrmustard_gb300 as mm
+
+    trip, groups = [], {}
+    for k, (A, b) in enumerate(zip(As, bs)):
+        Adm, bdm, _ = mm.ket_dm_triple(A, b, 1.0)
+        M = len(b)
+        K = Adm - np.block([[np.zeros((M, M)), np.eye(M)], [np.eye(M), np.zeros((M, M))]])
+        tr = abs(np.exp(-0.5 * bdm @ np.linalg.solve(K, bdm)) / np.sqrt(np.linalg.det(K)))
+        trip.append((Adm, bdm, np.complex128(1.0 / tr)))
+        groups.setdefault(M, []).append(k)
+    dev_groups = {M: tuple(torch.as_tensor(np.array([trip[k][i] for k in ks]), device=dev) for i in range(3))
+                  for M, ks in groups.items()}
+
+    def run():
+        return {M: mm.autoshape_batched(*dev_groups[M]) for M in dev_groups}
+
+    t = time_eager(run, reps=20)
+    got = {M: v.cpu().numpy() for M, v in run().items()}
+    shapes = [None] * len(As)
+    for M, ks in groups.items():
+        for row, k in enumerate(ks):
+            shapes[k] = got[M][row]
+    flat = np.concatenate(shapes)
+    out = {"states": len(As), "modes": int(flat.size), "ms": t, "states_per_s": len(As) / (t * 1e-3),
+           "launches": len(groups), "mean_cutoff": float(flat.mean()),
+           "clipped_at_max_fraction": float(np.mean(flat == 50)),
+           "note": "time of the autoshape_batched calls (one per mode count), Python included"}
+    if with_cpu:
+        import oracle
+
+        t0 = time.perf_counter()
+        ref = oracle.autoshape_ragged([x[0] for x in trip], [x[1] for x in trip], [x[2] for x in trip], 0.99999, 50, 1)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(As) / tc, "unit": "states/s", "cores": oracle.num_threads(),
+                               "kind": "port", "sample": f"all {len(As)} states, one pass, {tc * 1e3:.1f} ms",
+                               "mismatches_vs_gpu": int(sum(not np.array_equal(a, r) for a, r in zip(shapes, ref)))}
+    return out
 
 
 def run_single(dev, time_eager, dfma_peak=None):
@@ -551,6 +599,8 @@ def main(argv=None):
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's default schedule")
     ap.add_argument("--only-contraction", action="store_true",
                     help="run only the Fock-contraction leg (gate tensor on 256 kets) and print its figures")
+    ap.add_argument("--only-autoshape", action="store_true",
+                    help="run only autoshape over the workload's states (GPU and CPU oracle)")
     ap.add_argument("--only-single", action="store_true",
                     help="run only the single large recurrences (4 x 40 pure, 4 x 50 density matrix)")
     ap.add_argument("--skip-extras", action="store_true",
@@ -558,7 +608,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()
-    if args.only_contraction or args.only_single:
+    if args.only_contraction or args.only_single or args.only_autoshape:
         import torch
 
         dev = torch.device("cuda", local_rank)
@@ -575,7 +625,10 @@ def main(argv=None):
             torch.cuda.synchronize()
             return e0.elapsed_time(e1) / reps
 
-        if args.only_single:
+        if args.only_autoshape:
+            _, As, bs, _ = make_workload(20260000, args.instances)
+            print(json.dumps({"autoshape": run_autoshape(dev, time_eager, As, bs, not args.skip_cpu)}), flush=True)
+        elif args.only_single:
             print(json.dumps({"single_instance_forward": run_single(dev, time_eager, fp64_probe(dev, time_eager))}),
                   flush=True)
         else:
