@@ -201,6 +201,26 @@ MM_API size_t mm_fock_gemm_workspace_bytes(int mode, int64_t M, int64_t N, int64
 MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128 *U, const mm_c128 *X, mm_c128 *Y,
                         int slices, void *ws, size_t ws_bytes, mm_stream_t stream);
 
+/* ------------------------------------------------------------- binomial fill */
+
+/*
+ * Fock tensor of one triple filled by total photon number with an L2 early
+ * stop.  Replaces binomial(local_cutoffs, A, b, c, max_l2, global_cutoff)
+ * (mrmustard/math/lattice/strategies/binomial.py:30-70), reached through
+ * math.hermite_renormalized_binomial (mrmustard/math/backend_manager.py:790-814,
+ * backend_numpy.py:405-421, which default max_l2 to AUTOSHAPE_PROBABILITY and
+ * global_cutoff to sum(shape) - D + 1).
+ * G (shape, C order) receives every amplitude of total photon number up to the
+ * first weight w < global_cutoff after which the running sum of |G|^2 exceeds
+ * max_l2 (or up to global_cutoff - 1), zeros elsewhere; *norm_out (device,
+ * optional) that sum.  Pass max_l2 = +inf for no early stop.  Amplitudes equal
+ * the vanilla recurrence's (same pivot rule).  ws: mm_binomial_workspace_bytes.
+ */
+MM_API size_t mm_binomial_workspace_bytes(int D, const int64_t *shape);
+MM_API int mm_binomial(int D, const int64_t *shape, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c,
+                       double max_l2, int64_t global_cutoff, mm_c128 *G, double *norm_out, void *ws,
+                       size_t ws_bytes, mm_stream_t stream);
+
 /* ------------------------------------------------------------- autoshape */
 
 /*

@@ -14,6 +14,7 @@ from .autograd import HermiteRenormalizedFn, hermite_renormalized_autograd
 from .autoshape import autoshape_batched, autoshape_numba, ket_dm_triple
 from .autotune import autotune
 from .backend import BackendGB300
+from .binomial import binomial, device_binomial, hermite_renormalized_binomial
 from .fock import apply_unitary, fock_gemm
 from .hermite import (
     device_fwd,
@@ -52,6 +53,8 @@ __all__ = [
     "autoshape_batched",
     "autoshape_numba",
     "autotune",
+    "binomial",
+    "device_binomial",
     "build_library",
     "fock_gemm",
     "device_fwd",
@@ -59,6 +62,7 @@ __all__ = [
     "hermite_renormalized",
     "hermite_renormalized_autograd",
     "hermite_renormalized_batched",
+    "hermite_renormalized_binomial",
     "ket_dm_triple",
     "launch_count",
     "settings",

@@ -61,6 +61,8 @@ SIGNATURES = {
     "mm_fock_gemm_workspace_bytes": (SZ, [I32, I64, I64, I64, I32]),
     "mm_fock_gemm": (I32, [I32, I64, I64, I64, P, P, P, I32, P, SZ, P]),
     "mm_autoshape_batched": (I32, [I64, I32, P, P, P, ctypes.c_double, I64, I64, P, P]),
+    "mm_binomial_workspace_bytes": (SZ, [I32, P]),
+    "mm_binomial": (I32, [I32, P, P, P, P, ctypes.c_double, I64, P, P, P, SZ, P]),
 }
 
 

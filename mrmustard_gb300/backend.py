@@ -3,13 +3,15 @@
 MrMustard dispatches ``math.hermite_renormalized`` by name to the active backend
 (``BackendManager._apply``, mrmustard/math/backend_manager.py:89-116), which for the numpy
 backend calls ``hermite_renormalized`` / ``hermite_renormalized_batched``
-(mrmustard/math/backend_numpy.py:381-403).  ``BackendGB300`` provides those two methods with the
-same signatures; a maintainer mixes it into the numpy backend so every
-other op keeps its numpy implementation.
+(mrmustard/math/backend_numpy.py:381-403), and ``math.hermite_renormalized_binomial`` to
+``hermite_renormalized_binomial`` (backend_numpy.py:405-421).  ``BackendGB300`` provides those
+methods with the same signatures; a maintainer mixes it into the numpy backend (see
+INTEGRATION.md) so every other op keeps its numpy implementation.
 """
 
 from __future__ import annotations
 
+from .binomial import hermite_renormalized_binomial as _binomial
 from .hermite import stable_numba, vanilla_batch_numba, vanilla_numba
 
 
@@ -23,3 +25,6 @@ class BackendGB300:
 
     def hermite_renormalized_batched(self, A, b, c, shape, stable=False, out=None):
         return vanilla_batch_numba(tuple(shape), A, b, c, stable, out)
+
+    def hermite_renormalized_binomial(self, A, B, C, shape, max_l2, global_cutoff):
+        return _binomial(A, B, C, tuple(shape), max_l2, global_cutoff)

@@ -539,6 +539,70 @@ int mm_hermite_fwd(int D, const int64_t* shape, const mm_c128* A, const mm_c128*
   return mm_hermite_fwd_batched(1, D, shape, A, b, c, stable, G, ws, ws_bytes, stream);
 }
 
+// Binomial fill: the forward's workspace, then the per-weight sums of |G|^2
+// and the stop weight.
+namespace {
+int64_t binomial_weights(const Geom& g) {
+  int64_t W = 1;
+  for (int i = 0; i < g.D; ++i) W += g.shape[i] - 1;
+  return W;
+}
+}  // namespace
+
+size_t mm_binomial_workspace_bytes(int D, const int64_t* shape) {
+  DevInfo di;
+  int sms = device_info(di) == MM_OK ? di.sms : 152;
+  UniformPlan P;
+  if (plan_uniform(1, D, shape, P, sms)) return 0;
+  return align_up(P.L.total) + align_up((size_t)(binomial_weights(P.g) + 2) * sizeof(double));
+}
+
+int mm_binomial(int D, const int64_t* shape, const mm_c128* A, const mm_c128* b, const mm_c128* c, double max_l2,
+                int64_t global_cutoff, mm_c128* G, double* norm_out, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  DevInfo di;
+  int rc = common_checks(ws, stream, di);
+  if (rc) return rc;
+  UniformPlan P;
+  if ((rc = plan_uniform(1, D, shape, P, di.sms))) return rc;
+  if (!A || !b || !c || !G) return MM_ERR_INVALID_ARG;
+  const size_t need = mm_binomial_workspace_bytes(D, shape);
+  if ((rc = check_ws(ws, ws_bytes, need))) return rc;
+  if (P.g.n > (int64_t)INT32_MAX * 256) return MM_ERR_TOO_LARGE;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  UniformSrc src = uniform_src(P, (const double2*)A, (const double2*)b, (const double2*)c, (double2*)G, nullptr, w);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  if ((rc = launch_setup(src, 1, w, P.L, 1, st))) return rc;
+  if ((rc = launch_fwd_uniform(P, src, w, 0, di, st))) return rc;
+  const int64_t W = binomial_weights(P.g);
+  double* subnorm = reinterpret_cast<double*>(w + align_up(P.L.total));
+  int64_t* stop = reinterpret_cast<int64_t*>(subnorm + W + 1);
+  const unsigned mask_blocks = (unsigned)std::min<int64_t>((P.g.n + 255) / 256, (int64_t)di.sms * 8);
+  switch (D) {
+#define MM_BN_CASE(DD)                                                                                        \
+  case DD:                                                                                                    \
+    weight_norm_kernel<DD><<<(unsigned)W, MM_BLOCK, 0, st>>>((const double2*)G, P.g, subnorm);               \
+    binomial_stop_kernel<<<1, 32, 0, st>>>(subnorm, (int)W, (const double2*)c, max_l2, global_cutoff, norm_out, \
+                                          stop);                                                              \
+    binomial_mask_kernel<DD><<<mask_blocks, 256, 0, st>>>((double2*)G, P.g, stop);                           \
+    break;
+    MM_BN_CASE(1)
+    MM_BN_CASE(2)
+    MM_BN_CASE(3)
+    MM_BN_CASE(4)
+    MM_BN_CASE(5)
+    MM_BN_CASE(6)
+    MM_BN_CASE(7)
+    MM_BN_CASE(8)
+#undef MM_BN_CASE
+    default:
+      return MM_ERR_UNSUPPORTED;
+  }
+  g_launches.fetch_add(3);
+  MM_CUDA(cudaGetLastError());
+  return MM_OK;
+}
+
 int mm_hermite_vjp_batched(int64_t B, int D, const int64_t* shape, const mm_c128* G, const mm_c128* c,
                            const mm_c128* dLdG, mm_c128* dA, mm_c128* db, mm_c128* dc, void* ws, size_t ws_bytes,
                            mm_stream_t stream) {

@@ -1041,6 +1041,87 @@ __global__ void view_selftest_kernel(Src src, int64_t k, const InstView* __restr
 // is required), so every CTA gives up after budget_ns.
 __global__ void wait_timeout_test_kernel(WsHeader* h, uint64_t budget_ns) { grid_barrier(h, 1, budget_ns, 1); }
 
+// ============================================================== binomial fill
+// Binomial strategy (reference: strategies/binomial.py:30-70): the tensor is
+// filled by total photon number w = |k| and stops after the first w whose
+// running sum of |G|^2 exceeds max_l2.  Every amplitude of weight <= w obeys
+// the same recurrence as the vanilla one (steps.vanilla_step takes the first
+// non-zero axis as pivot), so the GPU runs the vanilla forward, then
+// weight_norm_kernel sums |G|^2 per weight, binomial_stop_kernel finds the stop
+// weight, and binomial_mask_kernel zeroes every amplitude above it.
+
+// CTA w: sum of |G[k]|^2 over |k| = w (prefixes over axes 0..D-2 strided over
+// the CTA, the last axis fixed by w), reduced in a fixed order.
+template <int D>
+__global__ void __launch_bounds__(256) weight_norm_kernel(const double2* __restrict__ G, Geom g,
+                                                          double* __restrict__ subnorm) {
+  const int w = (int)blockIdx.x;
+  const int32_t CL = (int32_t)g.shape[D - 1];
+  const uint32_t P = (uint32_t)(g.n / CL);
+  double acc = 0.0;
+  for (uint32_t p = threadIdx.x; p < P; p += blockDim.x) {
+    uint32_t q = p;
+    int32_t sum = 0;
+#pragma unroll
+    for (int j = D - 2; j >= 0; --j) {
+      const uint32_t c = (uint32_t)g.shape[j];
+      sum += (int32_t)(q % c);
+      q /= c;
+    }
+    const int32_t kl = w - sum;
+    if (kl >= 0 && kl < CL) {
+      const double2 v = G[(int64_t)p * CL + kl];
+      const double h = hypot(v.x, v.y);
+      acc += h * h;
+    }
+  }
+  typedef double PartT[MM_BLOCK / 32];
+  MM_SHARED(PartT, part);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = part[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) t += part[i];
+    subnorm[w] = t;
+  }
+}
+
+// One thread: norm = |c|^2, then weights 1 .. global_cutoff-1 in order until
+// norm > max_l2; writes the norm and the last weight kept.
+__global__ void binomial_stop_kernel(const double* __restrict__ subnorm, int W, const double2* __restrict__ c,
+                                     double max_l2, int64_t global_cutoff, double* norm_out, int64_t* stop_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double h = hypot(c->x, c->y);
+  double norm = h * h;
+  int64_t stop = 0;
+  for (int64_t w = 1; w < global_cutoff; ++w) {
+    if (w < W) norm += subnorm[w];
+    stop = w;
+    if (norm > max_l2) break;
+  }
+  *stop_out = stop;
+  if (norm_out) *norm_out = norm;
+}
+
+// Zero every amplitude whose total photon number exceeds the stop weight.
+template <int D>
+__global__ void __launch_bounds__(256) binomial_mask_kernel(double2* __restrict__ G, Geom g,
+                                                            const int64_t* __restrict__ stop) {
+  const int64_t s = *stop;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.n; f += (int64_t)gridDim.x * blockDim.x) {
+    int64_t q = f, w = 0;
+#pragma unroll
+    for (int j = D - 1; j >= 0; --j) {
+      const int64_t c = g.shape[j];
+      w += q % c;
+      q /= c;
+    }
+    if (w > s) G[f] = cmk(0.0, 0.0);
+  }
+}
+
 // ============================================================== VJP
 // Per-thread accumulation over the fibers q of [q0, q1) (q = flat index over
 // axes 1..D-1) for one instance; results go to tot[] (weights applied).

@@ -29,7 +29,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "hermite_oracle.c"
-SOURCES = (SRC, HERE / "autoshape_oracle.c")
+SOURCES = (SRC, HERE / "autoshape_oracle.c", HERE / "binomial_oracle.c")
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
 
@@ -75,6 +75,8 @@ def lib():
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = ctypes.c_int
+        L.oracle_binomial.argtypes = [I32, P, P, P, P, D, I64, P, P]
+        L.oracle_binomial.restype = D
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_set_numpy_division.argtypes = [ctypes.c_int]
         L.oracle_set_numpy_division.restype = None
@@ -246,6 +248,21 @@ def autoshape_ragged(As, bs, cs, max_prob, max_shape, min_shape):
     if rc:
         raise ValueError(f"oracle_autoshape_ragged failed ({rc})")
     return [out[o:o + m] for o, m in zip(s_off, Ms)]
+
+
+def binomial(local_cutoffs, A, b, c, max_l2, global_cutoff):
+    """``binomial(local_cutoffs, A, b, c, max_l2, global_cutoff)`` (strategies/binomial.py:30-70)
+    -> (G, norm, last photon number filled).  ``max_l2=None`` never stops early."""
+    shape = tuple(int(s) for s in local_cutoffs)
+    A, b = _cc(A), _cc(b)
+    cc = np.array([complex(np.asarray(c).reshape(-1)[0])], np.complex128)
+    sh = np.array(shape, np.int64)
+    G = np.empty(shape, np.complex128)
+    stop = ctypes.c_int64(0)
+    l2 = float("inf") if max_l2 is None else float(max_l2)
+    norm = lib().oracle_binomial(len(shape), _ptr(sh), _ptr(A), _ptr(b), _ptr(cc), l2, int(global_cutoff), _ptr(G),
+                                 ctypes.byref(stop))
+    return G, float(norm), int(stop.value)
 
 
 def fock_gemm(U, B):

@@ -16,6 +16,7 @@ if str(ROOT) not in sys.path:
 
 GOLDEN = ROOT / "tests" / "golden" / "hermite_golden.npz"
 AUTOSHAPE_GOLDEN = ROOT / "tests" / "golden" / "autoshape_golden.npz"
+BINOMIAL_GOLDEN = ROOT / "tests" / "golden" / "binomial_golden.npz"
 
 
 def pytest_configure(config):
@@ -31,6 +32,12 @@ def golden():
 @pytest.fixture(scope="session")
 def autoshape_golden():
     z = np.load(AUTOSHAPE_GOLDEN)
+    return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def binomial_golden():
+    z = np.load(BINOMIAL_GOLDEN)
     return {k: z[k] for k in z.files}
 
 

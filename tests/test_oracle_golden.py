@@ -128,3 +128,37 @@ def test_autoshape_oracle_ragged_equals_single(autoshape_golden):
                                      [g[f"{n}/c"] for n in names], 0.999, 40, 2)
     for n, s in zip(names, shapes):
         assert np.array_equal(s, oracle.autoshape(g[f"{n}/A"], g[f"{n}/b"], g[f"{n}/c"], 0.999, 40, 2))
+
+
+# ---------------------------------------------------------------- binomial
+def test_binomial_oracle_matches_reference(binomial_golden):
+    """The C restatement of binomial (strategies/binomial.py:30-70 with steps.vanilla_step) gives
+    the reference source's tensors bit for bit under numpy's division lowering (and within 1e-15
+    under numba's), the same stop weight (zero pattern), and the norm to 1e-15 (numpy's complex
+    abs differs from hypot in the last bit)."""
+    g = binomial_golden
+    try:
+        for numpy_div in (True, False):
+            oracle.set_numpy_division(numpy_div)
+            for n in g["names"]:
+                l2, gc = g[f"{n}/params"]
+                G, norm, _ = oracle.binomial(tuple(g[f"{n}/shape"]), g[f"{n}/A"], g[f"{n}/b"], g[f"{n}/c"], l2, int(gc))
+                ref = g[f"{n}/G"]
+                assert np.array_equal(G == 0, ref == 0), n
+                if numpy_div:
+                    assert np.array_equal(G, ref), n
+                else:
+                    assert np.abs(G - ref).max() <= 1e-15 * np.abs(ref).max(), n
+                assert abs(norm - float(g[f"{n}/norm"])) <= 1e-15 * abs(float(g[f"{n}/norm"])), n
+    finally:
+        oracle.set_numpy_division(False)
+
+
+def test_binomial_oracle_equals_vanilla_prefix(binomial_golden):
+    """test_lattice_functions.py:122-138: binomial with local cutoffs (5, 5) equals the vanilla
+    tensor's [:5, :5] block where it is filled."""
+    g = binomial_golden
+    A, b, c = g["vs_vanilla/A"], g["vs_vanilla/b"], g["vs_vanilla/c"]
+    G, _, _ = oracle.binomial((5, 5), A, b, c, 0.9999, 12)
+    V = oracle.vanilla((10, 10), A, b, c)[:5, :5]
+    assert np.allclose(G, V)
