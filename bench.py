@@ -446,6 +446,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     extras["single_instance_forward"] = run_single(dev, time_eager, dfma_peak)
     extras["autoshape"] = run_autoshape(dev, time_eager, As, bs,
                                         with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
+    extras["binomial"] = run_binomial(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
 
     extras["fock_contraction"] = run_contraction(dev, time_eager)
     return e2e_ms, h2d, d2h, plain_value, cpu, extras
@@ -471,8 +472,19 @@ def run_autoshape(dev, time_eager, As, bs, with_cpu=True):
     dev_groups = {M: tuple(torch.as_tensor(np.array([trip[k][i] for k in ks]), device=dev) for i in range(3))
                   for M, ks in groups.items()}
 
+    streams = {M: torch.cuda.Stream(dev) for M in dev_groups}
+    main = torch.cuda.current_stream(dev)
+
     def run():
-        return {M: mm.autoshape_batched(*dev_groups[M]) for M in dev_groups}
+        # one launch per mode count, each on its own stream (they are independent)
+        res = {}
+        for M in dev_groups:
+            streams[M].wait_stream(main)
+            with torch.cuda.stream(streams[M]):
+                res[M] = mm.autoshape_batched(*dev_groups[M])
+        for M in dev_groups:
+            main.wait_stream(streams[M])
+        return res
 
     t = time_eager(run, reps=20)
     got = {M: v.cpu().numpy() for M, v in run().items()}
@@ -484,7 +496,7 @@ def run_autoshape(dev, time_eager, As, bs, with_cpu=True):
     out = {"states": len(As), "modes": int(flat.size), "ms": t, "states_per_s": len(As) / (t * 1e-3),
            "launches": len(groups), "mean_cutoff": float(flat.mean()),
            "clipped_at_max_fraction": float(np.mean(flat == 50)),
-           "note": "time of the autoshape_batched calls (one per mode count), Python included"}
+           "note": "time of the autoshape_batched calls (one per mode count, concurrent streams), Python included"}
     if with_cpu:
         import oracle
 
@@ -494,6 +506,49 @@ def run_autoshape(dev, time_eager, As, bs, with_cpu=True):
         out["cpu_baseline"] = {"value": len(As) / tc, "unit": "states/s", "cores": oracle.num_threads(),
                                "kind": "port", "sample": f"all {len(As)} states, one pass, {tc * 1e3:.1f} ms",
                                "mismatches_vs_gpu": int(sum(not np.array_equal(a, r) for a, r in zip(shapes, ref)))}
+    return out
+
+
+def run_binomial(dev, time_eager, with_cpu=True):
+    """Binomial fill of one 4-mode pure state at local cutoff 30 (810 k amplitudes) with the
+    reference's default max_l2 (0.99999) and global cutoff (sum(shape) - D + 1): GPU time of
+    mm_binomial (forward, per-weight norms, stop search, mask) against the C oracle on one core
+    (the reference's strategy is sequential over weights)."""
+    import torch
+    from scipy.stats import unitary_group
+
+    import mrmustard_gb300 as mm
+
+    rng = np.random.default_rng(4343)
+    D, cut = 4, 30
+    Q = unitary_group.rvs(D, random_state=rng)
+    A = (Q * rng.uniform(0.0, 0.8, D)) @ Q.T
+    b = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+    # normalised ket: |c|^2 = 1 / trace of the density-matrix triple of c = 1
+    Adm, bdm, _ = mm.ket_dm_triple(A, b, 1.0)
+    K = Adm - np.block([[np.zeros((D, D)), np.eye(D)], [np.eye(D), np.zeros((D, D))]])
+    c0 = 1.0 / np.sqrt(abs(np.exp(-0.5 * bdm @ np.linalg.solve(K, bdm)) / np.sqrt(np.linalg.det(K))))
+    Ad, bd = torch.as_tensor(A, device=dev), torch.as_tensor(b, device=dev)
+    cd = torch.tensor(complex(c0), dtype=torch.complex128, device=dev)
+    shape = (cut,) * D
+    gc = sum(shape) - D + 1
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        t = time_eager(lambda: mm.device_binomial(Ad, bd, cd, shape, 0.99999, gc), reps=10)
+    G, norm = mm.device_binomial(Ad, bd, cd, shape, 0.99999, gc)
+    Gh = G.cpu().numpy()
+    w = np.indices(shape).sum(axis=0)
+    kept = int(w[Gh != 0].max()) if np.any(Gh != 0) else 0
+    out = {"shape": list(shape), "amplitudes": cut ** D, "ms": t, "amplitudes_per_s": cut ** D / (t * 1e-3),
+           "norm": float(norm), "stop_weight": kept}
+    if with_cpu:
+        import oracle
+
+        t0 = time.perf_counter()
+        ref, rnorm, stop = oracle.binomial(shape, A, b, complex(c0), 0.99999, gc)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cut ** D / tc, "unit": "amplitudes/s", "cores": 1, "kind": "port",
+                               "sample": f"the same fill, one pass, {tc * 1e3:.1f} ms",
+                               "stop_weight": stop, "max_rel_err_vs_gpu": float(np.abs(Gh - ref).max() / np.abs(ref).max())}
     return out
 
 
@@ -599,6 +654,8 @@ def main(argv=None):
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's default schedule")
     ap.add_argument("--only-contraction", action="store_true",
                     help="run only the Fock-contraction leg (gate tensor on 256 kets) and print its figures")
+    ap.add_argument("--only-binomial", action="store_true",
+                    help="run only the binomial fill of a 4-mode state at cutoff 30 (GPU and CPU oracle)")
     ap.add_argument("--only-autoshape", action="store_true",
                     help="run only autoshape over the workload's states (GPU and CPU oracle)")
     ap.add_argument("--only-single", action="store_true",
@@ -608,7 +665,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()
-    if args.only_contraction or args.only_single or args.only_autoshape:
+    if args.only_contraction or args.only_single or args.only_autoshape or args.only_binomial:
         import torch
 
         dev = torch.device("cuda", local_rank)
@@ -625,7 +682,9 @@ def main(argv=None):
             torch.cuda.synchronize()
             return e0.elapsed_time(e1) / reps
 
-        if args.only_autoshape:
+        if args.only_binomial:
+            print(json.dumps({"binomial": run_binomial(dev, time_eager, not args.skip_cpu)}), flush=True)
+        elif args.only_autoshape:
             _, As, bs, _ = make_workload(20260000, args.instances)
             print(json.dumps({"autoshape": run_autoshape(dev, time_eager, As, bs, not args.skip_cpu)}), flush=True)
         elif args.only_single:

@@ -199,9 +199,9 @@ __global__ void __launch_bounds__(128) autoshape_kernel(int64_t B, const double2
   buf3[0][1] = c1;
   double norm = hypot(c1.r, c1.i);
   int64_t k = 0;
+  double s0 = 0.0, s1 = 1.0, s2 = sqrt(2.0);  // sqrt(k), sqrt(k + 1), sqrt(k + 2), carried over steps
   while (norm < max_prob && k < max_shape) {
     const int o = (int)(k & 1), n1 = o ^ 1;
-    const double s0 = sqrt((double)k), s1 = sqrt((double)(k + 1)), s2 = sqrt((double)(k + 2));
     for (int i = 0; i < 2; ++i) {
       const cx Av = cadd(cmul(A1[i * 2 + 0], buf2[o][0]), cmul(A1[i * 2 + 1], buf2[o][1]));
       buf2[n1][i] = cdivr(cadd(cmul(b1[i], buf3[o][1]), cmulr(Av, s0)), s1);
@@ -217,6 +217,9 @@ __global__ void __launch_bounds__(128) autoshape_kernel(int64_t B, const double2
         s2);
     norm = __dadd_rn(norm, hypot(buf3[n1][1].r, buf3[n1][1].i));
     ++k;
+    s0 = s1;
+    s1 = s2;
+    s2 = sqrt((double)(k + 2));
   }
   if (k < min_shape) k = min_shape;
   if (k > max_shape) k = max_shape;
