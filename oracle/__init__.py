@@ -29,7 +29,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "hermite_oracle.c"
-SOURCES = (SRC, HERE / "autoshape_oracle.c", HERE / "binomial_oracle.c")
+SOURCES = (SRC, HERE / "autoshape_oracle.c", HERE / "binomial_oracle.c", HERE / "diagonal_oracle.c")
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
 
@@ -56,8 +56,7 @@ def build(force: bool = False) -> Path:
 def lib():
     global _lib
     if _lib is None:
-        if not LIB_PATH.exists():
-            build()
+        build()  # no-op unless a source is newer than the library
         L = ctypes.CDLL(str(LIB_PATH))
         P, I64, I32, D = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
         cplx = P
@@ -77,6 +76,14 @@ def lib():
             fn.restype = ctypes.c_int
         L.oracle_binomial.argtypes = [I32, P, P, P, P, D, I64, P, P]
         L.oracle_binomial.restype = D
+        L.oracle_diagonal_amps.argtypes = [I32, P, I64, P, P, P, P]
+        L.oracle_diagonal_amps.restype = ctypes.c_int
+        L.oracle_diagonal_grad.argtypes = [I32, P, P, P, P, P]
+        L.oracle_diagonal_grad.restype = ctypes.c_int
+        L.oracle_diagonal_slots.argtypes = [I32]
+        L.oracle_diagonal_slots.restype = I64
+        L.oracle_fast_diagonal.argtypes = [I32, P, I64, P, P, P, I32, P]
+        L.oracle_fast_diagonal.restype = ctypes.c_int
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_set_numpy_division.argtypes = [ctypes.c_int]
         L.oracle_set_numpy_division.restype = None
@@ -263,6 +270,82 @@ def binomial(local_cutoffs, A, b, c, max_l2, global_cutoff):
     norm = lib().oracle_binomial(len(shape), _ptr(sh), _ptr(A), _ptr(b), _ptr(cc), l2, int(global_cutoff), _ptr(G),
                                  ctypes.byref(stop))
     return G, float(norm), int(stop.value)
+
+
+def _diag_split(W, M, cutoffs, nb_shape):
+    """One slot buffer -> the reference's (arr0, arr2, arr1010, arr1001, arr1)."""
+    cut = tuple(cutoffs)
+    P = int(np.prod(cut))
+    nb = int(np.prod(nb_shape)) if nb_shape else 1
+    W = W.reshape(-1, P * nb)
+    m1 = max(M - 1, 0)
+    arr0 = W[0].reshape(cut + nb_shape)
+    arr2 = W[1:1 + M].reshape((M,) + cut + nb_shape)
+    o = 1 + M
+    if M == 1:
+        arr1010 = np.zeros((1, 1, 1) + nb_shape, np.complex128)
+        arr1001 = np.zeros((1, 1, 1) + nb_shape, np.complex128)
+    else:
+        arr1010 = W[o:o + M * m1].reshape((M, m1) + cut + nb_shape)
+        arr1001 = W[o + M * m1:o + 2 * M * m1].reshape((M, m1) + cut + nb_shape)
+    o += 2 * M * m1
+    arr1 = W[o:o + 2 * M].reshape((2 * M,) + cut + nb_shape)
+    return arr0, arr2, arr1010, arr1001, arr1
+
+
+def diagonal_amps(A, B, G0, cutoffs, slots=False):
+    """``hermite_multidimensional_diagonal(A, B, G0, cutoffs)`` (compactFock/inputValidation.py:61-79,
+    diagonal_amps.py:140-248) on A, B already in the interleaved (mode0, mode0', mode1, ...) order
+    -> (arr0, arr2, arr1010, arr1001, arr1).  B may carry a batch axis last: (2M, nb).
+    ``slots=True`` returns the raw slot buffer instead."""
+    A, B = _cc(A), _cc(B)
+    cut = tuple(int(x) for x in cutoffs)
+    M = len(cut)
+    nb_shape = B.shape[1:]
+    nb = int(np.prod(nb_shape)) if nb_shape else 1
+    g0 = np.broadcast_to(np.asarray(G0, np.complex128), (nb,)).copy() if nb_shape else \
+        np.array([complex(np.asarray(G0).reshape(-1)[0])], np.complex128)
+    W = np.empty(int(lib().oracle_diagonal_slots(M)) * int(np.prod(cut)) * nb, np.complex128)
+    sh = np.array(cut, np.int64)
+    if lib().oracle_diagonal_amps(M, _ptr(sh), nb, _ptr(A), _ptr(np.ascontiguousarray(B.reshape(2 * M, nb))),
+                                  _ptr(g0), _ptr(W)):
+        raise ValueError("bad arguments")
+    return W if slots else _diag_split(W, M, cut, nb_shape)
+
+
+def diagonal_grad(A, B, G0, cutoffs):
+    """``grad_hermite_multidimensional_diagonal`` (compactFock/inputValidation.py:82-100,
+    diagonal_grad.py:261-378) -> (arr0_dG0, arr0_dA, arr0_dB) with shapes cutoffs,
+    cutoffs + (2M, 2M), cutoffs + (2M,).  Runs the forward pass itself."""
+    A, B = _cc(A), _cc(B)
+    cut = tuple(int(x) for x in cutoffs)
+    M = len(cut)
+    W = diagonal_amps(A, B, G0, cut, slots=True)
+    n = 2 * M
+    J = np.empty(W.size * (n * n + n), np.complex128)
+    sh = np.array(cut, np.int64)
+    if lib().oracle_diagonal_grad(M, _ptr(sh), _ptr(A), _ptr(B), _ptr(W), _ptr(J)):
+        raise ValueError("bad arguments")
+    P = int(np.prod(cut))
+    J0 = J[:P * (n * n + n)].reshape(P, n * n + n)
+    arr0 = W[:P].reshape(cut)
+    dG0 = (arr0 / np.complex128(np.asarray(G0).reshape(-1)[0])).astype(np.complex128)
+    return dG0, J0[:, :n * n].reshape(cut + (n, n)), J0[:, n * n:].reshape(cut + (n,))
+
+
+def fast_diagonal(A, b, c, output_cutoff, pnr_cutoffs, stable=False):
+    """``fast_diagonal(A, b, c, output_cutoff, pnr_cutoffs, stable)`` (strategies/fast_diagonal.py:32-77)
+    -> (pnr_1+1, ..., oc+1, oc+1)."""
+    A, b = _cc(A), _cc(b)
+    pnr = tuple(int(p) for p in pnr_cutoffs)
+    L = len(pnr) + 1
+    oc = int(output_cutoff)
+    out = np.empty(tuple(p + 1 for p in pnr) + (oc + 1, oc + 1), np.complex128)
+    cc = np.array([complex(np.asarray(c).reshape(-1)[0])], np.complex128)
+    sh = np.array(pnr if pnr else (0,), np.int64)
+    if lib().oracle_fast_diagonal(L, _ptr(sh), oc, _ptr(A), _ptr(b), _ptr(cc), int(bool(stable)), _ptr(out)):
+        raise ValueError("bad arguments")
+    return out
 
 
 def fock_gemm(U, B):

@@ -17,6 +17,7 @@ if str(ROOT) not in sys.path:
 GOLDEN = ROOT / "tests" / "golden" / "hermite_golden.npz"
 AUTOSHAPE_GOLDEN = ROOT / "tests" / "golden" / "autoshape_golden.npz"
 BINOMIAL_GOLDEN = ROOT / "tests" / "golden" / "binomial_golden.npz"
+DIAGONAL_GOLDEN = ROOT / "tests" / "golden" / "diagonal_golden.npz"
 
 
 def pytest_configure(config):
@@ -39,6 +40,16 @@ def autoshape_golden():
 def binomial_golden():
     z = np.load(BINOMIAL_GOLDEN)
     return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def diagonal_golden():
+    z = np.load(DIAGONAL_GOLDEN)
+    return {k: z[k] for k in z.files}
+
+
+def diagonal_cases(z, kind):
+    return [str(n) for n in z["names"] if str(z[f"{n}/kind"]) == kind]
 
 
 def golden_cases(z, need=("G",)):

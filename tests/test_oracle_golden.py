@@ -162,3 +162,124 @@ def test_binomial_oracle_equals_vanilla_prefix(binomial_golden):
     G, _, _ = oracle.binomial((5, 5), A, b, c, 0.9999, 12)
     V = oracle.vanilla((10, 10), A, b, c)[:5, :5]
     assert np.allclose(G, V)
+
+
+# ---------------------------------------------------------------- diagonal strategies
+def _rel(x, ref):
+    den = np.abs(ref).max()
+    return float(np.abs(x - ref).max() / den) if den > 0 else float(np.abs(x - ref).max())
+
+
+def test_diagonal_amps_oracle_matches_reference(diagonal_golden):
+    """The C restatement of compactFock's diagonal amplitudes (diagonal_amps.py:17-248) gives the
+    reference source's five arrays, with and without a batch axis on B, to 1e-14 relative (the
+    reference's `A[i] @ G_in` is a BLAS dot with its own summation order), and the same zero
+    pattern (the same elements written)."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    try:
+        oracle.set_numpy_division(True)
+        for n in diagonal_cases(g, "amps"):
+            got = oracle.diagonal_amps(g[f"{n}/A"], g[f"{n}/B"], g[f"{n}/G0"], tuple(g[f"{n}/cutoffs"]))
+            for name, x in zip(("arr0", "arr2", "arr1010", "arr1001", "arr1"), got):
+                ref = g[f"{n}/{name}"]
+                assert x.shape == ref.shape, (n, name)
+                assert np.array_equal(x == 0, ref == 0), (n, name)
+                assert _rel(x, ref) <= 1e-14, (n, name, _rel(x, ref))
+    finally:
+        oracle.set_numpy_division(False)
+
+
+def test_diagonal_grad_oracle_matches_reference(diagonal_golden):
+    """Jacobians of the diagonal amplitudes (diagonal_grad.py:17-378, inputValidation.py:82-100):
+    dG0, dA (cutoffs + (2M, 2M)) and dB (cutoffs + (2M,)) to 1e-13 relative."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    try:
+        oracle.set_numpy_division(True)
+        for n in diagonal_cases(g, "grad"):
+            got = oracle.diagonal_grad(g[f"{n}/A"], g[f"{n}/B"], g[f"{n}/G0"], tuple(g[f"{n}/cutoffs"]))
+            for name, x in zip(("dG0", "dA", "dB"), got):
+                ref = g[f"{n}/{name}"]
+                assert x.shape == ref.shape, (n, name)
+                assert _rel(x, ref) <= 1e-13, (n, name, _rel(x, ref))
+    finally:
+        oracle.set_numpy_division(False)
+
+
+def test_diagonal_amps_equal_vanilla_diagonal(diagonal_golden):
+    """tests/test_math/test_compactFock.py:19-43: arr0[k] = G[k0, k0, k1, k1, ...] of the vanilla
+    tensor on the interleaved triple."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    for n in diagonal_cases(g, "amps"):
+        A, B, cut = g[f"{n}/A"], g[f"{n}/B"], tuple(int(x) for x in g[f"{n}/cutoffs"])
+        if B.ndim > 1 or np.prod(cut) ** 2 > 2e5:
+            continue
+        G = oracle.vanilla(tuple(x for x in cut for _ in range(2)), A, B, g[f"{n}/G0"])
+        diag = np.array([G[tuple(i for k in idx for i in (k, k))] for idx in np.ndindex(*cut)]).reshape(cut)
+        arr0 = oracle.diagonal_amps(A, B, g[f"{n}/G0"], cut)[0]
+        assert np.allclose(arr0, diag, rtol=1e-10, atol=1e-14), n
+
+
+def test_diagonal_grad_central_differences(diagonal_golden):
+    """dA and dB of the oracle's Jacobians against central differences of its own amplitudes."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    n = diagonal_cases(g, "grad")[1]
+    A, B, G0, cut = g[f"{n}/A"], g[f"{n}/B"], g[f"{n}/G0"], tuple(g[f"{n}/cutoffs"])
+    _, dA, dB = oracle.diagonal_grad(A, B, G0, cut)
+    h = 1e-6
+    for (p, q) in ((0, 0), (1, 2), (3, 0)):
+        E = np.zeros_like(A)
+        E[p, q] = h
+        fd = (oracle.diagonal_amps(A + E, B, G0, cut)[0] - oracle.diagonal_amps(A - E, B, G0, cut)[0]) / (2 * h)
+        assert np.allclose(dA[..., p, q], fd, rtol=1e-6, atol=1e-9)
+    for r in (0, 3):
+        E = np.zeros_like(B)
+        E[r] = h
+        fd = (oracle.diagonal_amps(A, B + E, G0, cut)[0] - oracle.diagonal_amps(A, B - E, G0, cut)[0]) / (2 * h)
+        assert np.allclose(dB[..., r], fd, rtol=1e-6, atol=1e-9)
+
+
+def test_fast_diagonal_oracle_matches_reference(diagonal_golden):
+    """fast_diagonal (fast_diagonal.py:32-77), vanilla and stable first block, to 1e-14 relative,
+    including an output cutoff of 0 where the reference's weight loop ends early (zeros kept)."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    try:
+        oracle.set_numpy_division(True)
+        for n in diagonal_cases(g, "fd"):
+            got = oracle.fast_diagonal(g[f"{n}/A"], g[f"{n}/b"], g[f"{n}/c"], int(g[f"{n}/oc"]),
+                                       tuple(g[f"{n}/pnr"]), bool(g[f"{n}/stable"]))
+            ref = g[f"{n}/out"]
+            assert got.shape == ref.shape, n
+            assert np.array_equal(got == 0, ref == 0), n
+            assert _rel(got, ref) <= 1e-14, (n, _rel(got, ref))
+    finally:
+        oracle.set_numpy_division(False)
+
+
+def test_fast_diagonal_equals_vanilla_block(diagonal_golden):
+    """tests/test_math/test_fast_diagonal.py:24-45: the leftover-mode blocks equal the vanilla
+    tensor's entries G[m, k, n, k] (2 modes) / G[m, k1, k2, n, k1, k2] (3 modes)."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    for n in diagonal_cases(g, "fd"):
+        pnr, oc = tuple(int(p) for p in g[f"{n}/pnr"]), int(g[f"{n}/oc"])
+        L = len(pnr) + 1
+        if L > 3 or oc == 0:
+            continue
+        A, b, c = g[f"{n}/A"], g[f"{n}/b"], g[f"{n}/c"]
+        shape = (oc + 1, *(p + 1 for p in pnr))
+        G = oracle.vanilla(shape + shape, A, b, c)
+        fd = oracle.fast_diagonal(A, b, c, oc, pnr, bool(g[f"{n}/stable"]))
+        for q in np.ndindex(*(p + 1 for p in pnr)):
+            ref = G[(slice(None), *q, slice(None), *q)]
+            assert np.allclose(fd[q], ref, rtol=1e-9, atol=1e-13), (n, q)
