@@ -243,6 +243,69 @@ MM_API int mm_autoshape_batched(int64_t B, int M, const mm_c128 *A, const mm_c12
                                 double max_prob, int64_t max_shape, int64_t min_shape, int64_t *shapes,
                                 mm_stream_t stream);
 
+/* ------------------------------------------------------------- diagonal strategies */
+
+/*
+ * Number of "slot" arrays of the diagonal strategy for M modes: the reference's
+ * arr0 (1), arr2 (M), arr1010 (M (M-1)), arr1001 (M (M-1)) and arr1 (2M), stored back
+ * to back in that order, each of P * nb values (P = prod cutoffs, params in C order,
+ * batch index last) -- each one exactly the layout of the reference's array.
+ */
+MM_API int64_t mm_diagonal_slots(int M);
+MM_API size_t mm_diagonal_workspace_bytes(int M, const int64_t *cutoffs, int64_t nb);
+
+/*
+ * Diagonal of the Fock representation (PNR amplitudes): replaces
+ * fock_representation_diagonal_amps(A, B, G0, M, cutoffs)
+ * (mrmustard/math/lattice/strategies/compactFock/diagonal_amps.py:217-248), reached
+ * through hermite_multidimensional_diagonal (compactFock/inputValidation.py:61-79) and
+ * math.hermite_renormalized_diagonal (mrmustard/math/backend_manager.py:729-757,
+ * backend_numpy.py:423-432).  A (2M, 2M) and B (2M, nb) in the interleaved mode order
+ * (mode0, mode0', mode1, ...), G0 (nb,): device complex128.  W receives
+ * mm_diagonal_slots(M) * P * nb values; W[0 .. P*nb) is arr0 = G[k0,k0,k1,k1,...].
+ * 1 <= M <= 8.  Asynchronous on `stream`; ws from mm_diagonal_workspace_bytes.
+ */
+MM_API int mm_diagonal_amps(int M, const int64_t *cutoffs, int64_t nb, const mm_c128 *A, const mm_c128 *B,
+                            const mm_c128 *G0, mm_c128 *W, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/*
+ * Jacobians of every slot w.r.t. A and B: replaces fock_representation_diagonal_grad
+ * (compactFock/diagonal_grad.py:261-378) behind grad_hermite_multidimensional_diagonal
+ * (compactFock/inputValidation.py:82-100).  W: the slots of mm_diagonal_amps with nb = 1.
+ * J receives mm_diagonal_slots(M) * P * (4M^2 + 2M) values, J[slot][point][d/dA (2M x 2M
+ * row-major), then d/dB (2M)]; J[0 .. P*(4M^2+2M)) are arr0_dA and arr0_dB.  ws as for
+ * mm_diagonal_workspace_bytes(M, cutoffs, 1).
+ */
+MM_API int mm_diagonal_jacobian(int M, const int64_t *cutoffs, const mm_c128 *A, const mm_c128 *B, const mm_c128 *W,
+                                mm_c128 *J, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/*
+ * Vector-Jacobian product of the diagonal: dA = sum_k g_k arr0_dA[k], dB = sum_k g_k
+ * arr0_dB[k], dG0 = sum_k g_k arr0[k] / G0 -- the contraction of
+ * hermite_renormalized_diagonal_jax_bwd (mrmustard/math/jax_vjps/hermite.py:292-329).
+ * J, W from the two calls above; g (P,) upstream; dA (2M, 2M), dB (2M,), dG0 (1,).
+ */
+MM_API int mm_diagonal_vjp(int M, const int64_t *cutoffs, const mm_c128 *J, const mm_c128 *W, const mm_c128 *G0,
+                           const mm_c128 *g, mm_c128 *dA, mm_c128 *dB, mm_c128 *dG0, mm_stream_t stream);
+
+MM_API size_t mm_fast_diagonal_workspace_bytes(int L, const int64_t *pnr_cutoffs, int64_t output_cutoff);
+
+/*
+ * Conditional density matrices of mode 0 with modes 1..L-1 photon-number resolved:
+ * replaces fast_diagonal(A, b, c, output_cutoff, pnr_cutoffs, stable)
+ * (mrmustard/math/lattice/strategies/fast_diagonal.py:32-77), which
+ * backend_numpy.hermite_renormalized_1leftoverMode calls (backend_numpy.py:434-446).
+ * A (2L, 2L), b (2L,), c (1,) in the caller's order (all first copies, then all second
+ * copies); out: (pnr_1+1, ..., pnr_{L-1}+1, oc+1, oc+1) complex128, the layout
+ * fast_diagonal returns (the backend transposes the last two axes to the front).
+ * stable != 0 fills the first block with stable_numba instead of vanilla_numba.
+ * Entries whose weight the reference's loop (range(1, 2 oc + 2 sum(pnr) - L)) never
+ * reaches stay zero, as there.  2 <= L <= 8 (L = 1 returns MM_ERR_UNSUPPORTED).
+ */
+MM_API int mm_fast_diagonal(int L, const int64_t *pnr_cutoffs, int64_t output_cutoff, const mm_c128 *A,
+                            const mm_c128 *b, const mm_c128 *c, int stable, mm_c128 *out, void *ws, size_t ws_bytes,
+                            mm_stream_t stream);
+
 /* ------------------------------------------------------------- diagnostics */
 
 /*

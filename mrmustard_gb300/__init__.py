@@ -1,7 +1,8 @@
 """GB300-native Gaussian->Fock hot path of MrMustard.
 
 The renormalised multidimensional Hermite recurrence (``vanilla`` / ``stable`` /
-batched / VJP), the Fock contraction after it and the autoshape cutoffs before it, computed by
+batched / VJP), the Fock contraction after it, the autoshape cutoffs before it, and the binomial
+and diagonal (PNR / leftover-mode) strategies of the same recurrence, computed by
 hand-written sm_103a CUDA
 kernels in ``libmm_gb300.so`` behind a C ABI (include/mm_gb300.h).  The Python layer mirrors
 the reference's interface for this path; it has no CPU compute path.
@@ -15,6 +16,14 @@ from .autoshape import autoshape_batched, autoshape_numba, ket_dm_triple
 from .autotune import autotune
 from .backend import BackendGB300
 from .binomial import binomial, device_binomial, hermite_renormalized_binomial
+from .diagonal import (
+    fast_diagonal,
+    grad_hermite_multidimensional_diagonal,
+    hermite_multidimensional_diagonal,
+    hermite_renormalized_1leftoverMode,
+    hermite_renormalized_diagonal,
+    hermite_renormalized_diagonal_autograd,
+)
 from .fock import apply_unitary, fock_gemm
 from .hermite import (
     device_fwd,
@@ -55,6 +64,12 @@ __all__ = [
     "autotune",
     "binomial",
     "device_binomial",
+    "fast_diagonal",
+    "grad_hermite_multidimensional_diagonal",
+    "hermite_multidimensional_diagonal",
+    "hermite_renormalized_1leftoverMode",
+    "hermite_renormalized_diagonal",
+    "hermite_renormalized_diagonal_autograd",
     "build_library",
     "fock_gemm",
     "device_fwd",

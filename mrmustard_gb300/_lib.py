@@ -63,6 +63,13 @@ SIGNATURES = {
     "mm_autoshape_batched": (I32, [I64, I32, P, P, P, ctypes.c_double, I64, I64, P, P]),
     "mm_binomial_workspace_bytes": (SZ, [I32, P]),
     "mm_binomial": (I32, [I32, P, P, P, P, ctypes.c_double, I64, P, P, P, SZ, P]),
+    "mm_diagonal_slots": (I64, [I32]),
+    "mm_diagonal_workspace_bytes": (SZ, [I32, P, I64]),
+    "mm_diagonal_amps": (I32, [I32, P, I64, P, P, P, P, P, SZ, P]),
+    "mm_diagonal_jacobian": (I32, [I32, P, P, P, P, P, P, SZ, P]),
+    "mm_diagonal_vjp": (I32, [I32, P, P, P, P, P, P, P, P, P]),
+    "mm_fast_diagonal_workspace_bytes": (SZ, [I32, P, I64]),
+    "mm_fast_diagonal": (I32, [I32, P, I64, P, P, P, I32, P, P, SZ, P]),
 }
 
 

@@ -3,8 +3,10 @@
 MrMustard dispatches ``math.hermite_renormalized`` by name to the active backend
 (``BackendManager._apply``, mrmustard/math/backend_manager.py:89-116), which for the numpy
 backend calls ``hermite_renormalized`` / ``hermite_renormalized_batched``
-(mrmustard/math/backend_numpy.py:381-403), and ``math.hermite_renormalized_binomial`` to
-``hermite_renormalized_binomial`` (backend_numpy.py:405-421).  ``BackendGB300`` provides those
+(mrmustard/math/backend_numpy.py:381-403), ``math.hermite_renormalized_binomial`` to
+``hermite_renormalized_binomial`` (backend_numpy.py:405-421), and
+``math.hermite_renormalized_diagonal`` / ``math.hermite_renormalized_1leftoverMode`` to the methods
+of those names (backend_numpy.py:423-446).  ``BackendGB300`` provides those
 methods with the same signatures; a maintainer mixes it into the numpy backend (see
 INTEGRATION.md) so every other op keeps its numpy implementation.
 """
@@ -12,6 +14,8 @@ INTEGRATION.md) so every other op keeps its numpy implementation.
 from __future__ import annotations
 
 from .binomial import hermite_renormalized_binomial as _binomial
+from .diagonal import hermite_renormalized_1leftoverMode as _leftover
+from .diagonal import hermite_renormalized_diagonal as _diagonal
 from .hermite import stable_numba, vanilla_batch_numba, vanilla_numba
 
 
@@ -28,3 +32,10 @@ class BackendGB300:
 
     def hermite_renormalized_binomial(self, A, B, C, shape, max_l2, global_cutoff):
         return _binomial(A, B, C, tuple(shape), max_l2, global_cutoff)
+
+    def hermite_renormalized_diagonal(self, A, B, C, cutoffs, reorderedAB=True):
+        return _diagonal(A, B, C, tuple(cutoffs), reorderedAB)
+
+    def hermite_renormalized_1leftoverMode(self, A, b, c, output_cutoff, pnr_cutoffs, stable=False,
+                                           reorderedAB=True):
+        return _leftover(A, b, c, output_cutoff, tuple(pnr_cutoffs), stable, reorderedAB)

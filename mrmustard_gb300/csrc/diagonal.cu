@@ -1,0 +1,879 @@
+// Diagonal strategies of the Fock recurrence: photon-number (PNR) probabilities and
+// leftover-mode density matrices without filling the whole tensor.
+//
+// 1. compactFock diagonal amplitudes (mrmustard/math/lattice/strategies/compactFock/
+//    diagonal_amps.py:17-248), called by math.hermite_renormalized_diagonal
+//    (backend_manager.py:729-757 -> backend_numpy.py:423-432 / backend_jax.py:513-522).
+//    For M modes with cutoffs c_k the recurrence walks the params lattice (a, b, ...)
+//    in order of a + b + ...; at each point a "diagonal pivot" fills the 2M
+//    neighbours [a+1,a,...] / [a,a+1,...] / ... (array arr1) and "off-diagonal
+//    pivots" fill arr0 (the diagonal G[a,a,b,b,...]), arr2, arr1010, arr1001.
+//    Points of equal weight are independent, so the kernel runs one weight per
+//    step of a cooperative grid, one thread per (point, output row, batch column);
+//    an off-diagonal row recomputes the diagonal-pivot value of its own point that
+//    it reads (the same expression on the same inputs), so a weight needs one grid
+//    barrier.  Storage: the reference's five arrays back to back in one buffer of
+//    "slots" (slot 0 = arr0, then arr2[d], arr1010[d][e], arr1001[d][e], arr1[i]),
+//    each P x nb values (P = prod c_k, params in C order, batch index last).
+// 2. their Jacobians (compactFock/diagonal_grad.py:17-378): the same schedule with
+//    one thread per (point, output row, component of d/dA (2M x 2M) and d/dB (2M)).
+// 3. fast_diagonal (mrmustard/math/lattice/strategies/fast_diagonal.py:32-200), which
+//    backend_numpy.hermite_renormalized_1leftoverMode calls: the recurrence on the
+//    detected modes' near-diagonal lattice (pairs |a - b| <= 2, at most one pair at
+//    distance 2), every lattice point an (oc+1) x (oc+1) block of mode 0.  Points are
+//    stored densely over per-pair states a*5 + (a - b + 2); one thread per (point,
+//    block element), one grid barrier per weight.
+//
+// Points are ordered by weight on the device (counting sort), so every entry point
+// is a fixed sequence of launches without host copies (capturable in a CUDA graph).
+// Arithmetic is FP64 with fused multiply-adds; parity with the reference is to
+// rounding (the reference's own row products are BLAS dots).
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+using namespace mm;
+
+namespace {
+
+constexpr int DG_MAXM = 8;          // modes of the diagonal strategy
+constexpr int FD_MAXK = 7;          // detected modes of fast_diagonal (L <= 8)
+constexpr int DG_BLOCK = 128;       // threads per CTA of the wavefront kernels
+constexpr int SORT_BLOCK = 256;
+constexpr int kMaxWeights = 1 << 16;
+constexpr size_t kWsAlign = 256;
+
+size_t al(size_t x) { return (x + kWsAlign - 1) / kWsAlign * kWsAlign; }
+
+#ifndef MM_HOST_EMULATION
+int cuda_status() { return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA; }
+#endif
+
+uint64_t budget_ns() {
+  const char* s = getenv("MM_WAIT_BUDGET_NS");
+  return s ? strtoull(s, nullptr, 10) : 2000000000ull;
+}
+
+// ------------------------------------------------------------------ lattices
+
+struct DiagLat {
+  int M;
+  int n;  // 2M
+  int32_t c[DG_MAXM];
+  int32_t st[DG_MAXM];
+  int32_t P;
+  int32_t nb;
+  int32_t W;  // number of weights: sum(c - 1) + 1
+};
+
+__host__ __device__ __forceinline__ int64_t slot_arr2(const DiagLat& L, int d) { return 1 + d; }
+__host__ __device__ __forceinline__ int64_t slot_1010(const DiagLat& L, int d, int e) {
+  return 1 + L.M + (int64_t)d * (L.M - 1) + e;
+}
+__host__ __device__ __forceinline__ int64_t slot_1001(const DiagLat& L, int d, int e) {
+  return 1 + L.M + (int64_t)L.M * (L.M - 1) + (int64_t)d * (L.M - 1) + e;
+}
+__host__ __device__ __forceinline__ int64_t slot_arr1(const DiagLat& L, int i) {
+  return 1 + L.M + 2 * (int64_t)L.M * (L.M - 1) + i;
+}
+__host__ __device__ __forceinline__ int64_t diag_slots(int M) { return 1 + M + 2 * (int64_t)M * (M - 1) + 2 * M; }
+
+__device__ __forceinline__ int diag_weight(const DiagLat& L, int32_t f, int32_t* p) {
+  int w = 0;
+  for (int k = 0; k < L.M; ++k) {
+    p[k] = f / L.st[k];
+    f -= p[k] * L.st[k];
+    w += p[k];
+  }
+  return w;
+}
+
+struct FdLat {
+  int K;  // detected modes (pairs)
+  int q;  // oc + 1
+  int32_t pnr[FD_MAXK];
+  int32_t rad[FD_MAXK];  // 5 (pnr + 1)
+  int32_t pst[FD_MAXK];  // mixed-radix strides of the dense point id
+  int32_t npts;
+  int32_t ost[FD_MAXK];  // strides of the output's leading (pnr + 1) axes
+  int32_t W;             // number of weights of the lattice: 2 sum(pnr) + 1
+  int32_t wend;          // the reference's loop bound: weights 1 .. wend - 1 are filled
+};
+
+// coordinates of a dense id: returns the weight, or -1 when the id is not a lattice point
+__device__ __forceinline__ int fd_decode(const FdLat& F, int32_t id, int32_t* k) {
+  int n2 = 0, w = 0;
+  for (int j = 0; j < F.K; ++j) {
+    const int32_t s = (id / F.pst[j]) % F.rad[j];
+    const int32_t a = s / 5, dl = s % 5 - 2, b = a - dl;
+    if (b < 0 || b > F.pnr[j]) return -1;
+    n2 += (dl == 2 || dl == -2);
+    k[2 * j] = a;
+    k[2 * j + 1] = b;
+    w += a + b;
+  }
+  return n2 <= 1 ? w : -1;
+}
+
+// ------------------------------------------------------------------ weight sort
+// Counting sort of the lattice points by weight: histogram, scan, scatter.  The
+// order inside one weight depends on atomics and does not matter (the points of one
+// weight are independent).
+
+struct SortBufs {
+  int32_t* count;   // W
+  int32_t* start;   // W + 1
+  int32_t* cursor;  // W
+  int32_t* order;   // points
+};
+
+template <class Lat>
+__device__ __forceinline__ int point_weight(const Lat& L, int32_t id);
+template <>
+__device__ __forceinline__ int point_weight<DiagLat>(const DiagLat& L, int32_t id) {
+  int32_t p[DG_MAXM];
+  return diag_weight(L, id, p);
+}
+template <>
+__device__ __forceinline__ int point_weight<FdLat>(const FdLat& F, int32_t id) {
+  int32_t k[2 * FD_MAXK];
+  return fd_decode(F, id, k);
+}
+
+template <class Lat>
+__global__ void sort_count_kernel(Lat L, int32_t n, SortBufs sb) {
+  for (int32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+    const int w = point_weight(L, id);
+    if (w >= 0) atomicAdd(&sb.count[w], 1);
+  }
+}
+
+__global__ void sort_scan_kernel(int32_t W, SortBufs sb) {
+  // one CTA: a serial scan in chunks by thread 0 is enough for W <= 65536
+  if (threadIdx.x == 0) {
+    int32_t acc = 0;
+    for (int32_t w = 0; w < W; ++w) {
+      sb.start[w] = acc;
+      sb.cursor[w] = acc;
+      acc += sb.count[w];
+    }
+    sb.start[W] = acc;
+  }
+}
+
+template <class Lat>
+__global__ void sort_scatter_kernel(Lat L, int32_t n, SortBufs sb) {
+  for (int32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+    const int w = point_weight(L, id);
+    if (w >= 0) sb.order[atomicAdd(&sb.cursor[w], 1)] = id;
+  }
+}
+
+#ifndef MM_HOST_EMULATION  // the host emulation of the kernels runs them without the launch code below
+template <class Lat>
+int launch_sort(const Lat& L, int32_t n, int32_t W, const SortBufs& sb, int sms, cudaStream_t st) {
+  if (cudaMemsetAsync(sb.count, 0, (size_t)W * sizeof(int32_t), st) != cudaSuccess) return MM_ERR_CUDA;
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + SORT_BLOCK - 1) / SORT_BLOCK, 4 * sms));
+  sort_count_kernel<Lat><<<blocks, SORT_BLOCK, 0, st>>>(L, n, sb);
+  sort_scan_kernel<<<1, 32, 0, st>>>(W, sb);
+  sort_scatter_kernel<Lat><<<blocks, SORT_BLOCK, 0, st>>>(L, n, sb);
+  note_launches(3);
+  return cuda_status();
+}
+#endif
+
+// ------------------------------------------------------------------ grid step barrier
+__device__ __forceinline__ bool step_barrier(WsHeader* h, uint32_t& epoch, uint64_t budget) {
+  if (gridDim.x == 1) {
+    __syncthreads();
+    return true;
+  }
+  return grid_barrier(h, ++epoch, budget, 0);
+}
+
+// ------------------------------------------------------------------ 1. diagonal amplitudes
+
+struct DiagArgs {
+  DiagLat L;
+  const double2* A;   // 2M x 2M, interleaved mode order
+  const double2* B;   // 2M x nb
+  const double2* G0;  // nb
+  double2* Wv;        // slots x P x nb
+  double2* J;         // Jacobians: slots x P x (4M^2 + 2M) (Jacobian kernel only)
+  SortBufs sb;
+  WsHeader* h;
+  uint64_t budget;
+};
+
+__device__ __forceinline__ double2 ldv(const double2* p) { return __ldcg(p); }
+__device__ __forceinline__ double2 cdivs(double2 a, double s) { return cmk(a.x / s, a.y / s); }
+
+// Row i of the diagonal pivot at point f (diagonal_amps.py:92-137):
+// (arr0[p] B_i + sum_l A_il sqrt(p_{l/2}) arr1[l^1][p - 1_{l/2}]) / sqrt(p_{i/2} + 1).
+__device__ __forceinline__ double2 diag_row(const DiagArgs& a, const int32_t* p, int32_t f, int i, int32_t col) {
+  const DiagLat& L = a.L;
+  const int64_t PN = (int64_t)L.P * L.nb;
+  double2 acc = cmul(ldv(&a.Wv[(int64_t)f * L.nb + col]), __ldg(&a.B[(int64_t)i * L.nb + col]));
+  for (int l = 0; l < L.n; ++l) {
+    const int k = l >> 1;
+    if (p[k] == 0) continue;
+    const double2 g = ldv(&a.Wv[slot_arr1(L, l ^ 1) * PN + (int64_t)(f - L.st[k]) * L.nb + col]);
+    acc = cfma(__ldg(&a.A[i * L.n + l]), cscale(sqrt((double)p[k]), g), acc);
+  }
+  return cdivs(acc, sqrt((double)(p[i >> 1] + 1)));
+}
+
+// Output row `row` of the off-diagonal pivot d at point f (diagonal_amps.py:17-89),
+// with g = arr1[2d][f] (the diagonal pivot's row 2d at the same point).
+__device__ __forceinline__ double2 offdiag_row(const DiagArgs& a, const int32_t* p, int32_t f, int d, int row,
+                                               double2 g, int32_t col) {
+  const DiagLat& L = a.L;
+  const int64_t PN = (int64_t)L.P * L.nb;
+  double2 acc = cmul(g, __ldg(&a.B[(int64_t)row * L.nb + col]));
+  // G_in[2d] = arr0[p] with K_l = sqrt(p_d + 1)
+  acc = cfma(__ldg(&a.A[row * L.n + 2 * d]), cscale(sqrt((double)(p[d] + 1)), ldv(&a.Wv[(int64_t)f * L.nb + col])), acc);
+  if (p[d] > 0)
+    acc = cfma(__ldg(&a.A[row * L.n + 2 * d + 1]),
+               cscale(sqrt((double)p[d]), ldv(&a.Wv[slot_arr2(L, d) * PN + (int64_t)(f - L.st[d]) * L.nb + col])), acc);
+  for (int i = d + 1; i < L.M; ++i) {
+    if (p[i] == 0) continue;
+    const double s = sqrt((double)p[i]);
+    const int64_t o = (int64_t)(f - L.st[i]) * L.nb + col;
+    acc = cfma(__ldg(&a.A[row * L.n + 2 * i]), cscale(s, ldv(&a.Wv[slot_1001(L, d, i - d - 1) * PN + o])), acc);
+    acc = cfma(__ldg(&a.A[row * L.n + 2 * i + 1]), cscale(s, ldv(&a.Wv[slot_1010(L, d, i - d - 1) * PN + o])), acc);
+  }
+  const int k = row >> 1;
+  const int lift = (row & 1) == 0 && k == d;  // K_i[2d] = sqrt(p_d + 2)
+  return cdivs(acc, sqrt((double)(p[k] + lift + 1)));
+}
+
+// Item o of a point: o < 2M -> diagonal-pivot row o; else off-diagonal pivot d, local row r.
+// Returns false when the reference writes nothing for this item.
+__device__ __forceinline__ bool item_target(const DiagLat& L, const int32_t* p, int o, int& d, int& row, int64_t& slot,
+                                            int32_t& dst_f, int32_t f) {
+  if (o < L.n) {
+    const int i = o;
+    if (!(L.c[0] == 1 || p[0] < L.c[0] - 1)) return false;
+    if (!(p[i >> 1] + 1 < L.c[i >> 1] && (i != 1 || p[0] + 2 < L.c[0]))) return false;
+    d = -1;
+    row = i;
+    slot = slot_arr1(L, i);
+    dst_f = f;
+    return true;
+  }
+  d = (o - L.n) / L.n;
+  const int r = (o - L.n) % L.n;
+  for (int k = 0; k < d; ++k)
+    if (p[k] != 0) return false;
+  if (!(p[d] < L.c[d] - 1) || r >= L.n - 2 * d) return false;
+  if (r == 0) {
+    row = 2 * d + 1;
+    slot = 0;
+    dst_f = f + L.st[d];
+    return true;
+  }
+  dst_f = f;
+  if (r == 1) {
+    if (!(p[d] + 2 < L.c[d])) return false;
+    row = 2 * d;
+    slot = slot_arr2(L, d);
+    return true;
+  }
+  const int i = d + 1 + (r - 2) / 2;
+  if (!(p[i] + 1 < L.c[i])) return false;
+  row = 2 * i + ((r - 2) & 1);
+  slot = (row & 1) ? slot_1001(L, d, i - d - 1) : slot_1010(L, d, i - d - 1);
+  return true;
+}
+
+__global__ void __launch_bounds__(DG_BLOCK) diag_amps_kernel(DiagArgs a) {
+  const DiagLat& L = a.L;
+  const int per_point = L.n + L.M * L.n;
+  const int64_t PN = (int64_t)L.P * L.nb;
+  uint32_t epoch = 0;
+  for (int w = 0; w < L.W; ++w) {
+    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
+    const int64_t items = (int64_t)cnt * per_point * L.nb;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+      const int32_t col = (int32_t)(t % L.nb);
+      const int64_t r = t / L.nb;
+      const int o = (int)(r % per_point);
+      const int32_t f = a.sb.order[s0 + (int32_t)(r / per_point)];
+      int32_t p[DG_MAXM];
+      diag_weight(L, f, p);
+      int d, row;
+      int64_t slot;
+      int32_t dst;
+      if (!item_target(L, p, o, d, row, slot, dst, f)) continue;
+      double2 v;
+      if (d < 0) {
+        v = diag_row(a, p, f, row, col);
+      } else {
+        const double2 g = diag_row(a, p, f, 2 * d, col);
+        v = offdiag_row(a, p, f, d, row, g, col);
+      }
+      a.Wv[slot * PN + (int64_t)dst * L.nb + col] = v;
+    }
+    if (!step_barrier(a.h, epoch, a.budget)) return;
+  }
+}
+
+__global__ void diag_init_kernel(DiagArgs a) {
+  for (int32_t col = threadIdx.x; col < a.L.nb; col += blockDim.x) a.Wv[col] = a.G0[col];
+}
+
+// ------------------------------------------------------------------ 2. Jacobians
+// calc_dA_dB (diagonal_grad.py:17-41): for output row i with pivot value g, pivot
+// Jacobian Jp and inputs (K_l Gin_l, J_l):
+//   d/dA_pq = (Jp_pq B_i + sum_l K_l A_il J_l,pq + [p == i] K_q Gin_q) / K_i
+//   d/dB_r  = (Jp_r  B_i + [r == i] g + sum_l K_l A_il J_l,r) / K_i
+
+__device__ __forceinline__ double2 jac_diag_row(const DiagArgs& a, const int32_t* p, int32_t f, int i, int q) {
+  const DiagLat& L = a.L;
+  const int nc = L.n * L.n + L.n;
+  const int64_t P = L.P;
+  double2 acc = cmul(ldv(&a.J[(int64_t)f * nc + q]), __ldg(&a.B[i]));
+  const bool isA = q < L.n * L.n;
+  if (!isA && q - L.n * L.n == i) acc = cadd(acc, ldv(&a.Wv[f]));
+  for (int l = 0; l < L.n; ++l) {
+    const int k = l >> 1;
+    if (p[k] == 0) continue;
+    const int64_t src = slot_arr1(L, l ^ 1) * P + (f - L.st[k]);
+    const double s = sqrt((double)p[k]);
+    acc = cfma(cscale(s, __ldg(&a.A[i * L.n + l])), ldv(&a.J[src * nc + q]), acc);
+    if (isA && q == i * L.n + l) acc = cadd(acc, cscale(s, ldv(&a.Wv[src])));
+  }
+  return cdivs(acc, sqrt((double)(p[i >> 1] + 1)));
+}
+
+__device__ __forceinline__ double2 jac_offdiag_row(const DiagArgs& a, const int32_t* p, int32_t f, int d, int row,
+                                                   double2 Jp, int q) {
+  const DiagLat& L = a.L;
+  const int nc = L.n * L.n + L.n;
+  const int64_t P = L.P;
+  const bool isA = q < L.n * L.n;
+  double2 acc = cmul(Jp, __ldg(&a.B[row]));
+  if (!isA && q - L.n * L.n == row) acc = cadd(acc, ldv(&a.Wv[slot_arr1(L, 2 * d) * P + f]));
+  auto term = [&](int l, double s, int64_t src) {
+    acc = cfma(cscale(s, __ldg(&a.A[row * L.n + l])), ldv(&a.J[src * nc + q]), acc);
+    if (isA && q == row * L.n + l) acc = cadd(acc, cscale(s, ldv(&a.Wv[src])));
+  };
+  term(2 * d, sqrt((double)(p[d] + 1)), (int64_t)f);
+  if (p[d] > 0) term(2 * d + 1, sqrt((double)p[d]), slot_arr2(L, d) * P + (f - L.st[d]));
+  for (int i = d + 1; i < L.M; ++i) {
+    if (p[i] == 0) continue;
+    const double s = sqrt((double)p[i]);
+    term(2 * i, s, slot_1001(L, d, i - d - 1) * P + (f - L.st[i]));
+    term(2 * i + 1, s, slot_1010(L, d, i - d - 1) * P + (f - L.st[i]));
+  }
+  const int k = row >> 1;
+  const int lift = (row & 1) == 0 && k == d;
+  return cdivs(acc, sqrt((double)(p[k] + lift + 1)));
+}
+
+__global__ void __launch_bounds__(DG_BLOCK) diag_jacobian_kernel(DiagArgs a) {
+  const DiagLat& L = a.L;
+  const int per_point = L.n + L.M * L.n;
+  const int nc = L.n * L.n + L.n;
+  const int64_t P = L.P;
+  uint32_t epoch = 0;
+  for (int w = 0; w < L.W; ++w) {
+    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
+    const int64_t items = (int64_t)cnt * per_point * nc;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+      const int q = (int)(t % nc);
+      const int64_t r = t / nc;
+      const int o = (int)(r % per_point);
+      const int32_t f = a.sb.order[s0 + (int32_t)(r / per_point)];
+      int32_t p[DG_MAXM];
+      diag_weight(L, f, p);
+      int d, row;
+      int64_t slot;
+      int32_t dst;
+      if (!item_target(L, p, o, d, row, slot, dst, f)) continue;
+      double2 v;
+      if (d < 0) {
+        v = jac_diag_row(a, p, f, row, q);
+      } else {
+        const double2 Jp = jac_diag_row(a, p, f, 2 * d, q);
+        v = jac_offdiag_row(a, p, f, d, row, Jp, q);
+      }
+      a.J[(slot * P + dst) * nc + q] = v;
+    }
+    if (!step_barrier(a.h, epoch, a.budget)) return;
+  }
+}
+
+// dL/dA_pq = sum_k g_k J0_k,pq ; dL/dB_r = sum_k g_k J0_k,r ; dL/dG0 = sum_k g_k (arr0_k / G0)
+// (the contraction of hermite_renormalized_diagonal_jax_bwd, jax_vjps/hermite.py:292-329).
+// One CTA per output component, fixed-order reduction.
+__global__ void diag_vjp_kernel(DiagLat L, const double2* J, const double2* Wv, const double2* G0, const double2* g,
+                                double2* dA, double2* dB, double2* dG0) {
+  const int nc = L.n * L.n + L.n;
+  const int comp = blockIdx.x;  // 0..nc (nc = dG0)
+  double2 acc = cmk(0.0, 0.0);
+  const double2 c0 = __ldg(G0);
+  for (int32_t k = threadIdx.x; k < L.P; k += blockDim.x) {
+    const double2 gk = __ldg(&g[k]);
+    const double2 x = comp < nc ? __ldg(&J[(int64_t)k * nc + comp]) : cdiv_smith(__ldg(&Wv[k]), c0);
+    acc = cfma(gk, x, acc);
+  }
+  __shared__ double2 red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (comp < L.n * L.n)
+      dA[comp] = red[0];
+    else if (comp < nc)
+      dB[comp - L.n * L.n] = red[0];
+    else
+      *dG0 = red[0];
+  }
+}
+
+// ------------------------------------------------------------------ 3. fast_diagonal
+
+struct FdArgs {
+  FdLat F;
+  const double2* A;  // 2L x 2L, caller's order (all first copies, then all second copies)
+  const double2* b;
+  const double2* c;
+  int stable;
+  double2* Ap;       // permuted (interleaved) A, 2L x 2L (workspace)
+  double2* bp;       // permuted b (workspace)
+  double2* G;        // npts x q^2 (workspace)
+  double2* out;      // (pnr + 1 ..., q, q)
+  SortBufs sb;
+  WsHeader* h;
+  uint64_t budget;
+};
+
+__device__ __forceinline__ int32_t fd_zero_id(const FdLat& F) {
+  int32_t id = 0;
+  for (int j = 0; j < F.K; ++j) id += 2 * F.pst[j];
+  return id;
+}
+
+// One CTA: permute A and b (perm = [m, m + L], fast_diagonal.py:56-59) and fill the
+// first block, the (q, q) recurrence of mode 0 (vanilla_numba or stable_numba on
+// A[:2, :2], b[:2], c; vanilla/core.py:25-213), by anti-diagonals.
+__global__ void fd_init_kernel(FdArgs a) {
+  const FdLat& F = a.F;
+  const int Lm = F.K + 1, n = 2 * Lm, q = F.q;
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+    const int r = t / n, s = t % n;
+    const int pr = (r & 1) ? (r >> 1) + Lm : (r >> 1), ps = (s & 1) ? (s >> 1) + Lm : (s >> 1);
+    a.Ap[t] = a.A[pr * n + ps];
+  }
+  for (int r = threadIdx.x; r < n; r += blockDim.x) a.bp[r] = a.b[(r & 1) ? (r >> 1) + Lm : (r >> 1)];
+  __syncthreads();
+  double2* G = a.G + (int64_t)fd_zero_id(F) * q * q;
+  const double2 A00 = a.Ap[0], A01 = a.Ap[1], A10 = a.Ap[n], A11 = a.Ap[n + 1], b0 = a.bp[0], b1 = a.bp[1];
+  if (threadIdx.x == 0) G[0] = __ldg(a.c);
+  __syncthreads();
+  auto at = [&](int m, int k) -> double2 { return (m < 0 || k < 0) ? cmk(0.0, 0.0) : G[m * q + k]; };
+  for (int s = 1; s <= 2 * (q - 1); ++s) {
+    for (int m = max(0, s - (q - 1)) + (int)threadIdx.x; m <= min(s, q - 1); m += blockDim.x) {
+      const int k = s - m;
+      double2 v;
+      if (!a.stable) {
+        if (m == 0) {  // face: pivot on axis 1
+          double2 acc = cmul(b1, at(0, k - 1));
+          acc = cfma(cscale(sqrt((double)(k - 1 > 0 ? k - 1 : 0)), A11), at(0, k - 2), acc);
+          v = cdivs(acc, sqrt((double)k));
+        } else {  // bulk: pivot on axis 0
+          double2 acc = cmul(b0, at(m - 1, k));
+          acc = cfma(cscale(sqrt((double)(m - 1)), A00), at(m - 2, k), acc);
+          acc = cfma(cscale(sqrt((double)k), A01), at(m - 1, k - 1), acc);
+          v = cdivs(acc, sqrt((double)m));
+        }
+      } else {  // average over the pivots with k_i > 0
+        double2 vals = cmk(0.0, 0.0);
+        int npiv = 0;
+        if (m > 0) {
+          double2 acc = cmul(b0, at(m - 1, k));
+          acc = cfma(cscale(sqrt((double)(m - 1)), A00), at(m - 2, k), acc);
+          acc = cfma(cscale(sqrt((double)k), A01), at(m - 1, k - 1), acc);
+          vals = cadd(vals, cdivs(acc, sqrt((double)m)));
+          ++npiv;
+        }
+        if (k > 0) {
+          double2 acc = cmul(b1, at(m, k - 1));
+          acc = cfma(cscale(sqrt((double)m), A10), at(m - 1, k - 1), acc);
+          acc = cfma(cscale(sqrt((double)(k - 1)), A11), at(m, k - 2), acc);
+          vals = cadd(vals, cdivs(acc, sqrt((double)k)));
+          ++npiv;
+        }
+        v = cdivs(vals, (double)npiv);
+      }
+      G[m * q + k] = v;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < q * q; t += blockDim.x) a.out[t] = G[t];
+}
+
+__global__ void __launch_bounds__(DG_BLOCK) fd_kernel(FdArgs a) {
+  const FdLat& F = a.F;
+  const int q = F.q, qq = q * q, n = 2 * (F.K + 1);
+  uint32_t epoch = 0;
+  const int wlast = min(F.W - 1, F.wend - 1);
+  for (int w = 1; w <= wlast; ++w) {
+    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
+    const int64_t items = (int64_t)cnt * qq;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+      const int e = (int)(t % qq);
+      const int32_t id = a.sb.order[s0 + (int32_t)(t / qq)];
+      const int m = e / q, kk = e % q;
+      int32_t k[2 * FD_MAXK];
+      fd_decode(F, id, k);
+      // get_pivot (fast_diagonal.py:80-99)
+      int mbest = 0, dbest = -1;
+      for (int j = 0; j < F.K; ++j) {
+        const int dl = abs(k[2 * j] - k[2 * j + 1]);
+        if (dl > dbest) {
+          dbest = dl;
+          mbest = j;
+        }
+      }
+      int i;
+      if (dbest == 0) {
+        i = 0;
+        for (int j = 1; j < 2 * F.K; ++j)
+          if (k[j] > k[i]) i = j;
+      } else {
+        i = k[2 * mbest] > k[2 * mbest + 1] ? 2 * mbest : 2 * mbest + 1;
+      }
+      // pivot id: lowering a (even coordinate) moves the pair state by -6, lowering b by +1
+      const int32_t pid = id + ((i & 1) ? 1 : -6) * F.pst[i >> 1];
+      k[i] -= 1;  // k is now the pivot's coordinates
+      const double2* mat = a.G + (int64_t)pid * qq;
+      const double2* Arow = a.Ap + (i + 2) * n;
+      // single_step (fast_diagonal.py:102-124)
+      double2 acc = cmul(a.bp[i + 2], ldv(&mat[e]));
+      if (m > 0) acc = cfma(cscale(sqrt((double)m), Arow[0]), ldv(&mat[e - q]), acc);
+      if (kk > 0) acc = cfma(cscale(sqrt((double)kk), Arow[1]), ldv(&mat[e - 1]), acc);
+      for (int j = 0; j < 2 * F.K; ++j) {
+        if (k[j] <= 0) continue;
+        const int32_t lid = pid + ((j & 1) ? 1 : -6) * F.pst[j >> 1];
+        acc = cfma(cscale(sqrt((double)k[j]), Arow[j + 2]), ldv(&a.G[(int64_t)lid * qq + e]), acc);
+      }
+      const double2 v = cdivs(acc, sqrt((double)(k[i] + 1)));
+      a.G[(int64_t)id * qq + e] = v;
+      k[i] += 1;
+      bool diag = true;
+      int32_t o = 0;
+      for (int j = 0; j < F.K; ++j) {
+        diag &= k[2 * j] == k[2 * j + 1];
+        o += k[2 * j] * F.ost[j];
+      }
+      if (diag) a.out[(int64_t)o * qq + e] = v;
+    }
+    if (!step_barrier(a.h, epoch, a.budget)) return;
+  }
+}
+
+// ------------------------------------------------------------------ host planning
+
+#ifndef MM_HOST_EMULATION
+struct DevCfg {
+  int sms = 0;
+  int occ = 0;
+};
+
+template <class K>
+int dev_cfg(K kernel, DevCfg& dc) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return MM_ERR_NO_DEVICE;
+  if (cudaDeviceGetAttribute(&dc.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MM_ERR_CUDA;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dc.occ, kernel, DG_BLOCK, 0) != cudaSuccess) return MM_ERR_CUDA;
+  if (dc.occ < 1) return MM_ERR_UNSUPPORTED;
+  return MM_OK;
+}
+
+#endif
+
+int diag_lat(int M, const int64_t* cutoffs, int64_t nb, DiagLat& L) {
+  if (M < 1 || cutoffs == nullptr || nb < 1) return MM_ERR_INVALID_ARG;
+  if (M > DG_MAXM) return MM_ERR_UNSUPPORTED;
+  memset(&L, 0, sizeof(L));
+  L.M = M;
+  L.n = 2 * M;
+  int64_t P = 1, W = 1;
+  for (int k = M - 1; k >= 0; --k) {
+    if (cutoffs[k] < 1) return MM_ERR_INVALID_ARG;
+    if (cutoffs[k] > 99999) return MM_ERR_TOO_LARGE;
+    L.c[k] = (int32_t)cutoffs[k];
+    L.st[k] = (int32_t)P;
+    P *= cutoffs[k];
+    W += cutoffs[k] - 1;
+    if (P * nb * diag_slots(M) > ((int64_t)1 << 40) || P > INT32_MAX / 64) return MM_ERR_TOO_LARGE;
+  }
+  if (W > kMaxWeights || nb > INT32_MAX) return MM_ERR_TOO_LARGE;
+  L.P = (int32_t)P;
+  L.nb = (int32_t)nb;
+  L.W = (int32_t)W;
+  return MM_OK;
+}
+
+// points per weight: coefficients of prod_k (1 + x + ... + x^{c_k - 1})
+std::vector<int64_t> diag_counts(const DiagLat& L) {
+  std::vector<int64_t> cnt(1, 1);
+  for (int k = 0; k < L.M; ++k) {
+    std::vector<int64_t> nx(cnt.size() + L.c[k] - 1, 0);
+    for (size_t s = 0; s < cnt.size(); ++s)
+      for (int v = 0; v < L.c[k]; ++v) nx[s + v] += cnt[s];
+    cnt.swap(nx);
+  }
+  return cnt;
+}
+
+struct DiagWs {
+  size_t header, count, start, cursor, order, total;
+};
+DiagWs diag_ws(int32_t W, int32_t npts) {
+  DiagWs w;
+  w.header = 0;
+  w.count = al(sizeof(WsHeader));
+  w.start = w.count + al((size_t)W * sizeof(int32_t));
+  w.cursor = w.start + al((size_t)(W + 1) * sizeof(int32_t));
+  w.order = w.cursor + al((size_t)W * sizeof(int32_t));
+  w.total = w.order + al((size_t)npts * sizeof(int32_t));
+  return w;
+}
+SortBufs sort_bufs(char* ws, const DiagWs& w) {
+  SortBufs sb;
+  sb.count = reinterpret_cast<int32_t*>(ws + w.count);
+  sb.start = reinterpret_cast<int32_t*>(ws + w.start);
+  sb.cursor = reinterpret_cast<int32_t*>(ws + w.cursor);
+  sb.order = reinterpret_cast<int32_t*>(ws + w.order);
+  return sb;
+}
+
+#ifndef MM_HOST_EMULATION
+int check_ws(void* ws, size_t ws_bytes, size_t need) {
+  if (ws == nullptr || ((uintptr_t)ws % kWsAlign) != 0 || ws_bytes < need) return MM_ERR_WORKSPACE;
+  return MM_OK;
+}
+
+int launch_wavefront(void* kern, void* arg, int64_t max_items, int sms, int occ, cudaStream_t st) {
+  const int64_t cap = (int64_t)sms * occ;
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((max_items + DG_BLOCK - 1) / DG_BLOCK, cap));
+  void* args[] = {arg};
+  if (cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(DG_BLOCK), args, 0, st) != cudaSuccess) return MM_ERR_CUDA;
+  note_launches(1);
+  return MM_OK;
+}
+
+#endif
+
+int fd_lat(int Lm, const int64_t* pnr, int64_t oc, FdLat& F) {
+  if (Lm < 2 || pnr == nullptr || oc < 0) return Lm == 1 ? MM_ERR_UNSUPPORTED : MM_ERR_INVALID_ARG;
+  if (Lm - 1 > FD_MAXK) return MM_ERR_UNSUPPORTED;
+  if (oc > 4096) return MM_ERR_TOO_LARGE;
+  memset(&F, 0, sizeof(F));
+  F.K = Lm - 1;
+  F.q = (int)(oc + 1);
+  int64_t npts = 1, nout = 1, sum = 0;
+  for (int j = F.K - 1; j >= 0; --j) {
+    if (pnr[j] < 0) return MM_ERR_INVALID_ARG;
+    if (pnr[j] > 9999) return MM_ERR_TOO_LARGE;  // the reference's sqrt table (fast_diagonal.py:29)
+    F.pnr[j] = (int32_t)pnr[j];
+    F.rad[j] = (int32_t)(5 * (pnr[j] + 1));
+    F.pst[j] = (int32_t)npts;
+    F.ost[j] = (int32_t)nout;
+    npts *= F.rad[j];
+    nout *= pnr[j] + 1;
+    sum += pnr[j];
+    if (npts > INT32_MAX / 8 || npts * F.q * F.q > ((int64_t)1 << 36)) return MM_ERR_TOO_LARGE;
+  }
+  F.npts = (int32_t)npts;
+  F.W = (int32_t)(2 * sum + 1);
+  F.wend = (int32_t)std::max<int64_t>(1, std::min<int64_t>(2 * oc + 2 * sum - Lm, (int64_t)F.W));
+  return MM_OK;
+}
+
+// lattice points per weight: per pair, states by a + b split into |a-b| < 2 and |a-b| = 2;
+// the product keeps at most one pair at distance 2
+std::vector<int64_t> fd_counts(const FdLat& F) {
+  std::vector<int64_t> c0(1, 1), c1(1, 0);  // no pair at distance 2 / exactly one
+  for (int j = 0; j < F.K; ++j) {
+    const int p = F.pnr[j];
+    std::vector<int64_t> s0(2 * p + 1, 0), s2(2 * p + 1, 0);
+    for (int a = 0; a <= p; ++a)
+      for (int b = std::max(0, a - 2); b <= std::min(p, a + 2); ++b) (std::abs(a - b) == 2 ? s2 : s0)[a + b] += 1;
+    std::vector<int64_t> n0(c0.size() + 2 * p, 0), n1(c0.size() + 2 * p, 0);
+    for (size_t s = 0; s < c0.size(); ++s)
+      for (int v = 0; v <= 2 * p; ++v) {
+        n0[s + v] += c0[s] * s0[v];
+        n1[s + v] += c1[s] * s0[v] + c0[s] * s2[v];
+      }
+    c0.swap(n0);
+    c1.swap(n1);
+  }
+  for (size_t s = 0; s < c0.size(); ++s) c0[s] += c1[s];
+  return c0;
+}
+
+struct FdWs {
+  DiagWs base;
+  size_t ap, g, total;
+};
+FdWs fd_ws(const FdLat& F) {
+  FdWs w;
+  w.base = diag_ws(F.W, F.npts);
+  const int n = 2 * (F.K + 1);
+  w.ap = w.base.total;
+  w.g = w.ap + al((size_t)(n * n + n) * sizeof(double2));
+  w.total = w.g + al((size_t)F.npts * F.q * F.q * sizeof(double2));
+  return w;
+}
+
+}  // namespace
+
+#ifndef MM_HOST_EMULATION
+// =================================================================== C ABI
+
+MM_API int64_t mm_diagonal_slots(int M) { return M < 1 ? 0 : diag_slots(M); }
+
+MM_API size_t mm_diagonal_workspace_bytes(int M, const int64_t* cutoffs, int64_t nb) {
+  DiagLat L;
+  if (diag_lat(M, cutoffs, nb, L)) return 0;
+  return diag_ws(L.W, L.P).total;
+}
+
+MM_API int mm_diagonal_amps(int M, const int64_t* cutoffs, int64_t nb, const mm_c128* A, const mm_c128* B,
+                            const mm_c128* G0, mm_c128* W, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  DiagLat L;
+  int rc = diag_lat(M, cutoffs, nb, L);
+  if (rc) return rc;
+  if (!A || !B || !G0 || !W) return MM_ERR_INVALID_ARG;
+  const DiagWs lay = diag_ws(L.W, L.P);
+  if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  DevCfg dc;
+  if ((rc = dev_cfg(diag_amps_kernel, dc))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  DiagArgs a;
+  memset(&a, 0, sizeof(a));
+  a.L = L;
+  a.A = (const double2*)A;
+  a.B = (const double2*)B;
+  a.G0 = (const double2*)G0;
+  a.Wv = (double2*)W;
+  a.sb = sort_bufs(w, lay);
+  a.h = reinterpret_cast<WsHeader*>(w);
+  a.budget = budget_ns();
+  if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
+  if (cudaMemsetAsync(W, 0, (size_t)diag_slots(M) * L.P * L.nb * sizeof(double2), st) != cudaSuccess)
+    return MM_ERR_CUDA;
+  if ((rc = launch_sort(L, L.P, L.W, a.sb, dc.sms, st))) return rc;
+  diag_init_kernel<<<1, 128, 0, st>>>(a);
+  note_launches(1);
+  if ((rc = cuda_status())) return rc;
+  const std::vector<int64_t> cnt = diag_counts(L);
+  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * (L.n + L.M * L.n) * L.nb;
+  return launch_wavefront((void*)diag_amps_kernel, &a, max_items, dc.sms, dc.occ, st);
+}
+
+MM_API int mm_diagonal_jacobian(int M, const int64_t* cutoffs, const mm_c128* A, const mm_c128* B, const mm_c128* W,
+                                mm_c128* J, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  DiagLat L;
+  int rc = diag_lat(M, cutoffs, 1, L);
+  if (rc) return rc;
+  if (!A || !B || !W || !J) return MM_ERR_INVALID_ARG;
+  const int64_t nc = (int64_t)L.n * L.n + L.n;
+  if ((int64_t)L.P * nc * diag_slots(M) > ((int64_t)1 << 36)) return MM_ERR_TOO_LARGE;
+  const DiagWs lay = diag_ws(L.W, L.P);
+  if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  DevCfg dc;
+  if ((rc = dev_cfg(diag_jacobian_kernel, dc))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  DiagArgs a;
+  memset(&a, 0, sizeof(a));
+  a.L = L;
+  a.A = (const double2*)A;
+  a.B = (const double2*)B;
+  a.Wv = (double2*)W;
+  a.J = (double2*)J;
+  a.sb = sort_bufs(w, lay);
+  a.h = reinterpret_cast<WsHeader*>(w);
+  a.budget = budget_ns();
+  if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
+  if (cudaMemsetAsync(J, 0, (size_t)diag_slots(M) * L.P * nc * sizeof(double2), st) != cudaSuccess) return MM_ERR_CUDA;
+  if ((rc = launch_sort(L, L.P, L.W, a.sb, dc.sms, st))) return rc;
+  const std::vector<int64_t> cnt = diag_counts(L);
+  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * (L.n + L.M * L.n) * nc;
+  return launch_wavefront((void*)diag_jacobian_kernel, &a, max_items, dc.sms, dc.occ, st);
+}
+
+MM_API int mm_diagonal_vjp(int M, const int64_t* cutoffs, const mm_c128* J, const mm_c128* W, const mm_c128* G0,
+                           const mm_c128* g, mm_c128* dA, mm_c128* dB, mm_c128* dG0, mm_stream_t stream) {
+  DiagLat L;
+  int rc = diag_lat(M, cutoffs, 1, L);
+  if (rc) return rc;
+  if (!J || !W || !G0 || !g || !dA || !dB || !dG0) return MM_ERR_INVALID_ARG;
+  const int nc = L.n * L.n + L.n;
+  diag_vjp_kernel<<<nc + 1, 256, 0, (cudaStream_t)stream>>>(L, (const double2*)J, (const double2*)W,
+                                                            (const double2*)G0, (const double2*)g, (double2*)dA,
+                                                            (double2*)dB, (double2*)dG0);
+  note_launches(1);
+  return cuda_status();
+}
+
+MM_API size_t mm_fast_diagonal_workspace_bytes(int L, const int64_t* pnr_cutoffs, int64_t output_cutoff) {
+  FdLat F;
+  if (fd_lat(L, pnr_cutoffs, output_cutoff, F)) return 0;
+  return fd_ws(F).total;
+}
+
+MM_API int mm_fast_diagonal(int L, const int64_t* pnr_cutoffs, int64_t output_cutoff, const mm_c128* A,
+                            const mm_c128* b, const mm_c128* c, int stable, mm_c128* out, void* ws, size_t ws_bytes,
+                            mm_stream_t stream) {
+  FdLat F;
+  int rc = fd_lat(L, pnr_cutoffs, output_cutoff, F);
+  if (rc) return rc;
+  if (!A || !b || !c || !out) return MM_ERR_INVALID_ARG;
+  const FdWs lay = fd_ws(F);
+  if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  DevCfg dc;
+  if ((rc = dev_cfg(fd_kernel, dc))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  FdArgs a;
+  memset(&a, 0, sizeof(a));
+  a.F = F;
+  a.A = (const double2*)A;
+  a.b = (const double2*)b;
+  a.c = (const double2*)c;
+  a.stable = stable ? 1 : 0;
+  const int n = 2 * L;
+  a.Ap = reinterpret_cast<double2*>(w + lay.ap);
+  a.bp = a.Ap + n * n;
+  a.G = reinterpret_cast<double2*>(w + lay.g);
+  a.out = (double2*)out;
+  a.sb = sort_bufs(w, lay.base);
+  a.h = reinterpret_cast<WsHeader*>(w);
+  a.budget = budget_ns();
+  int64_t nout = (int64_t)F.q * F.q;
+  for (int j = 0; j < F.K; ++j) nout *= F.pnr[j] + 1;
+  if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
+  if (cudaMemsetAsync(out, 0, (size_t)nout * sizeof(double2), st) != cudaSuccess) return MM_ERR_CUDA;
+  if ((rc = launch_sort(F, F.npts, F.W, a.sb, dc.sms, st))) return rc;
+  fd_init_kernel<<<1, 256, 0, st>>>(a);
+  note_launches(1);
+  if ((rc = cuda_status())) return rc;
+  const std::vector<int64_t> cnt = fd_counts(F);
+  int64_t mx = 1;
+  for (int wgt = 1; wgt < (int)cnt.size() && wgt < F.wend; ++wgt) mx = std::max(mx, cnt[wgt]);
+  return launch_wavefront((void*)fd_kernel, &a, mx * F.q * F.q, dc.sms, dc.occ, st);
+}
+#endif  // MM_HOST_EMULATION
