@@ -447,6 +447,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     extras["autoshape"] = run_autoshape(dev, time_eager, As, bs,
                                         with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
     extras["binomial"] = run_binomial(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
+    extras["diagonal"] = run_diagonal(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
 
     extras["fock_contraction"] = run_contraction(dev, time_eager)
     return e2e_ms, h2d, d2h, plain_value, cpu, extras
@@ -550,6 +551,103 @@ def run_binomial(dev, time_eager, with_cpu=True):
                                "sample": f"the same fill, one pass, {tc * 1e3:.1f} ms",
                                "stop_weight": stop, "max_rel_err_vs_gpu": float(np.abs(Gh - ref).max() / np.abs(ref).max())}
     return out
+
+
+def _pnr_triple(M, seed, r_max=0.6, t_max=0.3, beta=0.4):
+    """conj(-A), conj(b), c of a mixed M-mode Gaussian state in Bargmann order (bra modes, then ket
+    modes): A = [[conj(K), C^T], [C, K]], K = U diag(tanh r) U^T, C = V diag(t) V^dagger."""
+    from scipy.stats import unitary_group
+
+    rng = np.random.default_rng(seed)
+    U = unitary_group.rvs(M, random_state=rng)
+    V = unitary_group.rvs(M, random_state=rng)
+    K = (U * np.tanh(rng.uniform(0.05, r_max, M))) @ U.T
+    Cm = (V * rng.uniform(0.0, t_max, M)) @ V.conj().T
+    A = np.block([[K.conj(), Cm.T], [Cm, K]])
+    bk = beta * (rng.standard_normal(M) + 1j * rng.standard_normal(M))
+    return np.conj(-A), np.conj(np.concatenate([bk.conj(), bk])), np.complex128(0.7)
+
+
+def run_diagonal(dev, time_eager, with_cpu=True):
+    """Diagonal strategies on mixed Gaussian states: PNR amplitudes of 4 modes at cutoff 12 (20,736
+    lattice points), of 3 modes at cutoff 10 with 64 B vectors, their Jacobians (3 modes at cutoff 8),
+    and fast_diagonal of 3 modes (output cutoff 20, PNR cutoffs 10, 10) and 4 modes (10; 6, 6, 6).
+    GPU time per call (device tensors in and out, Python included) against the C oracle on one core
+    (the reference runs these single-threaded), with every output checked against the oracle."""
+    import torch
+
+    import mrmustard_gb300 as mm
+
+    def ilv(A, b):
+        o = np.arange(A.shape[0]).reshape(2, -1).T.flatten()
+        return A[o][:, o], b[o]
+
+    def td(x):
+        return torch.as_tensor(x, device=dev)
+
+    res = {}
+    cases = (("pnr_4x12", 4, (12,) * 4, 1), ("pnr_3x10_b64", 3, (10,) * 3, 64))
+    for name, M, cut, nb in cases:
+        A, b, c = _pnr_triple(M, 600 + M)
+        Ai, bi = ilv(A, b)
+        B = bi if nb == 1 else bi[:, None] * np.linspace(0.5, 1.5, nb)[None, :]
+        At, Bt, ct = td(Ai), td(B), td(c)
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            t = time_eager(lambda: mm.hermite_multidimensional_diagonal(At, Bt, ct, cut), reps=10)
+        got = mm.hermite_multidimensional_diagonal(At, Bt, ct, cut)
+        P = int(np.prod(cut))
+        r = {"modes": M, "cutoffs": list(cut), "batch": nb, "points": P, "ms": t, "points_per_s": P * nb / (t * 1e-3)}
+        if with_cpu:
+            import oracle
+
+            t0 = time.perf_counter()
+            ref = oracle.diagonal_amps(Ai, B, c, cut)
+            tc = time.perf_counter() - t0
+            err = max(oracle.rel_err(x.cpu().numpy(), y) for x, y in zip(got, ref))
+            r["cpu_baseline"] = {"value": P * nb / tc, "unit": "points/s", "cores": 1, "kind": "port",
+                                 "sample": f"the same call, one pass, {tc * 1e3:.1f} ms", "max_rel_err_vs_gpu": err}
+        res[name] = r
+    # Jacobians
+    M, cut = 3, (8, 8, 8)
+    A, b, c = _pnr_triple(M, 700)
+    Ai, bi = ilv(A, b)
+    At, bt, ct = td(Ai), td(bi), td(c)
+    arrs = mm.hermite_multidimensional_diagonal(At, bt, ct, cut)
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        t = time_eager(lambda: mm.grad_hermite_multidimensional_diagonal(At, bt, ct, *arrs), reps=10)
+    got = mm.grad_hermite_multidimensional_diagonal(At, bt, ct, *arrs)
+    P = int(np.prod(cut))
+    r = {"modes": M, "cutoffs": list(cut), "points": P, "jacobian_entries": P * (4 * M * M + 2 * M), "ms": t}
+    if with_cpu:
+        import oracle
+
+        t0 = time.perf_counter()
+        ref = oracle.diagonal_grad(Ai, bi, c, cut)
+        tc = time.perf_counter() - t0
+        r["cpu_baseline"] = {"value": P / tc, "unit": "points/s", "cores": 1, "kind": "port",
+                             "sample": f"amplitudes and Jacobians, one pass, {tc * 1e3:.1f} ms",
+                             "max_rel_err_vs_gpu": max(oracle.rel_err(x.cpu().numpy(), y) for x, y in zip(got, ref))}
+    res["jacobian_3x8"] = r
+    # fast_diagonal
+    for name, L, oc, pnr in (("leftover_3_oc20_pnr10x10", 3, 20, (10, 10)), ("leftover_4_oc10_pnr6x6x6", 4, 10, (6, 6, 6))):
+        A, b, c = _pnr_triple(L, 800 + L)
+        At, bt, ct = td(A), td(b), td(c)
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            t = time_eager(lambda: mm.fast_diagonal(At, bt, ct, oc, pnr), reps=10)
+        got = mm.fast_diagonal(At, bt, ct, oc, pnr)
+        nout = int(np.prod([p + 1 for p in pnr])) * (oc + 1) ** 2
+        r = {"modes": L, "output_cutoff": oc, "pnr_cutoffs": list(pnr), "output_amplitudes": nout, "ms": t}
+        if with_cpu:
+            import oracle
+
+            t0 = time.perf_counter()
+            ref = oracle.fast_diagonal(A, b, c, oc, pnr)
+            tc = time.perf_counter() - t0
+            r["cpu_baseline"] = {"value": nout / tc, "unit": "output amplitudes/s", "cores": 1, "kind": "port",
+                                 "sample": f"the same call, one pass, {tc * 1e3:.1f} ms",
+                                 "max_rel_err_vs_gpu": oracle.rel_err(got.cpu().numpy(), ref)}
+        res[name] = r
+    return res
 
 
 def run_single(dev, time_eager, dfma_peak=None):
@@ -656,6 +754,8 @@ def main(argv=None):
                     help="run only the Fock-contraction leg (gate tensor on 256 kets) and print its figures")
     ap.add_argument("--only-binomial", action="store_true",
                     help="run only the binomial fill of a 4-mode state at cutoff 30 (GPU and CPU oracle)")
+    ap.add_argument("--only-diagonal", action="store_true",
+                    help="run only the diagonal strategies (PNR amplitudes, Jacobians, fast_diagonal; GPU and CPU oracle)")
     ap.add_argument("--only-autoshape", action="store_true",
                     help="run only autoshape over the workload's states (GPU and CPU oracle)")
     ap.add_argument("--only-single", action="store_true",
@@ -665,7 +765,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()
-    if args.only_contraction or args.only_single or args.only_autoshape or args.only_binomial:
+    if args.only_contraction or args.only_single or args.only_autoshape or args.only_binomial or args.only_diagonal:
         import torch
 
         dev = torch.device("cuda", local_rank)
@@ -682,7 +782,9 @@ def main(argv=None):
             torch.cuda.synchronize()
             return e0.elapsed_time(e1) / reps
 
-        if args.only_binomial:
+        if args.only_diagonal:
+            print(json.dumps({"diagonal": run_diagonal(dev, time_eager, not args.skip_cpu)}), flush=True)
+        elif args.only_binomial:
             print(json.dumps({"binomial": run_binomial(dev, time_eager, not args.skip_cpu)}), flush=True)
         elif args.only_autoshape:
             _, As, bs, _ = make_workload(20260000, args.instances)

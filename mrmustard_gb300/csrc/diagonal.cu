@@ -194,6 +194,55 @@ __device__ __forceinline__ bool step_barrier(WsHeader* h, uint32_t& epoch, uint6
   return grid_barrier(h, ++epoch, budget, 0);
 }
 
+// ------------------------------------------------------------------ square-root tables
+// sq[k] = sqrt(k) (correctly rounded, as the reference's SQRT tables) and rs[k] = 1/sqrt(k),
+// filled once per call: FP64 square roots and divisions are multi-instruction FP64
+// sequences, far too costly to repeat per amplitude on this part.
+struct Tabs {
+  const double* sq;
+  const double* rs;
+};
+
+// Per-CTA copies of the read-only operands of a wavefront kernel: the square-root tables
+// (when they fit) and the 2M x 2M matrix, so that the per-item reads are shared-memory hits.
+constexpr int kSmemTab = 1024;
+constexpr int kSmemA = 16 * 16;
+struct StageSmem {
+  double sq[kSmemTab];
+  double rs[kSmemTab];
+  double2 A[kSmemA];
+  double2 b[16];
+};
+
+// Copies tables (first ntab entries) and the n x n matrix A (and the n-vector b when given)
+// into shared memory; returns the staged views.
+__device__ __forceinline__ void stage_operands(StageSmem& sm, Tabs& t, int32_t ntab, const double2*& A, int n,
+                                               const double2** b) {
+  if (ntab <= kSmemTab) {
+    for (int k = threadIdx.x; k < ntab; k += blockDim.x) {
+      sm.sq[k] = t.sq[k];
+      sm.rs[k] = t.rs[k];
+    }
+    t.sq = sm.sq;
+    t.rs = sm.rs;
+  }
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) sm.A[k] = A[k];
+  A = sm.A;
+  if (b) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sm.b[k] = (*b)[k];
+    *b = sm.b;
+  }
+  __syncthreads();
+}
+
+__global__ void sqrt_table_kernel(double* sq, double* rs, int32_t n) {
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const double s = sqrt((double)k);
+    sq[k] = s;
+    rs[k] = k > 0 ? 1.0 / s : 0.0;
+  }
+}
+
 // ------------------------------------------------------------------ 1. diagonal amplitudes
 
 struct DiagArgs {
@@ -203,79 +252,91 @@ struct DiagArgs {
   const double2* G0;  // nb
   double2* Wv;        // slots x P x nb
   double2* J;         // Jacobians: slots x P x (4M^2 + 2M) (Jacobian kernel only)
+  Tabs t;
+  int32_t ntab;
   SortBufs sb;
   WsHeader* h;
   uint64_t budget;
 };
 
 __device__ __forceinline__ double2 ldv(const double2* p) { return __ldcg(p); }
-__device__ __forceinline__ double2 cdivs(double2 a, double s) { return cmk(a.x / s, a.y / s); }
+
+template <int M>
+__device__ __forceinline__ void decode_params(const DiagLat& L, int32_t f, int32_t* p) {
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    p[k] = f / L.st[k];
+    f -= p[k] * L.st[k];
+  }
+}
 
 // Row i of the diagonal pivot at point f (diagonal_amps.py:92-137):
 // (arr0[p] B_i + sum_l A_il sqrt(p_{l/2}) arr1[l^1][p - 1_{l/2}]) / sqrt(p_{i/2} + 1).
+template <int M>
 __device__ __forceinline__ double2 diag_row(const DiagArgs& a, const int32_t* p, int32_t f, int i, int32_t col) {
+  constexpr int n = 2 * M;
   const DiagLat& L = a.L;
   const int64_t PN = (int64_t)L.P * L.nb;
-  double2 acc = cmul(ldv(&a.Wv[(int64_t)f * L.nb + col]), __ldg(&a.B[(int64_t)i * L.nb + col]));
-  for (int l = 0; l < L.n; ++l) {
+  double2 gin[n];
+#pragma unroll
+  for (int l = 0; l < n; ++l) {
     const int k = l >> 1;
-    if (p[k] == 0) continue;
-    const double2 g = ldv(&a.Wv[slot_arr1(L, l ^ 1) * PN + (int64_t)(f - L.st[k]) * L.nb + col]);
-    acc = cfma(__ldg(&a.A[i * L.n + l]), cscale(sqrt((double)p[k]), g), acc);
+    gin[l] = p[k] > 0 ? ldv(&a.Wv[slot_arr1(L, l ^ 1) * PN + (int64_t)(f - L.st[k]) * L.nb + col]) : cmk(0.0, 0.0);
   }
-  return cdivs(acc, sqrt((double)(p[i >> 1] + 1)));
+  double2 acc = cmul(ldv(&a.Wv[(int64_t)f * L.nb + col]), __ldg(&a.B[(int64_t)i * L.nb + col]));
+#pragma unroll
+  for (int l = 0; l < n; ++l) acc = cfma(a.A[i * n + l], cscale(a.t.sq[p[l >> 1]], gin[l]), acc);
+  return cscale(a.t.rs[p[i >> 1] + 1], acc);
 }
 
 // Output row `row` of the off-diagonal pivot d at point f (diagonal_amps.py:17-89),
 // with g = arr1[2d][f] (the diagonal pivot's row 2d at the same point).
+template <int M>
 __device__ __forceinline__ double2 offdiag_row(const DiagArgs& a, const int32_t* p, int32_t f, int d, int row,
                                                double2 g, int32_t col) {
+  constexpr int n = 2 * M;
   const DiagLat& L = a.L;
   const int64_t PN = (int64_t)L.P * L.nb;
-  double2 acc = cmul(g, __ldg(&a.B[(int64_t)row * L.nb + col]));
-  // G_in[2d] = arr0[p] with K_l = sqrt(p_d + 1)
-  acc = cfma(__ldg(&a.A[row * L.n + 2 * d]), cscale(sqrt((double)(p[d] + 1)), ldv(&a.Wv[(int64_t)f * L.nb + col])), acc);
-  if (p[d] > 0)
-    acc = cfma(__ldg(&a.A[row * L.n + 2 * d + 1]),
-               cscale(sqrt((double)p[d]), ldv(&a.Wv[slot_arr2(L, d) * PN + (int64_t)(f - L.st[d]) * L.nb + col])), acc);
-  for (int i = d + 1; i < L.M; ++i) {
-    if (p[i] == 0) continue;
-    const double s = sqrt((double)p[i]);
-    const int64_t o = (int64_t)(f - L.st[i]) * L.nb + col;
-    acc = cfma(__ldg(&a.A[row * L.n + 2 * i]), cscale(s, ldv(&a.Wv[slot_1001(L, d, i - d - 1) * PN + o])), acc);
-    acc = cfma(__ldg(&a.A[row * L.n + 2 * i + 1]), cscale(s, ldv(&a.Wv[slot_1010(L, d, i - d - 1) * PN + o])), acc);
+  double2 gin[n];
+  double kl[n];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    gin[2 * i] = cmk(0.0, 0.0);
+    gin[2 * i + 1] = cmk(0.0, 0.0);
+    kl[2 * i] = a.t.sq[p[i]];
+    kl[2 * i + 1] = kl[2 * i];
+    if (i < d) continue;
+    if (i == d) {  // G_in[2d] = arr0[p] with K_l = sqrt(p_d + 1); G_in[2d+1] = arr2[d][p - 1_d]
+      kl[2 * i] = a.t.sq[p[i] + 1];
+      gin[2 * i] = ldv(&a.Wv[(int64_t)f * L.nb + col]);
+      if (p[i] > 0) gin[2 * i + 1] = ldv(&a.Wv[slot_arr2(L, d) * PN + (int64_t)(f - L.st[i]) * L.nb + col]);
+    } else if (p[i] > 0) {
+      const int64_t o = (int64_t)(f - L.st[i]) * L.nb + col;
+      gin[2 * i] = ldv(&a.Wv[slot_1001(L, d, i - d - 1) * PN + o]);
+      gin[2 * i + 1] = ldv(&a.Wv[slot_1010(L, d, i - d - 1) * PN + o]);
+    }
   }
+  double2 acc = cmul(g, __ldg(&a.B[(int64_t)row * L.nb + col]));
+#pragma unroll
+  for (int l = 0; l < n; ++l)
+    if ((l >> 1) >= d) acc = cfma(a.A[row * n + l], cscale(kl[l], gin[l]), acc);
   const int k = row >> 1;
   const int lift = (row & 1) == 0 && k == d;  // K_i[2d] = sqrt(p_d + 2)
-  return cdivs(acc, sqrt((double)(p[k] + lift + 1)));
+  return cscale(a.t.rs[p[k] + lift + 1], acc);
 }
 
-// Item o of a point: o < 2M -> diagonal-pivot row o; else off-diagonal pivot d, local row r.
-// Returns false when the reference writes nothing for this item.
-__device__ __forceinline__ bool item_target(const DiagLat& L, const int32_t* p, int o, int& d, int& row, int64_t& slot,
-                                            int32_t& dst_f, int32_t f) {
-  if (o < L.n) {
-    const int i = o;
-    if (!(L.c[0] == 1 || p[0] < L.c[0] - 1)) return false;
-    if (!(p[i >> 1] + 1 < L.c[i >> 1] && (i != 1 || p[0] + 2 < L.c[0]))) return false;
-    d = -1;
-    row = i;
-    slot = slot_arr1(L, i);
-    dst_f = f;
-    return true;
-  }
-  d = (o - L.n) / L.n;
-  const int r = (o - L.n) % L.n;
-  for (int k = 0; k < d; ++k)
-    if (p[k] != 0) return false;
+// Target of local row r of the off-diagonal pivot d (r = 0: arr0[p + 1_d]; r = 1: arr2[d];
+// r >= 2: arr1010 / arr1001 of mode d + 1 + (r - 2) / 2).  False when the reference writes nothing.
+__device__ __forceinline__ bool offdiag_target(const DiagLat& L, const int32_t* p, int d, int r, int& row,
+                                               int64_t& slot, int32_t& dst, int32_t f) {
   if (!(p[d] < L.c[d] - 1) || r >= L.n - 2 * d) return false;
   if (r == 0) {
     row = 2 * d + 1;
     slot = 0;
-    dst_f = f + L.st[d];
+    dst = f + L.st[d];
     return true;
   }
-  dst_f = f;
+  dst = f;
   if (r == 1) {
     if (!(p[d] + 2 < L.c[d])) return false;
     row = 2 * d;
@@ -289,34 +350,70 @@ __device__ __forceinline__ bool item_target(const DiagLat& L, const int32_t* p, 
   return true;
 }
 
+__device__ __forceinline__ bool diag_target(const DiagLat& L, const int32_t* p, int i) {
+  return (L.c[0] == 1 || p[0] < L.c[0] - 1) && p[i >> 1] + 1 < L.c[i >> 1] && (i != 1 || p[0] + 2 < L.c[0]);
+}
+
+// The off-diagonal pivots d of a point are 0 .. (index of its first non-zero coordinate).
+template <int M>
+__device__ __forceinline__ int last_pivot(const int32_t* p) {
+  int fz = M - 1;
+#pragma unroll
+  for (int k = M - 1; k >= 0; --k)
+    if (p[k] != 0) fz = k;
+  return fz;
+}
+
+// Items of one weight: (slot r, point, column), column fastest, then point, so that the
+// lanes of a warp run the same row of neighbouring points (or columns).  Slots 0 .. 2M-1
+// are the diagonal-pivot rows; slots 2M .. 4M-1 the off-diagonal rows r - 2M of every pivot d.
+template <int M>
 __global__ void __launch_bounds__(DG_BLOCK) diag_amps_kernel(DiagArgs a) {
+  constexpr int n = 2 * M;
+  MM_SHARED(StageSmem, sm);
+  stage_operands(sm, a.t, a.ntab, a.A, n, nullptr);
   const DiagLat& L = a.L;
-  const int per_point = L.n + L.M * L.n;
   const int64_t PN = (int64_t)L.P * L.nb;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  // The point of this thread's first item of the next weight is read before the barrier
+  // (the order is fixed), taking two dependent loads off the path after it.
+  auto first_point = [&](int w, int32_t& s0, int32_t& cnt) -> int32_t {
+    s0 = a.sb.start[w];
+    cnt = a.sb.start[w + 1] - s0;
+    const int64_t per_slot = (int64_t)cnt * L.nb;
+    if (t0 >= per_slot * 2 * n) return -1;
+    const int64_t u = t0 - (t0 / per_slot) * per_slot;
+    return a.sb.order[s0 + (int32_t)(u / L.nb)];
+  };
+  int32_t s0, cnt;
+  int32_t fnext = first_point(0, s0, cnt);
   uint32_t epoch = 0;
   for (int w = 0; w < L.W; ++w) {
-    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
-    const int64_t items = (int64_t)cnt * per_point * L.nb;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
-      const int32_t col = (int32_t)(t % L.nb);
-      const int64_t r = t / L.nb;
-      const int o = (int)(r % per_point);
-      const int32_t f = a.sb.order[s0 + (int32_t)(r / per_point)];
-      int32_t p[DG_MAXM];
-      diag_weight(L, f, p);
-      int d, row;
-      int64_t slot;
-      int32_t dst;
-      if (!item_target(L, p, o, d, row, slot, dst, f)) continue;
-      double2 v;
-      if (d < 0) {
-        v = diag_row(a, p, f, row, col);
-      } else {
-        const double2 g = diag_row(a, p, f, 2 * d, col);
-        v = offdiag_row(a, p, f, d, row, g, col);
+    const int64_t per_slot = (int64_t)cnt * L.nb;
+    const int64_t items = per_slot * 2 * n;
+    for (int64_t t = t0; t < items; t += stride) {
+      const int r = (int)(t / per_slot);
+      const int64_t u = t - r * per_slot;
+      const int32_t pidx = (int32_t)(u / L.nb);
+      const int32_t col = (int32_t)(u - (int64_t)pidx * L.nb);
+      const int32_t f = t == t0 ? fnext : a.sb.order[s0 + pidx];
+      int32_t p[M];
+      decode_params<M>(L, f, p);
+      if (r < n) {
+        if (diag_target(L, p, r)) a.Wv[slot_arr1(L, r) * PN + (int64_t)f * L.nb + col] = diag_row<M>(a, p, f, r, col);
+        continue;
       }
-      a.Wv[slot * PN + (int64_t)dst * L.nb + col] = v;
+      const int lr = r - n, dl = last_pivot<M>(p);
+      for (int d = 0; d <= dl; ++d) {
+        int row;
+        int64_t slot;
+        int32_t dst;
+        if (!offdiag_target(L, p, d, lr, row, slot, dst, f)) continue;
+        const double2 g = diag_row<M>(a, p, f, 2 * d, col);
+        a.Wv[slot * PN + (int64_t)dst * L.nb + col] = offdiag_row<M>(a, p, f, d, row, g, col);
+      }
     }
+    if (w + 1 < L.W) fnext = first_point(w + 1, s0, cnt);
     if (!step_barrier(a.h, epoch, a.budget)) return;
   }
 }
@@ -331,78 +428,111 @@ __global__ void diag_init_kernel(DiagArgs a) {
 //   d/dA_pq = (Jp_pq B_i + sum_l K_l A_il J_l,pq + [p == i] K_q Gin_q) / K_i
 //   d/dB_r  = (Jp_r  B_i + [r == i] g + sum_l K_l A_il J_l,r) / K_i
 
+template <int M>
 __device__ __forceinline__ double2 jac_diag_row(const DiagArgs& a, const int32_t* p, int32_t f, int i, int q) {
+  constexpr int n = 2 * M, nc = n * n + n;
   const DiagLat& L = a.L;
-  const int nc = L.n * L.n + L.n;
   const int64_t P = L.P;
+  const bool isA = q < n * n;
+  const int qa = q / n, qb = q - qa * n;  // (row, column) of a dA component
+  double2 jin[n];
+#pragma unroll
+  for (int l = 0; l < n; ++l)
+    jin[l] = p[l >> 1] > 0 ? ldv(&a.J[(slot_arr1(L, l ^ 1) * P + (f - L.st[l >> 1])) * nc + q]) : cmk(0.0, 0.0);
   double2 acc = cmul(ldv(&a.J[(int64_t)f * nc + q]), __ldg(&a.B[i]));
-  const bool isA = q < L.n * L.n;
-  if (!isA && q - L.n * L.n == i) acc = cadd(acc, ldv(&a.Wv[f]));
-  for (int l = 0; l < L.n; ++l) {
-    const int k = l >> 1;
-    if (p[k] == 0) continue;
-    const int64_t src = slot_arr1(L, l ^ 1) * P + (f - L.st[k]);
-    const double s = sqrt((double)p[k]);
-    acc = cfma(cscale(s, __ldg(&a.A[i * L.n + l])), ldv(&a.J[src * nc + q]), acc);
-    if (isA && q == i * L.n + l) acc = cadd(acc, cscale(s, ldv(&a.Wv[src])));
-  }
-  return cdivs(acc, sqrt((double)(p[i >> 1] + 1)));
+  if (!isA && q - n * n == i) acc = cadd(acc, ldv(&a.Wv[f]));
+#pragma unroll
+  for (int l = 0; l < n; ++l) acc = cfma(cscale(a.t.sq[p[l >> 1]], a.A[i * n + l]), jin[l], acc);
+  if (isA && qa == i && p[qb >> 1] > 0)
+    acc = cadd(acc, cscale(a.t.sq[p[qb >> 1]], ldv(&a.Wv[slot_arr1(L, qb ^ 1) * P + (f - L.st[qb >> 1])])));
+  return cscale(a.t.rs[p[i >> 1] + 1], acc);
 }
 
+template <int M>
 __device__ __forceinline__ double2 jac_offdiag_row(const DiagArgs& a, const int32_t* p, int32_t f, int d, int row,
                                                    double2 Jp, int q) {
+  constexpr int n = 2 * M, nc = n * n + n;
   const DiagLat& L = a.L;
-  const int nc = L.n * L.n + L.n;
   const int64_t P = L.P;
-  const bool isA = q < L.n * L.n;
-  double2 acc = cmul(Jp, __ldg(&a.B[row]));
-  if (!isA && q - L.n * L.n == row) acc = cadd(acc, ldv(&a.Wv[slot_arr1(L, 2 * d) * P + f]));
-  auto term = [&](int l, double s, int64_t src) {
-    acc = cfma(cscale(s, __ldg(&a.A[row * L.n + l])), ldv(&a.J[src * nc + q]), acc);
-    if (isA && q == row * L.n + l) acc = cadd(acc, cscale(s, ldv(&a.Wv[src])));
-  };
-  term(2 * d, sqrt((double)(p[d] + 1)), (int64_t)f);
-  if (p[d] > 0) term(2 * d + 1, sqrt((double)p[d]), slot_arr2(L, d) * P + (f - L.st[d]));
-  for (int i = d + 1; i < L.M; ++i) {
-    if (p[i] == 0) continue;
-    const double s = sqrt((double)p[i]);
-    term(2 * i, s, slot_1001(L, d, i - d - 1) * P + (f - L.st[i]));
-    term(2 * i + 1, s, slot_1010(L, d, i - d - 1) * P + (f - L.st[i]));
+  const bool isA = q < n * n;
+  const int qa = q / n, qb = q - qa * n;
+  int64_t src[n];
+  double kl[n];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    src[2 * i] = -1;
+    src[2 * i + 1] = -1;
+    kl[2 * i] = a.t.sq[p[i]];
+    kl[2 * i + 1] = kl[2 * i];
+    if (i < d) continue;
+    if (i == d) {
+      kl[2 * i] = a.t.sq[p[i] + 1];
+      src[2 * i] = f;
+      if (p[i] > 0) src[2 * i + 1] = slot_arr2(L, d) * P + (f - L.st[i]);
+    } else if (p[i] > 0) {
+      src[2 * i] = slot_1001(L, d, i - d - 1) * P + (f - L.st[i]);
+      src[2 * i + 1] = slot_1010(L, d, i - d - 1) * P + (f - L.st[i]);
+    }
   }
+  double2 jin[n];
+#pragma unroll
+  for (int l = 0; l < n; ++l) jin[l] = src[l] >= 0 ? ldv(&a.J[src[l] * nc + q]) : cmk(0.0, 0.0);
+  double2 acc = cmul(Jp, __ldg(&a.B[row]));
+  if (!isA && q - n * n == row) acc = cadd(acc, ldv(&a.Wv[slot_arr1(L, 2 * d) * P + f]));
+#pragma unroll
+  for (int l = 0; l < n; ++l) acc = cfma(cscale(kl[l], a.A[row * n + l]), jin[l], acc);
+  if (isA && qa == row && src[qb] >= 0) acc = cadd(acc, cscale(kl[qb], ldv(&a.Wv[src[qb]])));
   const int k = row >> 1;
   const int lift = (row & 1) == 0 && k == d;
-  return cdivs(acc, sqrt((double)(p[k] + lift + 1)));
+  return cscale(a.t.rs[p[k] + lift + 1], acc);
 }
 
+// Items of one weight: (slot r, point, component q), q fastest (coalesced Jacobian rows).
+template <int M>
 __global__ void __launch_bounds__(DG_BLOCK) diag_jacobian_kernel(DiagArgs a) {
+  constexpr int n = 2 * M, nc = n * n + n;
+  MM_SHARED(StageSmem, sm);
+  stage_operands(sm, a.t, a.ntab, a.A, n, nullptr);
   const DiagLat& L = a.L;
-  const int per_point = L.n + L.M * L.n;
-  const int nc = L.n * L.n + L.n;
   const int64_t P = L.P;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  auto first_point = [&](int w, int32_t& s0, int32_t& cnt) -> int32_t {
+    s0 = a.sb.start[w];
+    cnt = a.sb.start[w + 1] - s0;
+    const int64_t per_slot = (int64_t)cnt * nc;
+    if (t0 >= per_slot * 2 * n) return -1;
+    const int64_t u = t0 - (t0 / per_slot) * per_slot;
+    return a.sb.order[s0 + (int32_t)(u / nc)];
+  };
+  int32_t s0, cnt;
+  int32_t fnext = first_point(0, s0, cnt);
   uint32_t epoch = 0;
   for (int w = 0; w < L.W; ++w) {
-    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
-    const int64_t items = (int64_t)cnt * per_point * nc;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
-      const int q = (int)(t % nc);
-      const int64_t r = t / nc;
-      const int o = (int)(r % per_point);
-      const int32_t f = a.sb.order[s0 + (int32_t)(r / per_point)];
-      int32_t p[DG_MAXM];
-      diag_weight(L, f, p);
-      int d, row;
-      int64_t slot;
-      int32_t dst;
-      if (!item_target(L, p, o, d, row, slot, dst, f)) continue;
-      double2 v;
-      if (d < 0) {
-        v = jac_diag_row(a, p, f, row, q);
-      } else {
-        const double2 Jp = jac_diag_row(a, p, f, 2 * d, q);
-        v = jac_offdiag_row(a, p, f, d, row, Jp, q);
+    const int64_t per_slot = (int64_t)cnt * nc;
+    const int64_t items = per_slot * 2 * n;
+    for (int64_t t = t0; t < items; t += stride) {
+      const int r = (int)(t / per_slot);
+      const int64_t u = t - r * per_slot;
+      const int32_t pidx = (int32_t)(u / nc);
+      const int q = (int)(u - (int64_t)pidx * nc);
+      const int32_t f = t == t0 ? fnext : a.sb.order[s0 + pidx];
+      int32_t p[M];
+      decode_params<M>(L, f, p);
+      if (r < n) {
+        if (diag_target(L, p, r)) a.J[(slot_arr1(L, r) * P + f) * nc + q] = jac_diag_row<M>(a, p, f, r, q);
+        continue;
       }
-      a.J[(slot * P + dst) * nc + q] = v;
+      const int lr = r - n, dl = last_pivot<M>(p);
+      for (int d = 0; d <= dl; ++d) {
+        int row;
+        int64_t slot;
+        int32_t dst;
+        if (!offdiag_target(L, p, d, lr, row, slot, dst, f)) continue;
+        const double2 Jp = jac_diag_row<M>(a, p, f, 2 * d, q);
+        a.J[(slot * P + dst) * nc + q] = jac_offdiag_row<M>(a, p, f, d, row, Jp, q);
+      }
     }
+    if (w + 1 < L.W) fnext = first_point(w + 1, s0, cnt);
     if (!step_barrier(a.h, epoch, a.budget)) return;
   }
 }
@@ -450,6 +580,8 @@ struct FdArgs {
   double2* bp;       // permuted b (workspace)
   double2* G;        // npts x q^2 (workspace)
   double2* out;      // (pnr + 1 ..., q, q)
+  Tabs t;
+  int32_t ntab;
   SortBufs sb;
   WsHeader* h;
   uint64_t budget;
@@ -467,6 +599,8 @@ __device__ __forceinline__ int32_t fd_zero_id(const FdLat& F) {
 __global__ void fd_init_kernel(FdArgs a) {
   const FdLat& F = a.F;
   const int Lm = F.K + 1, n = 2 * Lm, q = F.q;
+  const double* sq = a.t.sq;
+  const double* rs = a.t.rs;
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
     const int r = t / n, s = t % n;
     const int pr = (r & 1) ? (r >> 1) + Lm : (r >> 1), ps = (s & 1) ? (s >> 1) + Lm : (s >> 1);
@@ -486,32 +620,32 @@ __global__ void fd_init_kernel(FdArgs a) {
       if (!a.stable) {
         if (m == 0) {  // face: pivot on axis 1
           double2 acc = cmul(b1, at(0, k - 1));
-          acc = cfma(cscale(sqrt((double)(k - 1 > 0 ? k - 1 : 0)), A11), at(0, k - 2), acc);
-          v = cdivs(acc, sqrt((double)k));
+          acc = cfma(cscale(sq[k - 1], A11), at(0, k - 2), acc);
+          v = cscale(rs[k], acc);
         } else {  // bulk: pivot on axis 0
           double2 acc = cmul(b0, at(m - 1, k));
-          acc = cfma(cscale(sqrt((double)(m - 1)), A00), at(m - 2, k), acc);
-          acc = cfma(cscale(sqrt((double)k), A01), at(m - 1, k - 1), acc);
-          v = cdivs(acc, sqrt((double)m));
+          acc = cfma(cscale(sq[m - 1], A00), at(m - 2, k), acc);
+          acc = cfma(cscale(sq[k], A01), at(m - 1, k - 1), acc);
+          v = cscale(rs[m], acc);
         }
       } else {  // average over the pivots with k_i > 0
         double2 vals = cmk(0.0, 0.0);
         int npiv = 0;
         if (m > 0) {
           double2 acc = cmul(b0, at(m - 1, k));
-          acc = cfma(cscale(sqrt((double)(m - 1)), A00), at(m - 2, k), acc);
-          acc = cfma(cscale(sqrt((double)k), A01), at(m - 1, k - 1), acc);
-          vals = cadd(vals, cdivs(acc, sqrt((double)m)));
+          acc = cfma(cscale(sq[m - 1], A00), at(m - 2, k), acc);
+          acc = cfma(cscale(sq[k], A01), at(m - 1, k - 1), acc);
+          vals = cadd(vals, cscale(rs[m], acc));
           ++npiv;
         }
         if (k > 0) {
           double2 acc = cmul(b1, at(m, k - 1));
-          acc = cfma(cscale(sqrt((double)m), A10), at(m - 1, k - 1), acc);
-          acc = cfma(cscale(sqrt((double)(k - 1)), A11), at(m, k - 2), acc);
-          vals = cadd(vals, cdivs(acc, sqrt((double)k)));
+          acc = cfma(cscale(sq[m], A10), at(m - 1, k - 1), acc);
+          acc = cfma(cscale(sq[k - 1], A11), at(m, k - 2), acc);
+          vals = cadd(vals, cscale(rs[k], acc));
           ++npiv;
         }
-        v = cdivs(vals, (double)npiv);
+        v = npiv == 2 ? cscale(0.5, vals) : vals;  // / npiv (exact for 1 and 2)
       }
       G[m * q + k] = v;
     }
@@ -520,23 +654,47 @@ __global__ void fd_init_kernel(FdArgs a) {
   for (int t = threadIdx.x; t < q * q; t += blockDim.x) a.out[t] = G[t];
 }
 
+// Items of one weight: (point, block element e), e fastest: the lanes of a warp share the
+// point (and its pivot) and read consecutive block elements.
+template <int K>
 __global__ void __launch_bounds__(DG_BLOCK) fd_kernel(FdArgs a) {
+  constexpr int n = 2 * (K + 1);
+  MM_SHARED(StageSmem, sm);
+  const double2* Ap = a.Ap;
+  const double2* bp = a.bp;
+  stage_operands(sm, a.t, a.ntab, Ap, n, &bp);
   const FdLat& F = a.F;
-  const int q = F.q, qq = q * q, n = 2 * (F.K + 1);
+  const int q = F.q, qq = q * q;
+  const double* sq = a.t.sq;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  auto first_point = [&](int w, int32_t& s0, int32_t& cnt) -> int32_t {
+    s0 = a.sb.start[w];
+    cnt = a.sb.start[w + 1] - s0;
+    if (t0 >= (int64_t)cnt * qq) return -1;
+    return a.sb.order[s0 + (int32_t)(t0 / qq)];
+  };
   uint32_t epoch = 0;
   const int wlast = min(F.W - 1, F.wend - 1);
+  int32_t s0 = 0, cnt = 0, idnext = -1;
+  if (wlast >= 1) idnext = first_point(1, s0, cnt);
   for (int w = 1; w <= wlast; ++w) {
-    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
     const int64_t items = (int64_t)cnt * qq;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
-      const int e = (int)(t % qq);
-      const int32_t id = a.sb.order[s0 + (int32_t)(t / qq)];
-      const int m = e / q, kk = e % q;
-      int32_t k[2 * FD_MAXK];
-      fd_decode(F, id, k);
+    for (int64_t t = t0; t < items; t += stride) {
+      const int32_t pi = (int32_t)(t / qq);
+      const int e = (int)(t - (int64_t)pi * qq);
+      const int32_t id = t == t0 ? idnext : a.sb.order[s0 + pi];
+      const int m = e / q, kk = e - m * q;
+      int32_t k[2 * K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const int32_t s = (id / F.pst[j]) % F.rad[j];
+        k[2 * j] = s / 5;
+        k[2 * j + 1] = s / 5 - (s % 5 - 2);
+      }
       // get_pivot (fast_diagonal.py:80-99)
       int mbest = 0, dbest = -1;
-      for (int j = 0; j < F.K; ++j) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
         const int dl = abs(k[2 * j] - k[2 * j + 1]);
         if (dl > dbest) {
           dbest = dl;
@@ -546,36 +704,41 @@ __global__ void __launch_bounds__(DG_BLOCK) fd_kernel(FdArgs a) {
       int i;
       if (dbest == 0) {
         i = 0;
-        for (int j = 1; j < 2 * F.K; ++j)
+#pragma unroll
+        for (int j = 1; j < 2 * K; ++j)
           if (k[j] > k[i]) i = j;
       } else {
         i = k[2 * mbest] > k[2 * mbest + 1] ? 2 * mbest : 2 * mbest + 1;
       }
       // pivot id: lowering a (even coordinate) moves the pair state by -6, lowering b by +1
       const int32_t pid = id + ((i & 1) ? 1 : -6) * F.pst[i >> 1];
-      k[i] -= 1;  // k is now the pivot's coordinates
+      int32_t kp[2 * K];
+#pragma unroll
+      for (int j = 0; j < 2 * K; ++j) kp[j] = k[j] - (j == i);
       const double2* mat = a.G + (int64_t)pid * qq;
-      const double2* Arow = a.Ap + (i + 2) * n;
+      const double2* Arow = Ap + (i + 2) * n;
+      double2 low[2 * K];
+#pragma unroll
+      for (int j = 0; j < 2 * K; ++j)
+        low[j] = kp[j] > 0 ? ldv(&a.G[(int64_t)(pid + ((j & 1) ? 1 : -6) * F.pst[j >> 1]) * qq + e]) : cmk(0.0, 0.0);
       // single_step (fast_diagonal.py:102-124)
-      double2 acc = cmul(a.bp[i + 2], ldv(&mat[e]));
-      if (m > 0) acc = cfma(cscale(sqrt((double)m), Arow[0]), ldv(&mat[e - q]), acc);
-      if (kk > 0) acc = cfma(cscale(sqrt((double)kk), Arow[1]), ldv(&mat[e - 1]), acc);
-      for (int j = 0; j < 2 * F.K; ++j) {
-        if (k[j] <= 0) continue;
-        const int32_t lid = pid + ((j & 1) ? 1 : -6) * F.pst[j >> 1];
-        acc = cfma(cscale(sqrt((double)k[j]), Arow[j + 2]), ldv(&a.G[(int64_t)lid * qq + e]), acc);
-      }
-      const double2 v = cdivs(acc, sqrt((double)(k[i] + 1)));
+      double2 acc = cmul(bp[i + 2], ldv(&mat[e]));
+      if (m > 0) acc = cfma(cscale(sq[m], Arow[0]), ldv(&mat[e - q]), acc);
+      if (kk > 0) acc = cfma(cscale(sq[kk], Arow[1]), ldv(&mat[e - 1]), acc);
+#pragma unroll
+      for (int j = 0; j < 2 * K; ++j) acc = cfma(cscale(sq[kp[j]], Arow[j + 2]), low[j], acc);
+      const double2 v = cscale(a.t.rs[k[i]], acc);
       a.G[(int64_t)id * qq + e] = v;
-      k[i] += 1;
       bool diag = true;
       int32_t o = 0;
-      for (int j = 0; j < F.K; ++j) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
         diag &= k[2 * j] == k[2 * j + 1];
         o += k[2 * j] * F.ost[j];
       }
       if (diag) a.out[(int64_t)o * qq + e] = v;
     }
+    if (w + 1 <= wlast) idnext = first_point(w + 1, s0, cnt);
     if (!step_barrier(a.h, epoch, a.budget)) return;
   }
 }
@@ -588,8 +751,7 @@ struct DevCfg {
   int occ = 0;
 };
 
-template <class K>
-int dev_cfg(K kernel, DevCfg& dc) {
+int dev_cfg(const void* kernel, DevCfg& dc) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return MM_ERR_NO_DEVICE;
   if (cudaDeviceGetAttribute(&dc.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MM_ERR_CUDA;
@@ -636,17 +798,41 @@ std::vector<int64_t> diag_counts(const DiagLat& L) {
 }
 
 struct DiagWs {
-  size_t header, count, start, cursor, order, total;
+  size_t header, count, start, cursor, order, tabs, total;
+  int32_t ntab;
 };
-DiagWs diag_ws(int32_t W, int32_t npts) {
+// header | weight counts | starts | cursors | point order | sqrt and 1/sqrt tables (ntab each)
+DiagWs diag_ws(int32_t W, int32_t npts, int32_t ntab) {
   DiagWs w;
   w.header = 0;
+  w.ntab = ntab;
   w.count = al(sizeof(WsHeader));
   w.start = w.count + al((size_t)W * sizeof(int32_t));
   w.cursor = w.start + al((size_t)(W + 1) * sizeof(int32_t));
   w.order = w.cursor + al((size_t)W * sizeof(int32_t));
-  w.total = w.order + al((size_t)npts * sizeof(int32_t));
+  w.tabs = w.order + al((size_t)npts * sizeof(int32_t));
+  w.total = w.tabs + al(2 * (size_t)ntab * sizeof(double));
   return w;
+}
+Tabs tabs_of(char* ws, const DiagWs& w) {
+  Tabs t;
+  t.sq = reinterpret_cast<const double*>(ws + w.tabs);
+  t.rs = t.sq + w.ntab;
+  return t;
+}
+#ifndef MM_HOST_EMULATION
+int launch_tables(char* ws, const DiagWs& w, cudaStream_t st) {
+  double* sq = reinterpret_cast<double*>(ws + w.tabs);
+  sqrt_table_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((w.ntab + 255) / 256, 64)), 256, 0, st>>>(
+      sq, sq + w.ntab, w.ntab);
+  note_launches(1);
+  return cuda_status();
+}
+#endif
+int32_t diag_ntab(const DiagLat& L) {
+  int32_t mc = 1;
+  for (int k = 0; k < L.M; ++k) mc = std::max(mc, L.c[k]);
+  return mc + 3;  // sqrt(p + 2) with p <= c - 1
 }
 SortBufs sort_bufs(char* ws, const DiagWs& w) {
   SortBufs sb;
@@ -663,8 +849,19 @@ int check_ws(void* ws, size_t ws_bytes, size_t need) {
   return MM_OK;
 }
 
+// CTAs of a wavefront launch: one per DG_BLOCK items of the widest weight, at most what fits
+// co-resident (and at most MM_DIAG_MAX_CTAS when that is set).
+int64_t max_ctas_env() {
+  static const int64_t v = [] {
+    const char* s = getenv("MM_DIAG_MAX_CTAS");
+    return s ? (int64_t)strtoll(s, nullptr, 10) : (int64_t)0;
+  }();
+  return v;
+}
+
 int launch_wavefront(void* kern, void* arg, int64_t max_items, int sms, int occ, cudaStream_t st) {
-  const int64_t cap = (int64_t)sms * occ;
+  int64_t cap = (int64_t)sms * occ;
+  if (max_ctas_env() > 0) cap = std::min(cap, max_ctas_env());
   const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((max_items + DG_BLOCK - 1) / DG_BLOCK, cap));
   void* args[] = {arg};
   if (cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(DG_BLOCK), args, 0, st) != cudaSuccess) return MM_ERR_CUDA;
@@ -726,9 +923,14 @@ struct FdWs {
   DiagWs base;
   size_t ap, g, total;
 };
+int32_t fd_ntab(const FdLat& F) {
+  int32_t mx = F.q;
+  for (int j = 0; j < F.K; ++j) mx = std::max(mx, F.pnr[j] + 2);
+  return mx + 1;
+}
 FdWs fd_ws(const FdLat& F) {
   FdWs w;
-  w.base = diag_ws(F.W, F.npts);
+  w.base = diag_ws(F.W, F.npts, fd_ntab(F));
   const int n = 2 * (F.K + 1);
   w.ap = w.base.total;
   w.g = w.ap + al((size_t)(n * n + n) * sizeof(double2));
@@ -746,7 +948,46 @@ MM_API int64_t mm_diagonal_slots(int M) { return M < 1 ? 0 : diag_slots(M); }
 MM_API size_t mm_diagonal_workspace_bytes(int M, const int64_t* cutoffs, int64_t nb) {
   DiagLat L;
   if (diag_lat(M, cutoffs, nb, L)) return 0;
-  return diag_ws(L.W, L.P).total;
+  return diag_ws(L.W, L.P, diag_ntab(L)).total;
+}
+
+void* diag_amps_fn(int M) {
+  switch (M) {
+    case 1: return (void*)diag_amps_kernel<1>;
+    case 2: return (void*)diag_amps_kernel<2>;
+    case 3: return (void*)diag_amps_kernel<3>;
+    case 4: return (void*)diag_amps_kernel<4>;
+    case 5: return (void*)diag_amps_kernel<5>;
+    case 6: return (void*)diag_amps_kernel<6>;
+    case 7: return (void*)diag_amps_kernel<7>;
+    case 8: return (void*)diag_amps_kernel<8>;
+  }
+  return nullptr;
+}
+void* diag_jacobian_fn(int M) {
+  switch (M) {
+    case 1: return (void*)diag_jacobian_kernel<1>;
+    case 2: return (void*)diag_jacobian_kernel<2>;
+    case 3: return (void*)diag_jacobian_kernel<3>;
+    case 4: return (void*)diag_jacobian_kernel<4>;
+    case 5: return (void*)diag_jacobian_kernel<5>;
+    case 6: return (void*)diag_jacobian_kernel<6>;
+    case 7: return (void*)diag_jacobian_kernel<7>;
+    case 8: return (void*)diag_jacobian_kernel<8>;
+  }
+  return nullptr;
+}
+void* fd_fn(int K) {
+  switch (K) {
+    case 1: return (void*)fd_kernel<1>;
+    case 2: return (void*)fd_kernel<2>;
+    case 3: return (void*)fd_kernel<3>;
+    case 4: return (void*)fd_kernel<4>;
+    case 5: return (void*)fd_kernel<5>;
+    case 6: return (void*)fd_kernel<6>;
+    case 7: return (void*)fd_kernel<7>;
+  }
+  return nullptr;
 }
 
 MM_API int mm_diagonal_amps(int M, const int64_t* cutoffs, int64_t nb, const mm_c128* A, const mm_c128* B,
@@ -755,10 +996,11 @@ MM_API int mm_diagonal_amps(int M, const int64_t* cutoffs, int64_t nb, const mm_
   int rc = diag_lat(M, cutoffs, nb, L);
   if (rc) return rc;
   if (!A || !B || !G0 || !W) return MM_ERR_INVALID_ARG;
-  const DiagWs lay = diag_ws(L.W, L.P);
+  const DiagWs lay = diag_ws(L.W, L.P, diag_ntab(L));
   if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  void* kern = diag_amps_fn(M);
   DevCfg dc;
-  if ((rc = dev_cfg(diag_amps_kernel, dc))) return rc;
+  if ((rc = dev_cfg(kern, dc))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   DiagArgs a;
@@ -768,6 +1010,8 @@ MM_API int mm_diagonal_amps(int M, const int64_t* cutoffs, int64_t nb, const mm_
   a.B = (const double2*)B;
   a.G0 = (const double2*)G0;
   a.Wv = (double2*)W;
+  a.t = tabs_of(w, lay);
+  a.ntab = lay.ntab;
   a.sb = sort_bufs(w, lay);
   a.h = reinterpret_cast<WsHeader*>(w);
   a.budget = budget_ns();
@@ -775,12 +1019,13 @@ MM_API int mm_diagonal_amps(int M, const int64_t* cutoffs, int64_t nb, const mm_
   if (cudaMemsetAsync(W, 0, (size_t)diag_slots(M) * L.P * L.nb * sizeof(double2), st) != cudaSuccess)
     return MM_ERR_CUDA;
   if ((rc = launch_sort(L, L.P, L.W, a.sb, dc.sms, st))) return rc;
+  if ((rc = launch_tables(w, lay, st))) return rc;
   diag_init_kernel<<<1, 128, 0, st>>>(a);
   note_launches(1);
   if ((rc = cuda_status())) return rc;
   const std::vector<int64_t> cnt = diag_counts(L);
-  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * (L.n + L.M * L.n) * L.nb;
-  return launch_wavefront((void*)diag_amps_kernel, &a, max_items, dc.sms, dc.occ, st);
+  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * 2 * L.n * L.nb;
+  return launch_wavefront(kern, &a, max_items, dc.sms, dc.occ, st);
 }
 
 MM_API int mm_diagonal_jacobian(int M, const int64_t* cutoffs, const mm_c128* A, const mm_c128* B, const mm_c128* W,
@@ -791,10 +1036,11 @@ MM_API int mm_diagonal_jacobian(int M, const int64_t* cutoffs, const mm_c128* A,
   if (!A || !B || !W || !J) return MM_ERR_INVALID_ARG;
   const int64_t nc = (int64_t)L.n * L.n + L.n;
   if ((int64_t)L.P * nc * diag_slots(M) > ((int64_t)1 << 36)) return MM_ERR_TOO_LARGE;
-  const DiagWs lay = diag_ws(L.W, L.P);
+  const DiagWs lay = diag_ws(L.W, L.P, diag_ntab(L));
   if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  void* kern = diag_jacobian_fn(M);
   DevCfg dc;
-  if ((rc = dev_cfg(diag_jacobian_kernel, dc))) return rc;
+  if ((rc = dev_cfg(kern, dc))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   DiagArgs a;
@@ -804,15 +1050,18 @@ MM_API int mm_diagonal_jacobian(int M, const int64_t* cutoffs, const mm_c128* A,
   a.B = (const double2*)B;
   a.Wv = (double2*)W;
   a.J = (double2*)J;
+  a.t = tabs_of(w, lay);
+  a.ntab = lay.ntab;
   a.sb = sort_bufs(w, lay);
   a.h = reinterpret_cast<WsHeader*>(w);
   a.budget = budget_ns();
   if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
   if (cudaMemsetAsync(J, 0, (size_t)diag_slots(M) * L.P * nc * sizeof(double2), st) != cudaSuccess) return MM_ERR_CUDA;
   if ((rc = launch_sort(L, L.P, L.W, a.sb, dc.sms, st))) return rc;
+  if ((rc = launch_tables(w, lay, st))) return rc;
   const std::vector<int64_t> cnt = diag_counts(L);
-  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * (L.n + L.M * L.n) * nc;
-  return launch_wavefront((void*)diag_jacobian_kernel, &a, max_items, dc.sms, dc.occ, st);
+  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * 2 * L.n * nc;
+  return launch_wavefront(kern, &a, max_items, dc.sms, dc.occ, st);
 }
 
 MM_API int mm_diagonal_vjp(int M, const int64_t* cutoffs, const mm_c128* J, const mm_c128* W, const mm_c128* G0,
@@ -844,8 +1093,9 @@ MM_API int mm_fast_diagonal(int L, const int64_t* pnr_cutoffs, int64_t output_cu
   if (!A || !b || !c || !out) return MM_ERR_INVALID_ARG;
   const FdWs lay = fd_ws(F);
   if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  void* kern = fd_fn(F.K);
   DevCfg dc;
-  if ((rc = dev_cfg(fd_kernel, dc))) return rc;
+  if ((rc = dev_cfg(kern, dc))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   FdArgs a;
@@ -860,6 +1110,8 @@ MM_API int mm_fast_diagonal(int L, const int64_t* pnr_cutoffs, int64_t output_cu
   a.bp = a.Ap + n * n;
   a.G = reinterpret_cast<double2*>(w + lay.g);
   a.out = (double2*)out;
+  a.t = tabs_of(w, lay.base);
+  a.ntab = lay.base.ntab;
   a.sb = sort_bufs(w, lay.base);
   a.h = reinterpret_cast<WsHeader*>(w);
   a.budget = budget_ns();
@@ -868,12 +1120,13 @@ MM_API int mm_fast_diagonal(int L, const int64_t* pnr_cutoffs, int64_t output_cu
   if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
   if (cudaMemsetAsync(out, 0, (size_t)nout * sizeof(double2), st) != cudaSuccess) return MM_ERR_CUDA;
   if ((rc = launch_sort(F, F.npts, F.W, a.sb, dc.sms, st))) return rc;
+  if ((rc = launch_tables(w, lay.base, st))) return rc;
   fd_init_kernel<<<1, 256, 0, st>>>(a);
   note_launches(1);
   if ((rc = cuda_status())) return rc;
   const std::vector<int64_t> cnt = fd_counts(F);
   int64_t mx = 1;
   for (int wgt = 1; wgt < (int)cnt.size() && wgt < F.wend; ++wgt) mx = std::max(mx, cnt[wgt]);
-  return launch_wavefront((void*)fd_kernel, &a, mx * F.q * F.q, dc.sms, dc.occ, st);
+  return launch_wavefront(kern, &a, mx * F.q * F.q, dc.sms, dc.occ, st);
 }
 #endif  // MM_HOST_EMULATION
