@@ -306,6 +306,30 @@ MM_API int mm_fast_diagonal(int L, const int64_t *pnr_cutoffs, int64_t output_cu
                             const mm_c128 *b, const mm_c128 *c, int stable, mm_c128 *out, void *ws, size_t ws_bytes,
                             mm_stream_t stream);
 
+/* ------------------------------------------------------------- Fock einsum building blocks */
+
+/*
+ * The pieces of a general pairwise Fock-space contraction, replacing what
+ * ArrayAnsatz.contract (mrmustard/physics/ansatz/array_ansatz.py:159-226) reaches through
+ * math.einsum (mrmustard/math/backend_manager.py:526-548) and opt_einsum: the slicing of the
+ * contracted labels to a common dimension, the permutations, and the BLAS matrix product.
+ * All complex128 device pointers, asynchronous on `stream`, no workspace.
+ *
+ * mm_tensor_permute: out (C order over out_shape, rank <= 16) gets
+ *   out[i_0, ..., i_{r-1}] = in[in_offset + sum_k i_k * in_strides[k]]
+ * -- any strided view (a permutation, a slice, the diagonal of a repeated label) made contiguous.
+ */
+MM_API int mm_tensor_permute(int rank, const int64_t *out_shape, const int64_t *in_strides, int64_t in_offset,
+                             const mm_c128 *in, mm_c128 *out, mm_stream_t stream);
+/* out[r] = sum_j in[r * inner + j] (a label summed inside one operand). */
+MM_API int mm_tensor_sum_inner(int64_t rows, int64_t inner, const mm_c128 *in, mm_c128 *out, mm_stream_t stream);
+/*
+ * C[z] = A[z] @ B[z] for z < batch, row-major M x K, K x N, M x N blocks at element strides
+ * strideA / strideB / strideC; FP64 arithmetic (GEMV kernels when N == 1 or M == 1; zeros when K == 0).
+ */
+MM_API int mm_zgemm_batched(int64_t batch, int64_t M, int64_t N, int64_t K, const mm_c128 *A, int64_t strideA,
+                            const mm_c128 *B, int64_t strideB, mm_c128 *C, int64_t strideC, mm_stream_t stream);
+
 /* ------------------------------------------------------------- diagnostics */
 
 /*

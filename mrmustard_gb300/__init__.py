@@ -2,7 +2,8 @@
 
 The renormalised multidimensional Hermite recurrence (``vanilla`` / ``stable`` /
 batched / VJP), the Fock contraction after it, the autoshape cutoffs before it, and the binomial
-and diagonal (PNR / leftover-mode) strategies of the same recurrence, computed by
+and diagonal (PNR / leftover-mode) strategies of the same recurrence, and the general Fock-space
+einsum, computed by
 hand-written sm_103a CUDA
 kernels in ``libmm_gb300.so`` behind a C ABI (include/mm_gb300.h).  The Python layer mirrors
 the reference's interface for this path; it has no CPU compute path.
@@ -24,6 +25,7 @@ from .diagonal import (
     hermite_renormalized_diagonal,
     hermite_renormalized_diagonal_autograd,
 )
+from .einsum import contract, einsum
 from .fock import apply_unitary, fock_gemm
 from .hermite import (
     device_fwd,
@@ -64,6 +66,8 @@ __all__ = [
     "autotune",
     "binomial",
     "device_binomial",
+    "contract",
+    "einsum",
     "fast_diagonal",
     "grad_hermite_multidimensional_diagonal",
     "hermite_multidimensional_diagonal",

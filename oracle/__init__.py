@@ -353,6 +353,12 @@ def fock_gemm(U, B):
     return np.asarray(U, np.complex128) @ np.asarray(B, np.complex128)
 
 
+def einsum(subscripts, *operands):
+    """FP64 CPU oracle of the Fock einsum: numpy's einsum with a contraction path (BLAS underneath),
+    as math.einsum reaches opt_einsum (mrmustard/math/backend_manager.py:526-548)."""
+    return np.einsum(subscripts, *[np.asarray(x, np.complex128) for x in operands], optimize=True)
+
+
 def rel_err(x, ref) -> float:
     """max|x - ref| / max|ref| (the per-instance error metric used throughout the tests)."""
     x, ref = np.asarray(x), np.asarray(ref)

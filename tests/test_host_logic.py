@@ -41,3 +41,24 @@ def test_shard_balances_cost():
     loads = [costs[p].sum() for p in parts]
     assert max(loads) - min(loads) <= costs.max()
     assert shard.shard_instances(costs, 1)[0] == list(range(500))
+
+
+def test_einsum_subscript_parsing():
+    """Host-side planning of the Fock einsum: explicit and implicit outputs (numpy's rule: labels
+    seen once, sorted), errors for unknown/repeated output labels and ellipses."""
+    from mrmustard_gb300.einsum import parse_subscripts
+
+    assert parse_subscripts("ab,bc->ac", 2) == ([["a", "b"], ["b", "c"]], ["a", "c"])
+    assert parse_subscripts("ba,cb", 2) == ([["b", "a"], ["c", "b"]], ["a", "c"])
+    assert parse_subscripts("aa", 1) == ([["a", "a"]], [])
+    assert parse_subscripts(" a b , b c -> c a ", 2) == ([["a", "b"], ["b", "c"]], ["c", "a"])
+    import pytest
+
+    with pytest.raises(ValueError):
+        parse_subscripts("ab->ad", 1)
+    with pytest.raises(ValueError):
+        parse_subscripts("ab->aa", 1)
+    with pytest.raises(ValueError):
+        parse_subscripts("...a->a", 1)
+    with pytest.raises(ValueError):
+        parse_subscripts("ab,bc->ac", 3)
