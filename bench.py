@@ -448,6 +448,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
                                         with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
     extras["binomial"] = run_binomial(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
     extras["diagonal"] = run_diagonal(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
+    extras["einsum"] = run_einsum(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
 
     extras["fock_contraction"] = run_contraction(dev, time_eager)
     return e2e_ms, h2d, d2h, plain_value, cpu, extras
@@ -650,6 +651,50 @@ def run_diagonal(dev, time_eager, with_cpu=True):
     return res
 
 
+def run_einsum(dev, time_eager, with_cpu=True):
+    """Fock-space einsum: a 2-mode gate at cutoff 40 applied to 64 two-mode kets
+    ('abcd,zcd->zab', a 1600 x 1600 x 64 complex GEMM plus the permutations of kets and result), and
+    the ket0 / beamsplitter / ket1 network of mm_einsum's docstring at cutoff 60 ('a,cdab,b->cd', a
+    207 MB gate read once: HBM-bound), GPU time per call (device tensors) against numpy einsum on the
+    host cores (the reference's math.einsum is opt_einsum -> BLAS)."""
+    import torch
+
+    import mrmustard_gb300 as mm
+
+    rng = np.random.default_rng(9090)
+
+    def cn(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    res = {}
+    cases = (("gate40_on_64kets", "abcd,zcd->zab", (cn(40, 40, 40, 40) / 1600, cn(64, 40, 40)),
+              8.0 * 1600 * 1600 * 64, None),
+             ("bs60_network", "a,cdab,b->cd", (cn(60), cn(60, 60, 60, 60) / 3600, cn(60)), None, 16.0 * 60 ** 4))
+    for name, sub, ops, flops, nbytes in cases:
+        dops = [torch.as_tensor(x, device=dev) for x in ops]
+        t = time_eager(lambda: mm.einsum(sub, *dops), reps=10)
+        got = mm.einsum(sub, *dops).cpu().numpy()
+        r = {"subscripts": sub, "shapes": [list(x.shape) for x in ops], "ms": t}
+        if flops:
+            r["fp64_tflops"] = flops / (t * 1e-3) / 1e12
+        if nbytes:
+            r["gate_read_gbs"] = nbytes / (t * 1e-3) / 1e9
+        if name.startswith("gate"):
+            tz = time_eager(lambda: mm.einsum(sub, *dops, mode="ozaki"), reps=10)
+            r["ozaki_ms"] = tz
+        if with_cpu:
+            import oracle
+
+            t0 = time.perf_counter()
+            ref = oracle.einsum(sub, *ops)
+            tc = time.perf_counter() - t0
+            r["cpu_baseline"] = {"value": tc * 1e3, "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+                                 "sample": "numpy einsum (BLAS) of the same operands, one pass",
+                                 "max_rel_err_vs_gpu": oracle.rel_err(got, ref)}
+        res[name] = r
+    return res
+
+
 def run_single(dev, time_eager, dfma_peak=None):
     """Single large recurrences on the whole GPU (4 modes at cutoff 40, pure state; 4-index
     density-matrix triple at cutoff 50), timed with CUDA events; HBM and FP64-pipe fractions."""
@@ -754,6 +799,8 @@ def main(argv=None):
                     help="run only the Fock-contraction leg (gate tensor on 256 kets) and print its figures")
     ap.add_argument("--only-binomial", action="store_true",
                     help="run only the binomial fill of a 4-mode state at cutoff 30 (GPU and CPU oracle)")
+    ap.add_argument("--only-einsum", action="store_true",
+                    help="run only the Fock-space einsum cases (GPU and numpy on the host)")
     ap.add_argument("--only-diagonal", action="store_true",
                     help="run only the diagonal strategies (PNR amplitudes, Jacobians, fast_diagonal; GPU and CPU oracle)")
     ap.add_argument("--only-autoshape", action="store_true",
@@ -765,7 +812,8 @@ def main(argv=None):
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()
-    if args.only_contraction or args.only_single or args.only_autoshape or args.only_binomial or args.only_diagonal:
+    if (args.only_contraction or args.only_single or args.only_autoshape or args.only_binomial or args.only_diagonal
+            or args.only_einsum):
         import torch
 
         dev = torch.device("cuda", local_rank)
@@ -782,7 +830,9 @@ def main(argv=None):
             torch.cuda.synchronize()
             return e0.elapsed_time(e1) / reps
 
-        if args.only_diagonal:
+        if args.only_einsum:
+            print(json.dumps({"einsum": run_einsum(dev, time_eager, not args.skip_cpu)}), flush=True)
+        elif args.only_diagonal:
             print(json.dumps({"diagonal": run_diagonal(dev, time_eager, not args.skip_cpu)}), flush=True)
         elif args.only_binomial:
             print(json.dumps({"binomial": run_binomial(dev, time_eager, not args.skip_cpu)}), flush=True)

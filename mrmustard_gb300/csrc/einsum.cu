@@ -21,7 +21,8 @@
 //   permute_tile_kernel   32 x 32 shared-memory tiles between the input's contiguous axis and
 //                         the output's innermost axis (both accesses coalesced);
 //   sum_inner_kernel      one warp per row, fixed-order shuffle reduction;
-//   zgemm_batched_kernel  32 x 32 x 16 tiles, 2 x 2 outputs per thread, batch in grid.z;
+//   zgemm_batched_kernel  32 x 32 (2 x 2 outputs per thread) or 16 x 16 (1 x 1) tiles over 16-deep
+//                         K slabs, batch in grid.z;
 //   zgemv_rows_kernel     y = A x (N = 1): one warp per row of A;
 //   zgemv_cols_kernel     y = x B (M = 1): one thread per column of B.
 #include <algorithm>
@@ -143,54 +144,62 @@ __global__ void __launch_bounds__(256) sum_inner_kernel(int64_t rows, int64_t in
 }
 
 // ---------------------------------------------------------------- batched GEMM
-constexpr int BG_BM = 32, BG_BN = 32, BG_BK = 16;
+// BM x BN tiles over 16-deep K slabs, 256 threads, each TM x TN outputs (32 x 32 with 2 x 2,
+// or 16 x 16 with 1 x 1 when the 32 x 32 grid would leave SMs idle: FP64 throughput per SM
+// is the bound, so the number of CTAs in flight is what matters).
+constexpr int BG_BK = 16;
 
+template <int BM, int BN>
 __global__ void __launch_bounds__(256) zgemm_batched_kernel(const double2* __restrict__ A, int64_t sA,
                                                             const double2* __restrict__ B, int64_t sB,
                                                             double2* __restrict__ C, int64_t sC, int64_t batch,
                                                             int M, int N, int K) {
-  __shared__ double2 As[BG_BK][BG_BM];
-  __shared__ double2 Bs[BG_BK][BG_BN];
+  constexpr int TM = BM / 16, TN = BN / 16;
+  __shared__ double2 As[BG_BK][BM];
+  __shared__ double2 Bs[BG_BK][BN];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  const int m0 = blockIdx.y * BG_BM, n0 = blockIdx.x * BG_BN;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   for (int64_t z = blockIdx.z; z < batch; z += gridDim.z) {
     const double2* Az = A + z * sA;
     const double2* Bz = B + z * sB;
-    double2 acc[2][2];
+    double2 acc[TM][TN];
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-      for (int j = 0; j < 2; ++j) acc[i][j] = cmk(0.0, 0.0);
+      for (int j = 0; j < TN; ++j) acc[i][j] = cmk(0.0, 0.0);
     for (int k0 = 0; k0 < K; k0 += BG_BK) {
-#pragma unroll
-      for (int rr = 0; rr < 2; ++rr) {
-        const int idx = tid + rr * 256;
+      for (int idx = tid; idx < BG_BK * BM; idx += 256) {
         const int row = idx / BG_BK, kk = idx % BG_BK;
         const int gm = m0 + row, gk = k0 + kk;
         As[kk][row] = (gm < M && gk < K) ? __ldg(Az + (int64_t)gm * K + gk) : cmk(0.0, 0.0);
-        const int kx = idx / BG_BN, col = idx % BG_BN;
+      }
+      for (int idx = tid; idx < BG_BK * BN; idx += 256) {
+        const int kx = idx / BN, col = idx % BN;
         const int gk2 = k0 + kx, gn = n0 + col;
         Bs[kx][col] = (gk2 < K && gn < N) ? __ldg(Bz + (int64_t)gk2 * N + gn) : cmk(0.0, 0.0);
       }
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < BG_BK; ++kk) {
-        const double2 a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
-        const double2 b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
-        acc[0][0] = cfma(a0, b0, acc[0][0]);
-        acc[0][1] = cfma(a0, b1, acc[0][1]);
-        acc[1][0] = cfma(a1, b0, acc[1][0]);
-        acc[1][1] = cfma(a1, b1, acc[1][1]);
+        double2 a[TM], b[TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) a[i] = As[kk][ty * TM + i];
+#pragma unroll
+        for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx * TN + j];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
       }
       __syncthreads();
     }
     double2* Cz = C + z * sC;
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int gm = m0 + ty * 2 + i, gn = n0 + tx * 2 + j;
+      for (int j = 0; j < TN; ++j) {
+        const int gm = m0 + ty * TM + i, gn = n0 + tx * TN + j;
         if (gm < M && gn < N) Cz[(int64_t)gm * N + gn] = acc[i][j];
       }
   }
@@ -330,11 +339,18 @@ MM_API int mm_zgemm_batched(int64_t batch, int64_t M, int64_t N, int64_t K, cons
     zgemv_cols_kernel<<<blocks_for(batch * N, 256, sms), 256, 0, st>>>((const double2*)A, strideA, (const double2*)B,
                                                                        strideB, (double2*)C, strideC, batch, N, K);
   } else {
-    const int64_t gy = (M + BG_BM - 1) / BG_BM;
+    const int64_t tiles32 = ((M + 31) / 32) * ((N + 31) / 32) * batch;
+    const bool small = tiles32 < 2 * (int64_t)sms;
+    const int bm = small ? 16 : 32, bn = bm;
+    const int64_t gy = (M + bm - 1) / bm;
     if (gy > 65535) return MM_ERR_TOO_LARGE;
-    dim3 grid((unsigned)((N + BG_BN - 1) / BG_BN), (unsigned)gy, (unsigned)std::min<int64_t>(batch, 65535));
-    zgemm_batched_kernel<<<grid, 256, 0, st>>>((const double2*)A, strideA, (const double2*)B, strideB, (double2*)C,
-                                              strideC, batch, (int)M, (int)N, (int)K);
+    dim3 grid((unsigned)((N + bn - 1) / bn), (unsigned)gy, (unsigned)std::min<int64_t>(batch, 65535));
+    if (small)
+      zgemm_batched_kernel<16, 16><<<grid, 256, 0, st>>>((const double2*)A, strideA, (const double2*)B, strideB,
+                                                         (double2*)C, strideC, batch, (int)M, (int)N, (int)K);
+    else
+      zgemm_batched_kernel<32, 32><<<grid, 256, 0, st>>>((const double2*)A, strideA, (const double2*)B, strideB,
+                                                         (double2*)C, strideC, batch, (int)M, (int)N, (int)K);
   }
   mm::note_launches(1);
   return status();
