@@ -84,6 +84,10 @@ def lib():
         L.oracle_diagonal_slots.restype = I64
         L.oracle_fast_diagonal.argtypes = [I32, P, I64, P, P, P, I32, P]
         L.oracle_fast_diagonal.restype = ctypes.c_int
+        L.oracle_leftover_amps.argtypes = [I32, P, P, P, P, P]
+        L.oracle_leftover_amps.restype = ctypes.c_int
+        L.oracle_leftover_grad.argtypes = [I32, P, P, P, P, P]
+        L.oracle_leftover_grad.restype = ctypes.c_int
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_set_numpy_division.argtypes = [ctypes.c_int]
         L.oracle_set_numpy_division.restype = None
@@ -346,6 +350,67 @@ def fast_diagonal(A, b, c, output_cutoff, pnr_cutoffs, stable=False):
     if lib().oracle_fast_diagonal(L, _ptr(sh), oc, _ptr(A), _ptr(b), _ptr(cc), int(bool(stable)), _ptr(out)):
         raise ValueError("bad arguments")
     return out
+
+
+def leftover_split(W, M, cutoffs):
+    """Slot buffer [slot][m][n][P'] of the leftover strategy -> the reference's (arr0, arr2, arr1010,
+    arr1001, arr1) with the block axes first (singleLeftoverMode_amps.py:385-408)."""
+    q, tail = int(cutoffs[0]), tuple(int(c) for c in cutoffs[1:])
+    Mt = M - 1
+    W = np.asarray(W).reshape(-1, q, q, *tail)
+    mv = lambda x: np.moveaxis(x, 0, 2)  # (k, q, q, *tail) -> (q, q, k, *tail)
+    arr0 = W[0]
+    arr2 = mv(W[1:1 + Mt])
+    o = 1 + Mt
+    if Mt == 1:
+        arr1010 = np.zeros((1, 1, 1, 1, 1), np.complex128)
+        arr1001 = np.zeros((1, 1, 1, 1, 1), np.complex128)
+    else:
+        k = Mt * (Mt - 1)
+        arr1010 = mv(W[o:o + k]).reshape((q, q, Mt, Mt - 1) + tail)
+        arr1001 = mv(W[o + k:o + 2 * k]).reshape((q, q, Mt, Mt - 1) + tail)
+    o += 2 * Mt * (Mt - 1)
+    arr1 = mv(W[o:o + 2 * Mt])
+    return arr0, arr2, arr1010, arr1001, arr1
+
+
+def leftover_amps(A, B, G0, cutoffs, slots=False):
+    """``hermite_multidimensional_1leftoverMode(A, B, G0, cutoffs)`` (compactFock/inputValidation.py:103-119,
+    singleLeftoverMode_amps.py:385-421) on A, B in the interleaved order; cutoffs[0] is the leftover
+    mode's cutoff -> (arr0, arr2, arr1010, arr1001, arr1)."""
+    A, B = _cc(A), _cc(B)
+    cut = tuple(int(x) for x in cutoffs)
+    M = len(cut)
+    q = cut[0]
+    P = int(np.prod(cut[1:]))
+    W = np.empty(int(lib().oracle_diagonal_slots(M - 1)) * q * q * P, np.complex128)
+    g0 = np.array([complex(np.asarray(G0).reshape(-1)[0])], np.complex128)
+    sh = np.array(cut, np.int64)
+    if lib().oracle_leftover_amps(M, _ptr(sh), _ptr(A), _ptr(B), _ptr(g0), _ptr(W)):
+        raise ValueError("bad arguments")
+    return W if slots else leftover_split(W, M, cut)
+
+
+def leftover_grad(A, B, G0, cutoffs):
+    """``grad_hermite_multidimensional_1leftoverMode`` (inputValidation.py:122-142,
+    singleLeftoverMode_grad.py:571-724) -> (arr0_dG0, arr0_dA, arr0_dB) with shapes
+    (q, q, *tail), (q, q, *tail, 2M, 2M), (q, q, *tail, 2M).  Runs the forward pass itself."""
+    A, B = _cc(A), _cc(B)
+    cut = tuple(int(x) for x in cutoffs)
+    M = len(cut)
+    q, tail = cut[0], cut[1:]
+    W = leftover_amps(A, B, G0, cut, slots=True)
+    n = 2 * M
+    nc = n * n + n
+    J = np.empty(W.size * nc, np.complex128)
+    sh = np.array(cut, np.int64)
+    if lib().oracle_leftover_grad(M, _ptr(sh), _ptr(A), _ptr(B), _ptr(W), _ptr(J)):
+        raise ValueError("bad arguments")
+    P = int(np.prod(tail))
+    J0 = J[:q * q * P * nc].reshape((q, q) + tail + (nc,))
+    arr0 = W[:q * q * P].reshape((q, q) + tail)
+    dG0 = (arr0 / np.complex128(np.asarray(G0).reshape(-1)[0])).astype(np.complex128)
+    return dG0, J0[..., :n * n].reshape((q, q) + tail + (n, n)), J0[..., n * n:]
 
 
 def fock_gemm(U, B):

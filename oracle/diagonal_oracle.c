@@ -479,3 +479,304 @@ int oracle_fast_diagonal(int Lm, const int64_t *pnr, int64_t oc, const cplx *A_i
   free(G);
   return 0;
 }
+
+/* --------------------------------------------- 4. leftover mode (compactFock) */
+
+/*
+ * fock_representation_1leftoverMode_amps (compactFock/singleLeftoverMode_amps.py:18-421) and
+ * its Jacobians (singleLeftoverMode_grad.py:18-724), reached through
+ * hermite_multidimensional_1leftoverMode / grad_hermite_multidimensional_1leftoverMode
+ * (compactFock/inputValidation.py:103-142).  M modes: mode 0 is left over (block q x q,
+ * q = cutoffs[0]), modes 1..M-1 (M' = M - 1 of them) are detected, with the params lattice of
+ * the diagonal strategy over cutoffs[1..].  A (2M x 2M) and B (2M) in the interleaved order.
+ * Storage: W[slot][m][n][P'] with the diagonal strategy's slot numbering over the M' detected
+ * modes; J[slot][m][n][P'][4M^2 + 2M].
+ */
+typedef struct {
+  Lat t;     /* the detected modes' lattice (M' modes) */
+  int M;     /* all modes */
+  int64_t q; /* leftover cutoff */
+} LoLat;
+
+#define LW(slot, m, n, f) W[(((slot) * L->q + (m)) * L->q + (n)) * L->t.P + (f)]
+#define LJ(slot, m, n, f) (J + ((((slot) * L->q + (m)) * L->q + (n)) * L->t.P + (f)) * nc)
+
+/* one block entry of write_block (singleLeftoverMode_amps.py:20-75): row `row` of A (full
+ * index), the pivot block `ps` at params f, the scaled inputs Gin[l] (2M' of them) */
+static cplx lo_entry(const LoLat *L, const cplx *A, const cplx *B, int row, int64_t ps, int64_t f, int64_t m,
+                     int64_t n, const cplx *Gin, double Ki, const cplx *W) {
+  const int N = 2 * L->M;
+  cplx dot = 0.0;
+  if (m > 0) dot = dadd(dot, dmul(A[row * N + 0], dmulr(LW(ps, m - 1, n, f), SQ(m))));
+  if (n > 0) dot = dadd(dot, dmul(A[row * N + 1], dmulr(LW(ps, m, n - 1, f), SQ(n))));
+  for (int l = 0; l < N - 2; ++l) dot = dadd(dot, dmul(A[row * N + 2 + l], Gin[l]));
+  const cplx GB = dmul(LW(ps, m, n, f), B[row]);
+  return ddivr(dadd(GB, dot), Ki);
+}
+
+static void lo_first_fill(const LoLat *L, const cplx *A, const cplx *B, cplx *W) {
+  /* singleLeftoverMode_amps.py:339-352: the leftover mode with every detected mode at 0 */
+  const int N = 2 * L->M;
+  const int64_t q = L->q;
+  for (int64_t m = 0; m + 1 < q; ++m) {
+    const cplx prev = m >= 1 ? LW(0, m - 1, 0, 0) : LW(0, q - 1, 0, 0); /* index -1 wraps (times sqrt(0)) */
+    LW(0, m + 1, 0, 0) = ddivr(dadd(dmul(LW(0, m, 0, 0), B[0]), dmul(dmulr(A[0], SQ(m)), prev)), SQ(m + 1));
+  }
+  for (int64_t m = 0; m < q; ++m)
+    for (int64_t n = 0; n + 1 < q; ++n) {
+      const cplx up = m >= 1 ? LW(0, m - 1, n, 0) : LW(0, q - 1, n, 0);
+      const cplx left = n >= 1 ? LW(0, m, n - 1, 0) : LW(0, m, q - 1, 0);
+      cplx v = dmul(LW(0, m, n, 0), B[1]);
+      v = dadd(v, dmul(dmulr(A[N + 0], SQ(m)), up));
+      v = dadd(v, dmul(dmulr(A[N + 1], SQ(n)), left));
+      LW(0, m, n + 1, 0) = ddivr(v, SQ(n + 1));
+    }
+}
+
+int64_t oracle_leftover_slots(int M) { return oracle_diagonal_slots(M - 1); }
+
+int oracle_leftover_amps(int M, const int64_t *cutoffs, const cplx *A, const cplx *B, const cplx *G0, cplx *W) {
+  if (M < 2) return 1;
+  LoLat Ls, *L = &Ls;
+  if (lat_init(&L->t, M - 1, cutoffs + 1, 1)) return 1;
+  L->M = M;
+  L->q = cutoffs[0];
+  if (L->q < 1) return 1;
+  const int Mt = M - 1, nt = 2 * Mt;
+  const int64_t S = oracle_diagonal_slots(Mt);
+  memset(W, 0, (size_t)(S * L->q * L->q * L->t.P) * sizeof(cplx));
+  LW(0, 0, 0, 0) = *G0;
+  lo_first_fill(L, A, B, W);
+  int64_t nw;
+  int64_t *order = params_by_weight(&L->t, &nw);
+  int64_t p[DG_MAXM];
+  cplx Gin[2 * DG_MAXM];
+  for (int64_t t = 0; t < L->t.P; ++t) {
+    const int64_t f = order[t];
+    int64_t r = f;
+    for (int k = 0; k < Mt; ++k) {
+      p[k] = r / L->t.st[k];
+      r %= L->t.st[k];
+    }
+    /* use_diag_pivot (singleLeftoverMode_amps.py:213-284) */
+    if (L->t.c[0] == 1 || p[0] < L->t.c[0] - 1) {
+      for (int64_t m = 0; m < L->q; ++m)
+        for (int64_t n = 0; n < L->q; ++n) {
+          for (int i = 0; i < nt; ++i) {
+            Gin[i] = 0.0;
+            if (p[i / 2] > 0) Gin[i] = LW(slot_arr1(&L->t, i + 1 - 2 * (i % 2)), m, n, f - L->t.st[i / 2]);
+            Gin[i] = dmulr(Gin[i], SQ(p[i / 2]));
+          }
+          for (int i = 0; i < nt; ++i)
+            if (p[i / 2] + 1 < L->t.c[i / 2] && (i != 1 || p[0] + 2 < L->t.c[0]))
+              LW(slot_arr1(&L->t, i), m, n, f) = lo_entry(L, A, B, i + 2, 0, f, m, n, Gin, SQ(p[i / 2] + 1), W);
+        }
+    }
+    /* use_offDiag_pivot (singleLeftoverMode_amps.py:101-210) */
+    for (int d = 0; d < Mt; ++d) {
+      int lower_zero = 1;
+      for (int k = 0; k < d; ++k) lower_zero &= (p[k] == 0);
+      if (!(lower_zero && p[d] < L->t.c[d] - 1)) continue;
+      double Kl[2 * DG_MAXM], Ki[2 * DG_MAXM];
+      for (int k = 0; k < Mt; ++k) {
+        Kl[2 * k] = SQ(p[k] + (k == d));
+        Kl[2 * k + 1] = SQ(p[k]);
+        Ki[2 * k] = SQ(p[k] + (k == d) + 1);
+        Ki[2 * k + 1] = SQ(p[k] + 1);
+      }
+      const int64_t ps = slot_arr1(&L->t, 2 * d);
+      for (int64_t m = 0; m < L->q; ++m)
+        for (int64_t n = 0; n < L->q; ++n) {
+          for (int i = 0; i < nt; ++i) Gin[i] = 0.0;
+          Gin[2 * d] = LW(0, m, n, f);
+          if (p[d] > 0) Gin[2 * d + 1] = LW(slot_arr2(&L->t, d), m, n, f - L->t.st[d]);
+          for (int i = d + 1; i < Mt; ++i)
+            if (p[i] > 0) {
+              Gin[2 * i] = LW(slot_1001(&L->t, d, i - d - 1), m, n, f - L->t.st[i]);
+              Gin[2 * i + 1] = LW(slot_1010(&L->t, d, i - d - 1), m, n, f - L->t.st[i]);
+            }
+          for (int i = 0; i < nt; ++i) Gin[i] = dmulr(Gin[i], Kl[i]);
+          LW(0, m, n, f + L->t.st[d]) = lo_entry(L, A, B, 2 * d + 3, ps, f, m, n, Gin, Ki[2 * d + 1], W);
+          if (p[d] + 2 < L->t.c[d])
+            LW(slot_arr2(&L->t, d), m, n, f) = lo_entry(L, A, B, 2 * d + 2, ps, f, m, n, Gin, Ki[2 * d], W);
+          for (int i = d + 1; i < Mt; ++i)
+            if (p[i] + 1 < L->t.c[i]) {
+              LW(slot_1010(&L->t, d, i - d - 1), m, n, f) = lo_entry(L, A, B, 2 * i + 2, ps, f, m, n, Gin, Ki[2 * i], W);
+              LW(slot_1001(&L->t, d, i - d - 1), m, n, f) =
+                  lo_entry(L, A, B, 2 * i + 3, ps, f, m, n, Gin, Ki[2 * i + 1], W);
+            }
+        }
+    }
+  }
+  free(order);
+  return 0;
+}
+
+/* calc_dA_dB of the leftover strategy (singleLeftoverMode_grad.py:18-46) for block entry (m, n):
+ * terms l = 0 (m > 0: pivot (m-1, n), K = sqrt(m)), l = 1 (n > 0: pivot (m, n-1), K = sqrt(n)),
+ * l = 2 .. 2M-1 (input l - 2, K = Kl[l - 2]); Jacobian rows of nc entries. */
+static void lo_jac_entry(const LoLat *L, const cplx *A, const cplx *B, int row, int64_t ps, int64_t f, int64_t m,
+                         int64_t n, const cplx *Gin_scaled, const cplx *const *Jin, const double *Kl, double Ki,
+                         const cplx *W, cplx *J, cplx *out) {
+  const int N = 2 * L->M, nA = N * N;
+  const int64_t nc = (int64_t)nA + N;
+  int nterm = 0;
+  int ls[2 * DG_MAXM + 2];
+  double Ks[2 * DG_MAXM + 2];
+  cplx Gs[2 * DG_MAXM + 2];
+  const cplx *Js[2 * DG_MAXM + 2];
+  if (m > 0) {
+    ls[nterm] = 0;
+    Ks[nterm] = SQ(m);
+    Gs[nterm] = dmulr(LW(ps, m - 1, n, f), SQ(m));
+    Js[nterm++] = LJ(ps, m - 1, n, f);
+  }
+  if (n > 0) {
+    ls[nterm] = 1;
+    Ks[nterm] = SQ(n);
+    Gs[nterm] = dmulr(LW(ps, m, n - 1, f), SQ(n));
+    Js[nterm++] = LJ(ps, m, n - 1, f);
+  }
+  for (int l = 0; l < N - 2; ++l) {
+    ls[nterm] = l + 2;
+    Ks[nterm] = Kl[l];
+    Gs[nterm] = Gin_scaled[l];
+    Js[nterm++] = Jin[l];
+  }
+  const cplx *Jp = LJ(ps, m, n, f);
+  for (int64_t qd = 0; qd < nA; ++qd) {
+    cplx acc = dmul(Jp[qd], B[row]);
+    for (int t = 0; t < nterm; ++t) {
+      acc = dadd(acc, dmul(dmulr(A[row * N + ls[t]], Ks[t]), Js[t] ? Js[t][qd] : 0.0));
+      if (qd == (int64_t)row * N + ls[t]) acc = dadd(acc, Gs[t]);
+    }
+    out[qd] = ddivr(acc, Ki);
+  }
+  for (int r = 0; r < N; ++r) {
+    cplx acc = dmul(Jp[nA + r], B[row]);
+    if (r == row) acc = dadd(acc, LW(ps, m, n, f));
+    for (int t = 0; t < nterm; ++t) acc = dadd(acc, dmul(dmulr(A[row * N + ls[t]], Ks[t]), Js[t] ? Js[t][nA + r] : 0.0));
+    out[nA + r] = ddivr(acc, Ki);
+  }
+}
+
+int oracle_leftover_grad(int M, const int64_t *cutoffs, const cplx *A, const cplx *B, const cplx *W, cplx *J) {
+  if (M < 2) return 1;
+  LoLat Ls, *L = &Ls;
+  if (lat_init(&L->t, M - 1, cutoffs + 1, 1)) return 1;
+  L->M = M;
+  L->q = cutoffs[0];
+  const int Mt = M - 1, nt = 2 * Mt, N = 2 * M, nA = N * N;
+  const int64_t nc = (int64_t)nA + N, q = L->q;
+  const int64_t S = oracle_diagonal_slots(Mt);
+  memset(J, 0, (size_t)(S * q * q * L->t.P * nc) * sizeof(cplx));
+  /* first fill (singleLeftoverMode_grad.py:606-650) */
+  for (int64_t m = 0; m + 1 < q; ++m) {
+    cplx *dst = LJ(0, m + 1, 0, 0);
+    const cplx *cur = LJ(0, m, 0, 0), *prev = m >= 1 ? LJ(0, m - 1, 0, 0) : LJ(0, q - 1, 0, 0);
+    const cplx vprev = m >= 1 ? LW(0, m - 1, 0, 0) : LW(0, q - 1, 0, 0);
+    for (int64_t c = 0; c < nc; ++c)
+      dst[c] = ddivr_np(dadd(dmul(cur[c], B[0]), dmul(dmulr(A[0], SQ(m)), prev[c])), SQ(m + 1));
+    dst[0] = dadd(dst[0], ddivr_np(dmulr(vprev, SQ(m)), SQ(m + 1)));
+    dst[nA + 0] = dadd(dst[nA + 0], ddivr_np(LW(0, m, 0, 0), SQ(m + 1)));
+  }
+  for (int64_t m = 0; m < q; ++m)
+    for (int64_t n = 0; n + 1 < q; ++n) {
+      cplx *dst = LJ(0, m, n + 1, 0);
+      const cplx *cur = LJ(0, m, n, 0);
+      const cplx *up = m >= 1 ? LJ(0, m - 1, n, 0) : LJ(0, q - 1, n, 0);
+      const cplx *left = n >= 1 ? LJ(0, m, n - 1, 0) : LJ(0, m, q - 1, 0);
+      const cplx vup = m >= 1 ? LW(0, m - 1, n, 0) : LW(0, q - 1, n, 0);
+      const cplx vleft = n >= 1 ? LW(0, m, n - 1, 0) : LW(0, m, q - 1, 0);
+      for (int64_t c = 0; c < nc; ++c) {
+        cplx v = dmul(cur[c], B[1]);
+        v = dadd(v, dmul(dmulr(A[N + 0], SQ(m)), up[c]));
+        v = dadd(v, dmul(dmulr(A[N + 1], SQ(n)), left[c]));
+        dst[c] = ddivr_np(v, SQ(n + 1));
+      }
+      dst[N + 0] = dadd(dst[N + 0], ddivr_np(dmulr(vup, SQ(m)), SQ(n + 1)));
+      dst[N + 1] = dadd(dst[N + 1], ddivr_np(dmulr(vleft, SQ(n)), SQ(n + 1)));
+      dst[nA + 1] = dadd(dst[nA + 1], ddivr_np(LW(0, m, n, 0), SQ(n + 1)));
+    }
+  int64_t nw;
+  int64_t *order = params_by_weight(&L->t, &nw);
+  int64_t p[DG_MAXM];
+  cplx Gin[2 * DG_MAXM];
+  const cplx *Jin[2 * DG_MAXM];
+  double Kl[2 * DG_MAXM], Ki[2 * DG_MAXM];
+  for (int64_t t = 0; t < L->t.P; ++t) {
+    const int64_t f = order[t];
+    int64_t r = f;
+    for (int k = 0; k < Mt; ++k) {
+      p[k] = r / L->t.st[k];
+      r %= L->t.st[k];
+    }
+    if (L->t.c[0] == 1 || p[0] < L->t.c[0] - 1) {
+      for (int i = 0; i < nt; ++i) Kl[i] = SQ(p[i / 2]);
+      for (int64_t m = 0; m < q; ++m)
+        for (int64_t n = 0; n < q; ++n) {
+          for (int i = 0; i < nt; ++i) {
+            Gin[i] = 0.0;
+            Jin[i] = NULL;
+            if (p[i / 2] > 0) {
+              const int64_t s = slot_arr1(&L->t, i + 1 - 2 * (i % 2));
+              Gin[i] = LW(s, m, n, f - L->t.st[i / 2]);
+              Jin[i] = LJ(s, m, n, f - L->t.st[i / 2]);
+            }
+            Gin[i] = dmulr(Gin[i], Kl[i]);
+          }
+          for (int i = 0; i < nt; ++i)
+            if (p[i / 2] + 1 < L->t.c[i / 2] && (i != 1 || p[0] + 2 < L->t.c[0]))
+              lo_jac_entry(L, A, B, i + 2, 0, f, m, n, Gin, Jin, Kl, SQ(p[i / 2] + 1), W, J,
+                           LJ(slot_arr1(&L->t, i), m, n, f));
+        }
+    }
+    for (int d = 0; d < Mt; ++d) {
+      int lower_zero = 1;
+      for (int k = 0; k < d; ++k) lower_zero &= (p[k] == 0);
+      if (!(lower_zero && p[d] < L->t.c[d] - 1)) continue;
+      for (int k = 0; k < Mt; ++k) {
+        Kl[2 * k] = SQ(p[k] + (k == d));
+        Kl[2 * k + 1] = SQ(p[k]);
+        Ki[2 * k] = SQ(p[k] + (k == d) + 1);
+        Ki[2 * k + 1] = SQ(p[k] + 1);
+      }
+      const int64_t ps = slot_arr1(&L->t, 2 * d);
+      for (int64_t m = 0; m < q; ++m)
+        for (int64_t n = 0; n < q; ++n) {
+          for (int i = 0; i < nt; ++i) {
+            Gin[i] = 0.0;
+            Jin[i] = NULL;
+          }
+          Gin[2 * d] = LW(0, m, n, f);
+          Jin[2 * d] = LJ(0, m, n, f);
+          if (p[d] > 0) {
+            Gin[2 * d + 1] = LW(slot_arr2(&L->t, d), m, n, f - L->t.st[d]);
+            Jin[2 * d + 1] = LJ(slot_arr2(&L->t, d), m, n, f - L->t.st[d]);
+          }
+          for (int i = d + 1; i < Mt; ++i)
+            if (p[i] > 0) {
+              Gin[2 * i] = LW(slot_1001(&L->t, d, i - d - 1), m, n, f - L->t.st[i]);
+              Jin[2 * i] = LJ(slot_1001(&L->t, d, i - d - 1), m, n, f - L->t.st[i]);
+              Gin[2 * i + 1] = LW(slot_1010(&L->t, d, i - d - 1), m, n, f - L->t.st[i]);
+              Jin[2 * i + 1] = LJ(slot_1010(&L->t, d, i - d - 1), m, n, f - L->t.st[i]);
+            }
+          for (int i = 0; i < nt; ++i) Gin[i] = dmulr(Gin[i], Kl[i]);
+          lo_jac_entry(L, A, B, 2 * d + 3, ps, f, m, n, Gin, Jin, Kl, Ki[2 * d + 1], W, J, LJ(0, m, n, f + L->t.st[d]));
+          if (p[d] + 2 < L->t.c[d])
+            lo_jac_entry(L, A, B, 2 * d + 2, ps, f, m, n, Gin, Jin, Kl, Ki[2 * d], W, J, LJ(slot_arr2(&L->t, d), m, n, f));
+          for (int i = d + 1; i < Mt; ++i)
+            if (p[i] + 1 < L->t.c[i]) {
+              lo_jac_entry(L, A, B, 2 * i + 2, ps, f, m, n, Gin, Jin, Kl, Ki[2 * i], W, J,
+                           LJ(slot_1010(&L->t, d, i - d - 1), m, n, f));
+              lo_jac_entry(L, A, B, 2 * i + 3, ps, f, m, n, Gin, Jin, Kl, Ki[2 * i + 1], W, J,
+                           LJ(slot_1001(&L->t, d, i - d - 1), m, n, f));
+            }
+        }
+    }
+  }
+  free(order);
+  return 0;
+}
+#undef LW
+#undef LJ

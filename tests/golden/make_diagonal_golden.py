@@ -9,6 +9,9 @@ singleLeftoverMode_amps,singleLeftoverMode_grad,helperFunctions}.py`` and
 * ``amps*``: ``hermite_multidimensional_diagonal(A, B, G0, cutoffs)`` -> (arr0, arr2, arr1010,
   arr1001, arr1) for M = 1..4, with and without a batch axis on B;
 * ``grad*``: ``grad_hermite_multidimensional_diagonal(A, B, G0, *amps)`` -> (dG0, dA, dB);
+* ``lo*``: ``hermite_multidimensional_1leftoverMode(A, B, G0, cutoffs)`` -> (arr0, arr2, arr1010,
+  arr1001, arr1) and ``grad_hermite_multidimensional_1leftoverMode`` -> (dG0, dA, dB), M = 2..4
+  (cutoffs[0] is the leftover mode's);
 * ``fd*``: ``fast_diagonal(A, b, c, output_cutoff, pnr_cutoffs, stable)``, L = 2..4, both
   variants, including the reference tests' shapes (tests/test_math/test_fast_diagonal.py:24-45)
   and an output cutoff of 0, where the reference's weight loop (fast_diagonal.py:70) stops
@@ -106,6 +109,14 @@ def main(ref_root: str):
         if not batch:
             g = iv.grad_hermite_multidimensional_diagonal(Ai, B, c, *r)
             put(f"grad{len(names)}", "grad", A=Ai, B=B, G0=c, cutoffs=np.array(cut), dG0=g[0], dA=g[1], dB=g[2])
+
+    for M, cut in ((2, (5, 6)), (3, (4, 3, 4)), (4, (3, 2, 3, 2)), (2, (1, 4)), (3, (4, 1, 3)), (2, (6, 1))):
+        A, b, c = dm_triple(M, 200 + 10 * M + len(names))
+        Ai, bi = interleave(A, b)
+        r = iv.hermite_multidimensional_1leftoverMode(Ai, bi, c, cut)
+        g = iv.grad_hermite_multidimensional_1leftoverMode(Ai, bi, c, *r)
+        put(f"lo{len(names)}", "lo", A=Ai, B=bi, G0=c, cutoffs=np.array(cut), arr0=r[0], arr2=r[1], arr1010=r[2],
+            arr1001=r[3], arr1=r[4], dG0=g[0], dA=g[1], dB=g[2])
 
     for L, oc, pnr, seed in ((2, 5, (10,), 1), (3, 3, (4, 5), 2), (2, 8, (3,), 3), (3, 4, (2, 2), 4),
                              (4, 2, (2, 1, 2), 5), (3, 0, (2, 2), 6), (2, 0, (3,), 7), (4, 1, (1, 1, 1), 8)):

@@ -283,3 +283,48 @@ def test_fast_diagonal_equals_vanilla_block(diagonal_golden):
         for q in np.ndindex(*(p + 1 for p in pnr)):
             ref = G[(slice(None), *q, slice(None), *q)]
             assert np.allclose(fd[q], ref, rtol=1e-9, atol=1e-13), (n, q)
+
+
+def test_leftover_oracle_matches_reference(diagonal_golden):
+    """compactFock's leftover-mode strategy (singleLeftoverMode_amps.py, singleLeftoverMode_grad.py):
+    the five block arrays and the Jacobians of arr0 against the reference source, to 1e-14 / 1e-13
+    relative, with the same elements written."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    try:
+        oracle.set_numpy_division(True)
+        for n in diagonal_cases(g, "lo"):
+            A, B, G0, cut = g[f"{n}/A"], g[f"{n}/B"], g[f"{n}/G0"], tuple(g[f"{n}/cutoffs"])
+            got = oracle.leftover_amps(A, B, G0, cut)
+            for name, x in zip(("arr0", "arr2", "arr1010", "arr1001", "arr1"), got):
+                ref = g[f"{n}/{name}"]
+                assert x.shape == ref.shape, (n, name)
+                assert np.array_equal(x == 0, ref == 0), (n, name)
+                assert _rel(x, ref) <= 1e-14, (n, name, _rel(x, ref))
+            for name, x in zip(("dG0", "dA", "dB"), oracle.leftover_grad(A, B, G0, cut)):
+                ref = g[f"{n}/{name}"]
+                assert x.shape == ref.shape, (n, name)
+                assert _rel(x, ref) <= 1e-13, (n, name, _rel(x, ref))
+    finally:
+        oracle.set_numpy_division(False)
+
+
+def test_leftover_equals_vanilla_blocks(diagonal_golden):
+    """tests/test_math/test_compactFock.py:46-69: arr0[m, n, k1, k2, ...] = G[m, n, k1, k1, k2, k2, ...]
+    of the vanilla tensor on the interleaved triple."""
+    from conftest import diagonal_cases
+
+    g = diagonal_golden
+    for n in diagonal_cases(g, "lo"):
+        A, B, G0, cut = g[f"{n}/A"], g[f"{n}/B"], g[f"{n}/G0"], tuple(int(x) for x in g[f"{n}/cutoffs"])
+        shape = tuple(x for x in cut for _ in range(2))
+        if np.prod(shape) > 3e5:
+            continue
+        G = oracle.vanilla(shape, A, B, G0)
+        arr0 = oracle.leftover_amps(A, B, G0, cut)[0]
+        for m in range(cut[0]):
+            for nn in range(cut[0]):
+                for tail in np.ndindex(*cut[1:]):
+                    ref = G[(m, nn) + tuple(x for k in tail for x in (k, k))]
+                    assert abs(arr0[(m, nn) + tail] - ref) <= 1e-10 * max(1.0, abs(ref)), (n, m, nn, tail)
