@@ -288,6 +288,31 @@ MM_API int mm_diagonal_jacobian(int M, const int64_t *cutoffs, const mm_c128 *A,
 MM_API int mm_diagonal_vjp(int M, const int64_t *cutoffs, const mm_c128 *J, const mm_c128 *W, const mm_c128 *G0,
                            const mm_c128 *g, mm_c128 *dA, mm_c128 *dB, mm_c128 *dG0, mm_stream_t stream);
 
+/*
+ * Leftover-mode strategy (M modes: mode 0 left over with cutoff q = cutoffs[0], modes
+ * 1..M-1 photon-number resolved with cutoffs[1..]): replaces
+ * fock_representation_1leftoverMode_amps (compactFock/singleLeftoverMode_amps.py:385-421) and
+ * fock_representation_1leftoverMode_grad (singleLeftoverMode_grad.py:571-724), reached through
+ * hermite_multidimensional_1leftoverMode / grad_hermite_multidimensional_1leftoverMode
+ * (compactFock/inputValidation.py:103-142) and hermite_renormalized_1leftoverMode_jax
+ * (mrmustard/math/jax_vjps/hermite.py:339-430, the JAX backend's path).
+ * A (2M, 2M), B (2M) interleaved, G0 (1): device complex128.  W receives mm_leftover_slots(M)
+ * slots (the diagonal strategy's slots over the M-1 detected modes) of q*q*P' values each,
+ * [slot][m][n][params]; W[0 .. q*q*P') is arr0 (q, q, *cutoffs[1..]).  J receives
+ * mm_leftover_slots(M) * q*q*P' * (4M^2 + 2M) values (Jacobian rows as for the diagonal).
+ * 2 <= M <= 8, q <= 1000 (the reference's sqrt table).
+ */
+MM_API int64_t mm_leftover_slots(int M);
+MM_API size_t mm_leftover_workspace_bytes(int M, const int64_t *cutoffs);
+MM_API int mm_leftover_amps(int M, const int64_t *cutoffs, const mm_c128 *A, const mm_c128 *B, const mm_c128 *G0,
+                            mm_c128 *W, void *ws, size_t ws_bytes, mm_stream_t stream);
+MM_API int mm_leftover_jacobian(int M, const int64_t *cutoffs, const mm_c128 *A, const mm_c128 *B, const mm_c128 *W,
+                                mm_c128 *J, void *ws, size_t ws_bytes, mm_stream_t stream);
+/* dA = sum g * arr0_dA, dB = sum g * arr0_dB, dG0 = sum g * arr0 / G0 over the q*q*P' entries of arr0
+ * (the contraction of hermite_renormalized_1leftoverMode_jax_bwd, jax_vjps/hermite.py:389-430). */
+MM_API int mm_leftover_vjp(int M, const int64_t *cutoffs, const mm_c128 *J, const mm_c128 *W, const mm_c128 *G0,
+                           const mm_c128 *g, mm_c128 *dA, mm_c128 *dB, mm_c128 *dG0, mm_stream_t stream);
+
 MM_API size_t mm_fast_diagonal_workspace_bytes(int L, const int64_t *pnr_cutoffs, int64_t output_cutoff);
 
 /*

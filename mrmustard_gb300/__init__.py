@@ -19,10 +19,13 @@ from .backend import BackendGB300
 from .binomial import binomial, device_binomial, hermite_renormalized_binomial
 from .diagonal import (
     fast_diagonal,
+    grad_hermite_multidimensional_1leftoverMode,
     grad_hermite_multidimensional_diagonal,
+    hermite_multidimensional_1leftoverMode,
     hermite_multidimensional_diagonal,
     hermite_renormalized_1leftoverMode,
     hermite_renormalized_diagonal,
+    hermite_renormalized_1leftoverMode_autograd,
     hermite_renormalized_diagonal_autograd,
 )
 from .einsum import contract, einsum
@@ -69,7 +72,10 @@ __all__ = [
     "contract",
     "einsum",
     "fast_diagonal",
+    "grad_hermite_multidimensional_1leftoverMode",
     "grad_hermite_multidimensional_diagonal",
+    "hermite_multidimensional_1leftoverMode",
+    "hermite_renormalized_1leftoverMode_autograd",
     "hermite_multidimensional_diagonal",
     "hermite_renormalized_1leftoverMode",
     "hermite_renormalized_diagonal",

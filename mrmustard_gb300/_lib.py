@@ -70,6 +70,11 @@ SIGNATURES = {
     "mm_diagonal_vjp": (I32, [I32, P, P, P, P, P, P, P, P, P]),
     "mm_fast_diagonal_workspace_bytes": (SZ, [I32, P, I64]),
     "mm_fast_diagonal": (I32, [I32, P, I64, P, P, P, I32, P, P, SZ, P]),
+    "mm_leftover_slots": (I64, [I32]),
+    "mm_leftover_workspace_bytes": (SZ, [I32, P]),
+    "mm_leftover_amps": (I32, [I32, P, P, P, P, P, P, SZ, P]),
+    "mm_leftover_jacobian": (I32, [I32, P, P, P, P, P, P, SZ, P]),
+    "mm_leftover_vjp": (I32, [I32, P, P, P, P, P, P, P, P, P]),
     "mm_tensor_permute": (I32, [I32, P, P, I64, P, P, P]),
     "mm_tensor_sum_inner": (I32, [I64, I64, P, P, P]),
     "mm_zgemm_batched": (I32, [I64, I64, I64, I64, P, I64, P, I64, P, I64, P]),

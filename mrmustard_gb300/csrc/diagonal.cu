@@ -743,6 +743,288 @@ __global__ void __launch_bounds__(DG_BLOCK) fd_kernel(FdArgs a) {
   }
 }
 
+// ------------------------------------------------------------------ 4. leftover mode
+// compactFock's leftover-mode strategy (compactFock/singleLeftoverMode_amps.py:18-421 and
+// singleLeftoverMode_grad.py:18-724): mode 0 is left over, its q x q block is carried by every
+// point of the detected modes' params lattice.  Block entry (m, n) of an output row i (full
+// index) reads the pivot block at (m, n), (m-1, n), (m, n-1) and the inputs at (m, n):
+//   (pivot[m,n] B_i + A_i0 sqrt(m) pivot[m-1,n] + A_i1 sqrt(n) pivot[m,n-1]
+//    + sum_l A_i,l+2 K_l G_l[m,n]) / K_i.
+// The first block (every detected mode at 0) is a 2-D recurrence filled by one CTA by
+// anti-diagonals.  Storage W[slot][m][n][P'] (the diagonal strategy's slots over the detected
+// modes), J[slot][m][n][P'][4M^2 + 2M].  Two phases per weight: diagonal pivots, then
+// off-diagonal pivots (which read three entries of a diagonal pivot's block).
+
+struct LoArgs {
+  DiagLat L;  // detected modes' lattice (M' modes; L.n = 2M')
+  int q;      // leftover cutoff
+  int N;      // 2M (rows of A)
+  const double2* A;
+  const double2* B;
+  const double2* G0;
+  double2* Wv;
+  double2* J;
+  Tabs t;
+  int32_t ntab;
+  SortBufs sb;
+  WsHeader* h;
+  uint64_t budget;
+};
+
+__device__ __forceinline__ int64_t lo_at(const LoArgs& a, int64_t slot, int m, int n, int32_t f) {
+  return ((slot * a.q + m) * a.q + n) * (int64_t)a.L.P + f;
+}
+
+// Block entry (m, n) of full row `row`; gin[l] are the scaled inputs K_l G_l[m, n].
+template <int MT>
+__device__ __forceinline__ double2 lo_value(const LoArgs& a, int row, int64_t ps, int32_t f, int m, int n,
+                                            const double2* gin, double kinv) {
+  const double2* W = a.Wv;
+  double2 acc = cmul(ldv(&W[lo_at(a, ps, m, n, f)]), a.B[row]);
+  if (m > 0) acc = cfma(a.A[row * a.N + 0], cscale(a.t.sq[m], ldv(&W[lo_at(a, ps, m - 1, n, f)])), acc);
+  if (n > 0) acc = cfma(a.A[row * a.N + 1], cscale(a.t.sq[n], ldv(&W[lo_at(a, ps, m, n - 1, f)])), acc);
+#pragma unroll
+  for (int l = 0; l < 2 * MT; ++l) acc = cfma(a.A[row * a.N + l + 2], gin[l], acc);
+  return cscale(kinv, acc);
+}
+
+// Inputs of the diagonal pivot at (m, n): arr1[l^1] at p - 1_{l/2}, scaled by sqrt(p_{l/2}).
+template <int MT>
+__device__ __forceinline__ void lo_diag_inputs(const LoArgs& a, const int32_t* p, int32_t f, int m, int n,
+                                               int64_t* src, double* kl) {
+#pragma unroll
+  for (int l = 0; l < 2 * MT; ++l) {
+    const int k = l >> 1;
+    kl[l] = a.t.sq[p[k]];
+    src[l] = p[k] > 0 ? lo_at(a, slot_arr1(a.L, l ^ 1), m, n, f - a.L.st[k]) : -1;
+  }
+}
+
+// Inputs of the off-diagonal pivot d at (m, n).
+template <int MT>
+__device__ __forceinline__ void lo_offdiag_inputs(const LoArgs& a, const int32_t* p, int32_t f, int d, int m, int n,
+                                                  int64_t* src, double* kl) {
+#pragma unroll
+  for (int i = 0; i < MT; ++i) {
+    src[2 * i] = -1;
+    src[2 * i + 1] = -1;
+    kl[2 * i] = a.t.sq[p[i]];
+    kl[2 * i + 1] = kl[2 * i];
+    if (i < d) continue;
+    if (i == d) {
+      kl[2 * i] = a.t.sq[p[i] + 1];
+      src[2 * i] = lo_at(a, 0, m, n, f);
+      if (p[i] > 0) src[2 * i + 1] = lo_at(a, slot_arr2(a.L, d), m, n, f - a.L.st[i]);
+    } else if (p[i] > 0) {
+      src[2 * i] = lo_at(a, slot_1001(a.L, d, i - d - 1), m, n, f - a.L.st[i]);
+      src[2 * i + 1] = lo_at(a, slot_1010(a.L, d, i - d - 1), m, n, f - a.L.st[i]);
+    }
+  }
+}
+
+template <int MT>
+__device__ __forceinline__ void lo_gather(const LoArgs& a, const int64_t* src, const double* kl, double2* gin) {
+#pragma unroll
+  for (int l = 0; l < 2 * MT; ++l) gin[l] = src[l] >= 0 ? cscale(kl[l], ldv(&a.Wv[src[l]])) : cmk(0.0, 0.0);
+}
+
+// First block (singleLeftoverMode_amps.py:339-352): anti-diagonals s = m + k of the q x q block.
+__global__ void lo_fill_kernel(LoArgs a) {
+  const int q = a.q, N = a.N;
+  double2* W = a.Wv;
+  if (threadIdx.x == 0) W[lo_at(a, 0, 0, 0, 0)] = __ldg(a.G0);
+  __syncthreads();
+  auto at = [&](int m, int k) -> double2 { return (m < 0 || k < 0) ? cmk(0.0, 0.0) : W[lo_at(a, 0, m, k, 0)]; };
+  for (int s = 1; s <= 2 * (q - 1); ++s) {
+    for (int m = max(0, s - (q - 1)) + (int)threadIdx.x; m <= min(s, q - 1); m += blockDim.x) {
+      const int k = s - m;
+      double2 acc;
+      if (k == 0) {  // column 0, from (m - 1, 0) and (m - 2, 0)
+        acc = cmul(at(m - 1, 0), a.B[0]);
+        acc = cfma(cscale(a.t.sq[m - 1], a.A[0]), at(m - 2, 0), acc);
+        acc = cscale(a.t.rs[m], acc);
+      } else {  // from (m, k - 1), (m - 1, k - 1), (m, k - 2)
+        acc = cmul(at(m, k - 1), a.B[1]);
+        acc = cfma(cscale(a.t.sq[m], a.A[N + 0]), at(m - 1, k - 1), acc);
+        acc = cfma(cscale(a.t.sq[k - 1], a.A[N + 1]), at(m, k - 2), acc);
+        acc = cscale(a.t.rs[k], acc);
+      }
+      W[lo_at(a, 0, m, k, 0)] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+template <int MT>
+__global__ void __launch_bounds__(DG_BLOCK) lo_amps_kernel(LoArgs a) {
+  MM_SHARED(StageSmem, sm);
+  const double2* Bs = a.B;
+  stage_operands(sm, a.t, a.ntab, a.A, a.N, &Bs);
+  a.B = Bs;
+  const DiagLat& L = a.L;
+  const int q = a.q, qq = q * q;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  uint32_t epoch = 0;
+  for (int w = 0; w < L.W; ++w) {
+    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
+    const int64_t per_row = (int64_t)cnt * qq;
+    for (int phase = 0; phase < 2; ++phase) {
+      for (int64_t t = t0; t < per_row * 2 * MT; t += stride) {
+        const int r = (int)(t / per_row);
+        const int64_t u = t - r * per_row;
+        const int mn = (int)(u / cnt);
+        const int32_t f = a.sb.order[s0 + (int32_t)(u - (int64_t)mn * cnt)];
+        const int m = mn / q, n = mn - m * q;
+        int32_t p[MT];
+        decode_params<MT>(L, f, p);
+        int64_t src[2 * MT];
+        double kl[2 * MT];
+        double2 gin[2 * MT];
+        if (phase == 0) {
+          if (!diag_target(L, p, r)) continue;
+          lo_diag_inputs<MT>(a, p, f, m, n, src, kl);
+          lo_gather<MT>(a, src, kl, gin);
+          a.Wv[lo_at(a, slot_arr1(L, r), m, n, f)] = lo_value<MT>(a, r + 2, 0, f, m, n, gin, a.t.rs[p[r >> 1] + 1]);
+          continue;
+        }
+        const int dl = last_pivot<MT>(p);
+        for (int d = 0; d <= dl; ++d) {
+          int row;
+          int64_t slot;
+          int32_t dst;
+          if (!offdiag_target(L, p, d, r, row, slot, dst, f)) continue;
+          lo_offdiag_inputs<MT>(a, p, f, d, m, n, src, kl);
+          lo_gather<MT>(a, src, kl, gin);
+          const int k = row >> 1;
+          const int lift = (row & 1) == 0 && k == d;
+          a.Wv[lo_at(a, slot, m, n, dst)] =
+              lo_value<MT>(a, row + 2, slot_arr1(L, 2 * d), f, m, n, gin, a.t.rs[p[k] + lift + 1]);
+        }
+      }
+      if (!step_barrier(a.h, epoch, a.budget)) return;
+    }
+  }
+}
+
+// ---- Jacobians
+
+template <int MT>
+__device__ __forceinline__ double2 lo_jac_value(const LoArgs& a, int row, int64_t ps, int32_t f, int m, int n,
+                                                const int64_t* src, const double* kl, int qc, double kinv) {
+  const int N = a.N, nA = N * N, nc = nA + N;
+  const bool isA = qc < nA;
+  const int qa = qc / N, qb = qc - qa * N;
+  const double2* W = a.Wv;
+  const double2* J = a.J;
+  const int64_t pv = lo_at(a, ps, m, n, f);
+  double2 acc = cmul(ldv(&J[pv * nc + qc]), a.B[row]);
+  if (!isA && qc - nA == row) acc = cadd(acc, ldv(&W[pv]));
+  if (m > 0) {
+    const int64_t o = lo_at(a, ps, m - 1, n, f);
+    acc = cfma(cscale(a.t.sq[m], a.A[row * N + 0]), ldv(&J[o * nc + qc]), acc);
+    if (isA && qa == row && qb == 0) acc = cadd(acc, cscale(a.t.sq[m], ldv(&W[o])));
+  }
+  if (n > 0) {
+    const int64_t o = lo_at(a, ps, m, n - 1, f);
+    acc = cfma(cscale(a.t.sq[n], a.A[row * N + 1]), ldv(&J[o * nc + qc]), acc);
+    if (isA && qa == row && qb == 1) acc = cadd(acc, cscale(a.t.sq[n], ldv(&W[o])));
+  }
+#pragma unroll
+  for (int l = 0; l < 2 * MT; ++l) {
+    if (src[l] < 0) continue;
+    acc = cfma(cscale(kl[l], a.A[row * N + l + 2]), ldv(&J[src[l] * nc + qc]), acc);
+    if (isA && qa == row && qb == l + 2) acc = cadd(acc, cscale(kl[l], ldv(&W[src[l]])));
+  }
+  return cscale(kinv, acc);
+}
+
+// First block's Jacobians (singleLeftoverMode_grad.py:606-650), one thread per component.
+__global__ void lo_fill_jacobian_kernel(LoArgs a) {
+  const int q = a.q, N = a.N, nA = N * N, nc = nA + N;
+  const double2* W = a.Wv;
+  double2* J = a.J;
+  auto jat = [&](int m, int k, int c) -> double2 {
+    return (m < 0 || k < 0) ? cmk(0.0, 0.0) : J[lo_at(a, 0, m, k, 0) * nc + c];
+  };
+  auto wat = [&](int m, int k) -> double2 { return (m < 0 || k < 0) ? cmk(0.0, 0.0) : W[lo_at(a, 0, m, k, 0)]; };
+  for (int s = 1; s <= 2 * (q - 1); ++s) {
+    const int m_lo = max(0, s - (q - 1)), m_hi = min(s, q - 1);
+    const int items = (m_hi - m_lo + 1) * nc;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int m = m_lo + it / nc, c = it % nc, k = s - m;
+      double2 acc;
+      if (k == 0) {
+        acc = cmul(jat(m - 1, 0, c), a.B[0]);
+        acc = cfma(cscale(a.t.sq[m - 1], a.A[0]), jat(m - 2, 0, c), acc);
+        if (c == 0) acc = cadd(acc, cscale(a.t.sq[m - 1], wat(m - 2, 0)));
+        if (c == nA) acc = cadd(acc, wat(m - 1, 0));
+        acc = cscale(a.t.rs[m], acc);
+      } else {
+        acc = cmul(jat(m, k - 1, c), a.B[1]);
+        acc = cfma(cscale(a.t.sq[m], a.A[N + 0]), jat(m - 1, k - 1, c), acc);
+        acc = cfma(cscale(a.t.sq[k - 1], a.A[N + 1]), jat(m, k - 2, c), acc);
+        if (c == N) acc = cadd(acc, cscale(a.t.sq[m], wat(m - 1, k - 1)));
+        if (c == N + 1) acc = cadd(acc, cscale(a.t.sq[k - 1], wat(m, k - 2)));
+        if (c == nA + 1) acc = cadd(acc, wat(m, k - 1));
+        acc = cscale(a.t.rs[k], acc);
+      }
+      J[lo_at(a, 0, m, k, 0) * nc + c] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+template <int MT>
+__global__ void __launch_bounds__(DG_BLOCK) lo_jacobian_kernel(LoArgs a) {
+  MM_SHARED(StageSmem, sm);
+  const double2* Bs = a.B;
+  stage_operands(sm, a.t, a.ntab, a.A, a.N, &Bs);
+  a.B = Bs;
+  const DiagLat& L = a.L;
+  const int q = a.q, qq = q * q, nc = a.N * a.N + a.N;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  uint32_t epoch = 0;
+  for (int w = 0; w < L.W; ++w) {
+    const int32_t s0 = a.sb.start[w], cnt = a.sb.start[w + 1] - s0;
+    const int64_t per_row = (int64_t)cnt * qq * nc;
+    for (int phase = 0; phase < 2; ++phase) {
+      for (int64_t t = t0; t < per_row * 2 * MT; t += stride) {
+        const int r = (int)(t / per_row);
+        const int64_t u = t - r * per_row;
+        const int64_t v = u / nc;
+        const int qc = (int)(u - v * nc);
+        const int mn = (int)(v / cnt);
+        const int32_t f = a.sb.order[s0 + (int32_t)(v - (int64_t)mn * cnt)];
+        const int m = mn / q, n = mn - m * q;
+        int32_t p[MT];
+        decode_params<MT>(L, f, p);
+        int64_t src[2 * MT];
+        double kl[2 * MT];
+        if (phase == 0) {
+          if (!diag_target(L, p, r)) continue;
+          lo_diag_inputs<MT>(a, p, f, m, n, src, kl);
+          a.J[lo_at(a, slot_arr1(L, r), m, n, f) * nc + qc] =
+              lo_jac_value<MT>(a, r + 2, 0, f, m, n, src, kl, qc, a.t.rs[p[r >> 1] + 1]);
+          continue;
+        }
+        const int dl = last_pivot<MT>(p);
+        for (int d = 0; d <= dl; ++d) {
+          int row;
+          int64_t slot;
+          int32_t dst;
+          if (!offdiag_target(L, p, d, r, row, slot, dst, f)) continue;
+          lo_offdiag_inputs<MT>(a, p, f, d, m, n, src, kl);
+          const int k = row >> 1;
+          const int lift = (row & 1) == 0 && k == d;
+          a.J[lo_at(a, slot, m, n, dst) * nc + qc] =
+              lo_jac_value<MT>(a, row + 2, slot_arr1(L, 2 * d), f, m, n, src, kl, qc, a.t.rs[p[k] + lift + 1]);
+        }
+      }
+      if (!step_barrier(a.h, epoch, a.budget)) return;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host planning
 
 #ifndef MM_HOST_EMULATION
@@ -897,6 +1179,19 @@ int fd_lat(int Lm, const int64_t* pnr, int64_t oc, FdLat& F) {
   return MM_OK;
 }
 
+int lo_lat(int M, const int64_t* cutoffs, DiagLat& L, int& q) {
+  if (cutoffs == nullptr || M < 2) return M == 1 ? MM_ERR_UNSUPPORTED : MM_ERR_INVALID_ARG;
+  if (M > DG_MAXM) return MM_ERR_UNSUPPORTED;
+  if (cutoffs[0] < 1) return MM_ERR_INVALID_ARG;
+  if (cutoffs[0] > 1000) return MM_ERR_TOO_LARGE;  // the reference's sqrt table (helperFunctions.py:12)
+  q = (int)cutoffs[0];
+  const int rc = diag_lat(M - 1, cutoffs + 1, 1, L);
+  if (rc) return rc;
+  if ((int64_t)L.P * q * q * diag_slots(M - 1) > ((int64_t)1 << 36)) return MM_ERR_TOO_LARGE;
+  return MM_OK;
+}
+int32_t lo_ntab(const DiagLat& L, int q) { return std::max(diag_ntab(L), q + 1); }
+
 // lattice points per weight: per pair, states by a + b split into |a-b| < 2 and |a-b| = 2;
 // the product keeps at most one pair at distance 2
 std::vector<int64_t> fd_counts(const FdLat& F) {
@@ -977,6 +1272,31 @@ void* diag_jacobian_fn(int M) {
   }
   return nullptr;
 }
+void* lo_amps_fn(int MT) {
+  switch (MT) {
+    case 1: return (void*)lo_amps_kernel<1>;
+    case 2: return (void*)lo_amps_kernel<2>;
+    case 3: return (void*)lo_amps_kernel<3>;
+    case 4: return (void*)lo_amps_kernel<4>;
+    case 5: return (void*)lo_amps_kernel<5>;
+    case 6: return (void*)lo_amps_kernel<6>;
+    case 7: return (void*)lo_amps_kernel<7>;
+  }
+  return nullptr;
+}
+void* lo_jacobian_fn(int MT) {
+  switch (MT) {
+    case 1: return (void*)lo_jacobian_kernel<1>;
+    case 2: return (void*)lo_jacobian_kernel<2>;
+    case 3: return (void*)lo_jacobian_kernel<3>;
+    case 4: return (void*)lo_jacobian_kernel<4>;
+    case 5: return (void*)lo_jacobian_kernel<5>;
+    case 6: return (void*)lo_jacobian_kernel<6>;
+    case 7: return (void*)lo_jacobian_kernel<7>;
+  }
+  return nullptr;
+}
+
 void* fd_fn(int K) {
   switch (K) {
     case 1: return (void*)fd_kernel<1>;
@@ -1128,5 +1448,116 @@ MM_API int mm_fast_diagonal(int L, const int64_t* pnr_cutoffs, int64_t output_cu
   int64_t mx = 1;
   for (int wgt = 1; wgt < (int)cnt.size() && wgt < F.wend; ++wgt) mx = std::max(mx, cnt[wgt]);
   return launch_wavefront(kern, &a, mx * F.q * F.q, dc.sms, dc.occ, st);
+}
+
+MM_API int64_t mm_leftover_slots(int M) { return M < 2 ? 0 : diag_slots(M - 1); }
+
+MM_API size_t mm_leftover_workspace_bytes(int M, const int64_t* cutoffs) {
+  DiagLat L;
+  int q;
+  if (lo_lat(M, cutoffs, L, q)) return 0;
+  return diag_ws(L.W, L.P, lo_ntab(L, q)).total;
+}
+
+static int lo_setup(int M, const int64_t* cutoffs, const mm_c128* A, const mm_c128* B, void* ws, size_t ws_bytes,
+                    LoArgs& a, DiagWs& lay) {
+  int q;
+  int rc = lo_lat(M, cutoffs, a.L, q);
+  if (rc) return rc;
+  if (!A || !B) return MM_ERR_INVALID_ARG;
+  lay = diag_ws(a.L.W, a.L.P, lo_ntab(a.L, q));
+  if ((rc = check_ws(ws, ws_bytes, lay.total))) return rc;
+  char* w = static_cast<char*>(ws);
+  a.q = q;
+  a.N = 2 * M;
+  a.A = (const double2*)A;
+  a.B = (const double2*)B;
+  a.t = tabs_of(w, lay);
+  a.ntab = lay.ntab;
+  a.sb = sort_bufs(w, lay);
+  a.h = reinterpret_cast<WsHeader*>(w);
+  a.budget = budget_ns();
+  return MM_OK;
+}
+
+MM_API int mm_leftover_amps(int M, const int64_t* cutoffs, const mm_c128* A, const mm_c128* B, const mm_c128* G0,
+                            mm_c128* W, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  LoArgs a;
+  memset(&a, 0, sizeof(a));
+  DiagWs lay;
+  int rc = lo_setup(M, cutoffs, A, B, ws, ws_bytes, a, lay);
+  if (rc) return rc;
+  if (!G0 || !W) return MM_ERR_INVALID_ARG;
+  a.G0 = (const double2*)G0;
+  a.Wv = (double2*)W;
+  void* kern = lo_amps_fn(M - 1);
+  DevCfg dc;
+  if ((rc = dev_cfg(kern, dc))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  const int64_t qq = (int64_t)a.q * a.q;
+  if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
+  if (cudaMemsetAsync(W, 0, (size_t)diag_slots(M - 1) * qq * a.L.P * sizeof(double2), st) != cudaSuccess)
+    return MM_ERR_CUDA;
+  if ((rc = launch_sort(a.L, a.L.P, a.L.W, a.sb, dc.sms, st))) return rc;
+  if ((rc = launch_tables(w, lay, st))) return rc;
+  lo_fill_kernel<<<1, 256, 0, st>>>(a);
+  note_launches(1);
+  if ((rc = cuda_status())) return rc;
+  const std::vector<int64_t> cnt = diag_counts(a.L);
+  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * qq * a.L.n;
+  return launch_wavefront(kern, &a, max_items, dc.sms, dc.occ, st);
+}
+
+MM_API int mm_leftover_jacobian(int M, const int64_t* cutoffs, const mm_c128* A, const mm_c128* B, const mm_c128* W,
+                                mm_c128* J, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  LoArgs a;
+  memset(&a, 0, sizeof(a));
+  DiagWs lay;
+  int rc = lo_setup(M, cutoffs, A, B, ws, ws_bytes, a, lay);
+  if (rc) return rc;
+  if (!W || !J) return MM_ERR_INVALID_ARG;
+  a.Wv = (double2*)W;
+  a.J = (double2*)J;
+  const int64_t nc = (int64_t)a.N * a.N + a.N, qq = (int64_t)a.q * a.q;
+  if ((int64_t)a.L.P * qq * nc * diag_slots(M - 1) > ((int64_t)1 << 36)) return MM_ERR_TOO_LARGE;
+  void* kern = lo_jacobian_fn(M - 1);
+  DevCfg dc;
+  if ((rc = dev_cfg(kern, dc))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  if (cudaMemsetAsync(w + MM_WS_LAUNCH_STATE_OFFSET, 0, MM_WS_LAUNCH_STATE_BYTES, st) != cudaSuccess) return MM_ERR_CUDA;
+  if (cudaMemsetAsync(J, 0, (size_t)diag_slots(M - 1) * qq * a.L.P * nc * sizeof(double2), st) != cudaSuccess)
+    return MM_ERR_CUDA;
+  if ((rc = launch_sort(a.L, a.L.P, a.L.W, a.sb, dc.sms, st))) return rc;
+  if ((rc = launch_tables(w, lay, st))) return rc;
+  lo_fill_jacobian_kernel<<<1, 256, 0, st>>>(a);
+  note_launches(1);
+  if ((rc = cuda_status())) return rc;
+  const std::vector<int64_t> cnt = diag_counts(a.L);
+  const int64_t max_items = *std::max_element(cnt.begin(), cnt.end()) * qq * nc * a.L.n;
+  return launch_wavefront(kern, &a, max_items, dc.sms, dc.occ, st);
+}
+
+MM_API int mm_leftover_vjp(int M, const int64_t* cutoffs, const mm_c128* J, const mm_c128* W, const mm_c128* G0,
+                           const mm_c128* g, mm_c128* dA, mm_c128* dB, mm_c128* dG0, mm_stream_t stream) {
+  DiagLat L;
+  int q;
+  int rc = lo_lat(M, cutoffs, L, q);
+  if (rc) return rc;
+  if (!J || !W || !G0 || !g || !dA || !dB || !dG0) return MM_ERR_INVALID_ARG;
+  // arr0's Jacobian is [block entry][component] with the entries (m, n, params) flat, the layout
+  // the diagonal strategy's VJP contracts: reuse it with 2M rows and q^2 P' entries.
+  DiagLat V;
+  memset(&V, 0, sizeof(V));
+  V.M = M;
+  V.n = 2 * M;
+  V.P = (int32_t)((int64_t)q * q * L.P);
+  const int nc = V.n * V.n + V.n;
+  diag_vjp_kernel<<<nc + 1, 256, 0, (cudaStream_t)stream>>>(V, (const double2*)J, (const double2*)W,
+                                                            (const double2*)G0, (const double2*)g, (double2*)dA,
+                                                            (double2*)dB, (double2*)dG0);
+  note_launches(1);
+  return cuda_status();
 }
 #endif  // MM_HOST_EMULATION

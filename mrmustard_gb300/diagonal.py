@@ -8,6 +8,10 @@ Mirrors, with the same arguments, return values and errors:
   (arr0_dG0, arr0_dA, arr0_dB) (inputValidation.py:82-100, diagonal_grad.py:261-378);
 * ``fast_diagonal(A, b, c, output_cutoff, pnr_cutoffs, stable)``
   (mrmustard/math/lattice/strategies/fast_diagonal.py:32-77);
+* ``hermite_multidimensional_1leftoverMode`` / ``grad_hermite_multidimensional_1leftoverMode``
+  (compactFock/inputValidation.py:103-142, singleLeftoverMode_amps.py, singleLeftoverMode_grad.py),
+  the JAX backend's leftover-mode path, with ``hermite_renormalized_1leftoverMode_autograd``
+  (``hermite_renormalized_1leftoverMode_jax``, jax_vjps/hermite.py:339-430);
 * the backend methods ``hermite_renormalized_diagonal(A, B, C, cutoffs, reorderedAB)`` and
   ``hermite_renormalized_1leftoverMode(A, b, c, output_cutoff, pnr_cutoffs, stable, reorderedAB)``
   (mrmustard/math/backend_numpy.py:423-446), and a differentiable
@@ -36,6 +40,9 @@ __all__ = [
     "hermite_renormalized_1leftoverMode",
     "reorder_AB_bargmann",
     "device_diagonal_slots",
+    "hermite_multidimensional_1leftoverMode",
+    "grad_hermite_multidimensional_1leftoverMode",
+    "hermite_renormalized_1leftoverMode_autograd",
 ]
 
 
@@ -218,6 +225,156 @@ def hermite_renormalized_diagonal_autograd(A, B, C, cutoffs, reorderedAB: bool =
     under the JAX backend (backend_jax.py:513-522)."""
     A, B = reorder_AB_bargmann(A, B) if reorderedAB else (A, B)
     return DiagonalFn.apply(A, B, C, tuple(int(c) for c in cutoffs))
+
+
+# ----------------------------------------------------------------- leftover mode (compactFock)
+def _lo_split(W: torch.Tensor, M: int, cut: tuple):
+    """Slot buffer [slot][m][n][P'] -> the reference's arrays with the block axes first
+    (singleLeftoverMode_amps.py:385-408); views, no copies."""
+    q, tail = cut[0], tuple(cut[1:])
+    Mt = M - 1
+    W = W.reshape((-1, q, q) + tail)
+    mv = lambda x: x.movedim(0, 2)
+    arr0 = W[0]
+    arr2 = mv(W[1:1 + Mt])
+    o = 1 + Mt
+    if Mt == 1:
+        z = torch.zeros((1, 1, 1, 1, 1), dtype=W.dtype, device=W.device)
+        arr1010, arr1001 = z, z.clone()
+    else:
+        k = Mt * (Mt - 1)
+        arr1010 = mv(W[o:o + k]).reshape((q, q, Mt, Mt - 1) + tail)
+        arr1001 = mv(W[o + k:o + 2 * k]).reshape((q, q, Mt, Mt - 1) + tail)
+    o += 2 * Mt * (Mt - 1)
+    arr1 = mv(W[o:o + 2 * Mt])
+    return arr0, arr2, arr1010, arr1001, arr1
+
+
+def _lo_join(M, cut, arr0, arr2, arr1010, arr1001, arr1, dev) -> torch.Tensor:
+    q, tail = cut[0], tuple(cut[1:])
+    Mt = M - 1
+    parts = [_to_dev(arr0, dev).reshape((1, q, q) + tail), _to_dev(arr2, dev).movedim(2, 0)]
+    if Mt > 1:
+        k = Mt * (Mt - 1)
+        parts += [_to_dev(arr1010, dev).reshape((q, q, k) + tail).movedim(2, 0),
+                  _to_dev(arr1001, dev).reshape((q, q, k) + tail).movedim(2, 0)]
+    parts.append(_to_dev(arr1, dev).movedim(2, 0))
+    return torch.cat([p.contiguous().reshape(-1) for p in parts]).contiguous()
+
+
+def device_leftover_slots(A, B, G0, cutoffs):
+    """Device forward of the leftover strategy: the slot buffer (A, B interleaved; cutoffs[0] the
+    leftover mode's cutoff)."""
+    dev = A.device if _is_dev(A) else require_cuda()
+    cut, sh = _shape_arr(cutoffs)
+    M = len(cut)
+    Ad, Bd = _to_dev(A, dev).contiguous(), _to_dev(B, dev).reshape(-1).contiguous()
+    g0 = _to_dev(G0, dev).reshape(-1)[:1].contiguous()
+    lib = _lib.load()
+    W = torch.empty(int(lib.mm_leftover_slots(M)) * cut[0] ** 2 * int(np.prod(cut[1:])), dtype=torch.complex128,
+                    device=dev)
+    ws = Workspace(lib.mm_leftover_workspace_bytes(M, sh), dev)
+    _lib.check(lib.mm_leftover_amps(M, sh, Ad.data_ptr(), Bd.data_ptr(), g0.data_ptr(), W.data_ptr(), ws.ptr,
+                                    ws.nbytes, _stream()), "mm_leftover_amps")
+    _finish(ws, "leftover")
+    return W
+
+
+def hermite_multidimensional_1leftoverMode(A, B, G0, cutoffs, rtol=1e-05, atol=1e-08):
+    """The five arrays of the leftover-mode strategy (inputValidation.py:103-119); A, B interleaved."""
+    _input_validation(A, atol=atol, rtol=rtol)
+    if A.shape[0] != B.shape[0]:
+        raise ValueError("The matrix A and vector B have incompatible dimensions")
+    if isinstance(cutoffs, Iterable):
+        cutoffs = tuple(int(c) for c in cutoffs)
+    else:
+        raise ValueError("cutoffs should be array like of length M")
+    M = len(cutoffs)
+    if A.shape[0] // 2 != M:
+        raise ValueError("The matrix A and cutoffs have incompatible dimensions")
+    if M <= 1:
+        raise ValueError("The number of modes should be greater than 1.")
+    dev_mode = _is_dev(A)
+    W = device_leftover_slots(A, B, G0, cutoffs)
+    return tuple(_out(x, dev_mode) for x in _lo_split(W, M, cutoffs))
+
+
+def _lo_jacobian(A, B, W, cut, dev):
+    M = len(cut)
+    n = 2 * M
+    _, sh = _shape_arr(cut)
+    lib = _lib.load()
+    Ad, Bd = _to_dev(A, dev).contiguous(), _to_dev(B, dev).reshape(-1).contiguous()
+    J = torch.empty(W.numel() * (n * n + n), dtype=torch.complex128, device=dev)
+    ws = Workspace(lib.mm_leftover_workspace_bytes(M, sh), dev)
+    _lib.check(lib.mm_leftover_jacobian(M, sh, Ad.data_ptr(), Bd.data_ptr(), W.data_ptr(), J.data_ptr(), ws.ptr,
+                                        ws.nbytes, _stream()), "mm_leftover_jacobian")
+    _finish(ws, "leftover jacobian")
+    return J
+
+
+def grad_hermite_multidimensional_1leftoverMode(A, B, G0, arr0, arr2, arr1010, arr1001, arr1):
+    """(arr0_dG0, arr0_dA, arr0_dB) of the leftover strategy (inputValidation.py:122-142)."""
+    if A.shape[0] != B.shape[0]:
+        raise ValueError("The matrix A and vector B have incompatible dimensions")
+    M = A.shape[0] // 2
+    if M <= 1:
+        raise ValueError("The number of modes should be greater than 1.")
+    dev_mode = _is_dev(A)
+    dev = A.device if dev_mode else require_cuda()
+    cut = (int(arr0.shape[0]),) + tuple(int(x) for x in arr0.shape[2:])
+    W = _lo_join(M, cut, arr0, arr2, arr1010, arr1001, arr1, dev)
+    J = _lo_jacobian(A, B, W, cut, dev)
+    n = 2 * M
+    E = int(np.prod(arr0.shape))
+    J0 = J[:E * (n * n + n)].reshape(tuple(arr0.shape) + (n * n + n,))
+    g0 = _to_dev(G0, dev).reshape(-1)[0]
+    dG0 = (W[:E] / g0).reshape(tuple(arr0.shape))
+    return (_out(dG0, dev_mode), _out(J0[..., :n * n].reshape(tuple(arr0.shape) + (n, n)), dev_mode),
+            _out(J0[..., n * n:], dev_mode))
+
+
+class LeftoverFn(torch.autograd.Function):
+    """arr0 (q, q, *tail) of the leftover strategy with the reference's custom VJP
+    (jax_vjps/hermite.py:381-430), on the device; PyTorch's convention as DiagonalFn."""
+
+    @staticmethod
+    def forward(ctx, A, B, C, cutoffs):
+        cut = tuple(cutoffs)
+        W = device_leftover_slots(A.detach(), B.detach(), C.detach(), cut)
+        Ad = raw(A.detach().to(torch.complex128)).contiguous()
+        Bd = raw(B.detach().to(torch.complex128)).contiguous()
+        cd = raw(C.detach().to(torch.complex128)).reshape(1).contiguous()
+        ctx.save_for_backward(Ad, Bd, cd, W)
+        ctx.cut = cut
+        ctx.c_shape = C.shape
+        E = cut[0] ** 2 * int(np.prod(cut[1:]))
+        return W[:E].reshape((cut[0], cut[0]) + tuple(cut[1:])).clone()
+
+    @staticmethod
+    def backward(ctx, grad):
+        A, B, C, W = ctx.saved_tensors
+        cut = ctx.cut
+        M = len(cut)
+        n = 2 * M
+        J = _lo_jacobian(A, B, W, cut, A.device)
+        g = grad.conj().resolve_conj().to(torch.complex128).reshape(-1).contiguous()
+        dA = torch.empty((n, n), dtype=torch.complex128, device=A.device)
+        dB = torch.empty((n,), dtype=torch.complex128, device=A.device)
+        dC = torch.empty((1,), dtype=torch.complex128, device=A.device)
+        _, sh = _shape_arr(cut)
+        _lib.check(_lib.load().mm_leftover_vjp(M, sh, J.data_ptr(), W.data_ptr(), C.data_ptr(), g.data_ptr(),
+                                               dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), _stream()),
+                   "mm_leftover_vjp")
+        return dA.conj(), dB.conj(), dC.conj().reshape(ctx.c_shape), None
+
+
+def hermite_renormalized_1leftoverMode_autograd(A, B, C, output_cutoff, pnr_cutoffs, reorderedAB: bool = True):
+    """Differentiable leftover-mode density matrices, ``math.hermite_renormalized_1leftoverMode`` under
+    the JAX backend (backend_jax.py:524-534): (oc+1, oc+1, pnr_1+1, ...) for CUDA tensors."""
+    A, B = reorder_AB_bargmann(A, B) if reorderedAB else (A, B)
+    cutoffs = (int(output_cutoff) + 1, *(int(p) + 1 for p in pnr_cutoffs))
+    return LeftoverFn.apply(A, B, C, cutoffs)
 
 
 # ----------------------------------------------------------------- fast_diagonal

@@ -224,3 +224,100 @@ def test_diagonal_device_in_device_out(cuda):
     assert fd.is_cuda and fd.shape == (6, 5, 5)
     ref = oracle.fast_diagonal(A, b, c, 4, (5,))
     assert _rel(fd.cpu().numpy(), ref) <= TOL
+
+
+# ----------------------------------------------------------------- leftover mode (compactFock)
+def test_leftover_golden(cuda, diagonal_golden):
+    """hermite_multidimensional_1leftoverMode and its gradient on the device against the reference
+    source: the five block arrays (zero patterns equal) and (dG0, dA, dB)."""
+    import mrmustard_gb300 as gb
+
+    g = diagonal_golden
+    for n in diagonal_cases(g, "lo"):
+        A, B, G0, cut = g[f"{n}/A"], g[f"{n}/B"], g[f"{n}/G0"], tuple(g[f"{n}/cutoffs"])
+        arrs = gb.hermite_multidimensional_1leftoverMode(A, B, G0, cut)
+        for name, x in zip(("arr0", "arr2", "arr1010", "arr1001", "arr1"), arrs):
+            ref = g[f"{n}/{name}"]
+            assert x.shape == ref.shape, (n, name)
+            assert np.array_equal(x == 0, ref == 0), (n, name)
+            assert _rel(x, ref) <= TOL, (n, name, _rel(x, ref))
+        for name, x in zip(("dG0", "dA", "dB"), gb.grad_hermite_multidimensional_1leftoverMode(A, B, G0, *arrs)):
+            ref = g[f"{n}/{name}"]
+            assert x.shape == ref.shape, (n, name)
+            assert _rel(x, ref) <= TOL_JAC, (n, name, _rel(x, ref))
+
+
+@pytest.mark.parametrize("M,cut", [(2, (20, 15)), (3, (10, 6, 6)), (4, (6, 4, 4, 4)), (5, (4, 3, 3, 3, 3))])
+def test_leftover_vs_oracle(cuda, M, cut):
+    import mrmustard_gb300 as gb
+
+    A, b, c = _dm_triple(M, 120 + M)
+    Ai, bi = _interleave(A, b)
+    got = gb.hermite_multidimensional_1leftoverMode(Ai, bi, c, cut)
+    ref = oracle.leftover_amps(Ai, bi, c, cut)
+    for name, x, r in zip(("arr0", "arr2", "arr1010", "arr1001", "arr1"), got, ref):
+        assert np.array_equal(x == 0, r == 0), name
+        assert _rel(x, r) <= TOL, (name, _rel(x, r))
+
+
+@pytest.mark.parametrize("M,cut", [(2, (6, 5)), (3, (4, 3, 3))])
+def test_leftover_jacobian_vs_oracle(cuda, M, cut):
+    import mrmustard_gb300 as gb
+
+    A, b, c = _dm_triple(M, 140 + M)
+    Ai, bi = _interleave(A, b)
+    arrs = gb.hermite_multidimensional_1leftoverMode(Ai, bi, c, cut)
+    got = gb.grad_hermite_multidimensional_1leftoverMode(Ai, bi, c, *arrs)
+    for x, r in zip(got, oracle.leftover_grad(Ai, bi, c, cut)):
+        assert _rel(x, r) <= TOL_JAC
+
+
+def test_leftover_jax_path_equals_vanilla(cuda):
+    """tests/test_math/test_compactFock.py:46-69 under the JAX backend's path: output cutoff 3, PNR
+    cutoffs (1, 2) on a Bargmann-order triple equal the vanilla tensor's diagonal blocks."""
+    import torch
+
+    import mrmustard_gb300 as gb
+
+    A, b, c = _dm_triple(3, 11)
+    got = gb.hermite_renormalized_1leftoverMode_autograd(torch.tensor(A, device=cuda), torch.tensor(b, device=cuda),
+                                                         torch.tensor(c, device=cuda), 3, (1, 2))
+    G = gb.vanilla_numba((4, 2, 3, 4, 2, 3), A, b, c)
+    expected = np.diagonal(np.diagonal(G, axis1=1, axis2=4), axis1=1, axis2=3)
+    assert got.shape == (4, 4, 2, 3)
+    assert np.allclose(expected, got.detach().cpu().numpy())
+
+
+def test_leftover_autograd_matches_jacobian_contraction(cuda):
+    import torch
+
+    import mrmustard_gb300 as gb
+
+    A, b, c = _dm_triple(3, 12)
+    At = torch.tensor(A, device=cuda, requires_grad=True)
+    bt = torch.tensor(b, device=cuda, requires_grad=True)
+    ct = torch.tensor(c, device=cuda, requires_grad=True)
+    out = gb.hermite_renormalized_1leftoverMode_autograd(At, bt, ct, 3, (2, 1))
+    rng = np.random.default_rng(4)
+    w = rng.standard_normal(out.shape) + 1j * rng.standard_normal(out.shape)
+    torch.real(torch.sum(torch.tensor(w, device=cuda) * out)).backward()
+    Ai, bi = _interleave(A, b)
+    dG0, dA, dB = oracle.leftover_grad(Ai, bi, c, (4, 3, 2))
+    exp_A = np.einsum("k,kpq->pq", w.reshape(-1), dA.reshape(-1, 6, 6)).conj()
+    exp_B = np.einsum("k,kp->p", w.reshape(-1), dB.reshape(-1, 6)).conj()
+    exp_c = np.sum(w * dG0).conj()
+    inv = np.argsort(np.arange(6).reshape(2, -1).T.flatten())
+    assert _rel(At.grad.cpu().numpy(), exp_A[inv][:, inv]) <= 1e-12
+    assert _rel(bt.grad.cpu().numpy(), exp_B[inv]) <= 1e-12
+    assert abs(ct.grad.item() - exp_c) <= 1e-12 * abs(exp_c)
+
+
+def test_leftover_validation(cuda):
+    import mrmustard_gb300 as gb
+
+    A, b, c = _dm_triple(1, 13)
+    with pytest.raises(ValueError, match="greater than 1"):
+        gb.hermite_multidimensional_1leftoverMode(A, b, c, (3,))
+    A, b, c = _dm_triple(2, 13)
+    with pytest.raises(ValueError, match="incompatible"):
+        gb.hermite_multidimensional_1leftoverMode(A, b[:3], c, (3, 3))
