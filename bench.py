@@ -572,7 +572,9 @@ def _pnr_triple(M, seed, r_max=0.6, t_max=0.3, beta=0.4):
 def run_diagonal(dev, time_eager, with_cpu=True):
     """Diagonal strategies on mixed Gaussian states: PNR amplitudes of 4 modes at cutoff 12 (20,736
     lattice points), of 3 modes at cutoff 10 with 64 B vectors, their Jacobians (3 modes at cutoff 8),
-    and fast_diagonal of 3 modes (output cutoff 20, PNR cutoffs 10, 10) and 4 modes (10; 6, 6, 6).
+    compactFock's leftover-mode blocks of 3 modes (output cutoff 10, PNR cutoffs 10, 10) and their
+    Jacobians (5; 4, 4), and fast_diagonal of 3 modes (output cutoff 20, PNR cutoffs 10, 10) and
+    4 modes (10; 6, 6, 6).
     GPU time per call (device tensors in and out, Python included) against the C oracle on one core
     (the reference runs these single-threaded), with every output checked against the oracle."""
     import torch
@@ -629,6 +631,32 @@ def run_diagonal(dev, time_eager, with_cpu=True):
                              "sample": f"amplitudes and Jacobians, one pass, {tc * 1e3:.1f} ms",
                              "max_rel_err_vs_gpu": max(oracle.rel_err(x.cpu().numpy(), y) for x, y in zip(got, ref))}
     res["jacobian_3x8"] = r
+    # compactFock leftover mode (the JAX backend's path): amplitudes and Jacobians
+    for name, M, cut, jac in (("leftover_compact_3_oc10_pnr10x10", 3, (11, 11, 11), False),
+                              ("leftover_compact_jacobian_3_oc5_pnr4x4", 3, (6, 5, 5), True)):
+        A, b, c = _pnr_triple(M, 900 + M)
+        Ai, bi = ilv(A, b)
+        At, bt, ct = td(Ai), td(bi), td(c)
+        arrs = mm.hermite_multidimensional_1leftoverMode(At, bt, ct, cut)
+        if jac:
+            fn = lambda: mm.grad_hermite_multidimensional_1leftoverMode(At, bt, ct, *arrs)
+        else:
+            fn = lambda: mm.hermite_multidimensional_1leftoverMode(At, bt, ct, cut)
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            t = time_eager(fn, reps=10)
+        got = fn()
+        nout = int(np.prod(cut)) * cut[0]
+        r = {"modes": M, "cutoffs": list(cut), "block_entries": nout, "ms": t}
+        if with_cpu:
+            import oracle
+
+            t0 = time.perf_counter()
+            ref = oracle.leftover_grad(Ai, bi, c, cut) if jac else oracle.leftover_amps(Ai, bi, c, cut)
+            tc = time.perf_counter() - t0
+            r["cpu_baseline"] = {"value": tc * 1e3, "unit": "ms", "cores": 1, "kind": "port",
+                                 "sample": "the same call, one pass" + (" (amplitudes and Jacobians)" if jac else ""),
+                                 "max_rel_err_vs_gpu": max(oracle.rel_err(x.cpu().numpy(), y) for x, y in zip(got, ref))}
+        res[name] = r
     # fast_diagonal
     for name, L, oc, pnr in (("leftover_3_oc20_pnr10x10", 3, 20, (10, 10)), ("leftover_4_oc10_pnr6x6x6", 4, 10, (6, 6, 6))):
         A, b, c = _pnr_triple(L, 800 + L)
