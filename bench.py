@@ -376,7 +376,7 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
 
     e2e_steps = max(2, min(args.steps, 5))
     e2e_modes = {}
-    for mode in ("prefetch", "zero_copy"):
+    for mode in ("prefetch", "zero_copy", "pipelined", "fused"):
         with mm.settings(CHECK_DEVICE_STATUS=False):
             rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode)
             torch.cuda.synchronize()

@@ -179,6 +179,13 @@ MM_API int mm_ragged_fwd(const mm_ragged_plan *plan, const mm_c128 *A, const mm_
  * addresses, including pinned host memory (read by the kernels over the host link). */
 MM_API int mm_ragged_vjp(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG, mm_c128 *dA,
                   mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
+/* mm_ragged_vjp that also writes a copy of G (every amplitude, once) to G_copy, which may be
+ * pinned host memory: the VJP kernels store the G values they load anyway, so a host-buffer
+ * step gets G back over the host link while the VJP runs, without a copy-engine transfer.
+ * G_copy = NULL is mm_ragged_vjp.  (No counterpart in the reference.) */
+MM_API int mm_ragged_vjp_copy_g(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG,
+                                mm_c128 *dA, mm_c128 *db, mm_c128 *dc, mm_c128 *G_copy, void *ws, size_t ws_bytes,
+                                mm_stream_t stream);
 
 /* ------------------------------------------------------- Fock contraction */
 

@@ -55,6 +55,7 @@ SIGNATURES = {
     "mm_ragged_plan_upload": (I32, [P, P, SZ, P]),
     "mm_ragged_fwd": (I32, [P, P, P, P, I32, P, P, SZ, P]),
     "mm_ragged_vjp": (I32, [P, P, P, P, P, P, P, P, SZ, P]),
+    "mm_ragged_vjp_copy_g": (I32, [P, P, P, P, P, P, P, P, P, SZ, P]),
     "mm_test_wait_timeout": (I32, [P, SZ, U64, P]),
     "mm_probe_dfma": (I32, [P, I32, I32, P]),
     "mm_selftest": (I32, [P, SZ, P, ctypes.POINTER(I32)]),

@@ -427,6 +427,7 @@ RaggedSrc ragged_src(const mm_ragged_plan* p, char* ws, const double2* A, const 
   s.dLdG = dLdG;
   s.coef = reinterpret_cast<double2*>(ws + p->L.coef);
   s.items = reinterpret_cast<const VjpItem*>(ws + p->L.items);
+  s.Gout = nullptr;
   return s;
 }
 }  // namespace
@@ -752,6 +753,12 @@ int mm_ragged_fwd(const mm_ragged_plan* plan, const mm_c128* A, const mm_c128* b
 
 int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c, const mm_c128* dLdG, mm_c128* dA,
                   mm_c128* db, mm_c128* dc, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  return mm_ragged_vjp_copy_g(plan, G, c, dLdG, dA, db, dc, nullptr, ws, ws_bytes, stream);
+}
+
+int mm_ragged_vjp_copy_g(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c, const mm_c128* dLdG,
+                         mm_c128* dA, mm_c128* db, mm_c128* dc, mm_c128* G_copy, void* ws, size_t ws_bytes,
+                         mm_stream_t stream) {
   if (!plan) return MM_ERR_INVALID_ARG;
   DevInfo di;
   int rc = device_info(di);
@@ -762,6 +769,7 @@ int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   RaggedSrc src = ragged_src(plan, w, nullptr, nullptr, (const double2*)c, (double2*)G, (const double2*)dLdG);
+  src.Gout = (double2*)G_copy;
   if ((rc = reset_launch_state(w, st))) return rc;
   if ((rc = launch_setup(src, plan->B, w, plan->L, 0, st))) return rc;
   double2* partials = reinterpret_cast<double2*>(w + plan->L.partials);
@@ -769,9 +777,16 @@ int mm_ragged_vjp(const mm_ragged_plan* plan, const mm_c128* G, const mm_c128* c
   const int64_t n_items = (int64_t)plan->items.size();
   for (int64_t done = 0; done < n_items;) {
     const unsigned nb = (unsigned)std::min<int64_t>(n_items - done, INT32_MAX);
-    if (plan->maxD <= 2) vjp_items_kernel<1, 2, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
-    else if (plan->maxD <= 4) vjp_items_kernel<1, 4, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
-    else vjp_items_kernel<1, 8, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+    if (G_copy == nullptr) {
+      if (plan->maxD <= 2) vjp_items_kernel<1, 2, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+      else if (plan->maxD <= 4) vjp_items_kernel<1, 4, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+      else vjp_items_kernel<1, 8, RaggedSrc><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+    } else {
+      if (plan->maxD <= 2) vjp_items_kernel<1, 2, RaggedSrc, true><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+      else if (plan->maxD <= 4)
+        vjp_items_kernel<1, 4, RaggedSrc, true><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+      else vjp_items_kernel<1, 8, RaggedSrc, true><<<nb, MM_BLOCK, 0, st>>>(src, T, partials, done);
+    }
     MM_LAUNCHED();
     done += nb;
   }

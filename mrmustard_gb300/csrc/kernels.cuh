@@ -102,6 +102,7 @@ struct UniformSrc {
   }
   __device__ __forceinline__ const Geom& geom(int64_t) const { return g; }
   __device__ __forceinline__ double2* coef_of(int64_t k) const { return coef + k * coef_stride; }
+  __device__ __forceinline__ double2* gout_of(int64_t) const { return nullptr; }
   __device__ __forceinline__ void item(int64_t it, int64_t& k, uint32_t& q0, uint32_t& q1) const {
     k = it / items_per_inst;
     const int64_t r = it - k * items_per_inst;
@@ -129,8 +130,10 @@ struct RaggedSrc {
   const double2* dLdG;
   double2* coef;
   const VjpItem* items;
+  double2* Gout;  // optional copy of G written by the VJP (may be pinned host memory), or null
   __device__ __forceinline__ int64_t n_inst() const { return B; }
   __device__ __forceinline__ int64_t sched(int64_t t) const { return order[t]; }
+  __device__ __forceinline__ double2* gout_of(int64_t k) const { return Gout ? Gout + desc[k].g_off : nullptr; }
   __device__ __forceinline__ void load(int64_t k, InstView& v) const {
     const InstDesc& d = desc[k];
     copy_geom(v.g, d.g);
@@ -1125,9 +1128,11 @@ __global__ void __launch_bounds__(256) binomial_mask_kernel(double2* __restrict_
 // ============================================================== VJP
 // Per-thread accumulation over the fibers q of [q0, q1) (q = flat index over
 // axes 1..D-1) for one instance; results go to tot[] (weights applied).
-template <int D>
+// gout (optional): receives G[f] for every amplitude of the item's fibers, so a caller that
+// needs G elsewhere (pinned host memory) gets it from the loads the VJP makes anyway.
+template <int D, bool COPY = false>
 __device__ __forceinline__ void vjp_fibers(const InstView& v, const Tables& T, uint32_t q0, uint32_t q1,
-                                           double2 (&tot)[vjp_nv(D)]) {
+                                           double2 (&tot)[vjp_nv(D)], double2* gout = nullptr) {
   constexpr int NV = vjp_nv(D);
   const Geom& g = v.g;
   const int C0 = (int)g.shape[0];
@@ -1148,7 +1153,9 @@ __device__ __forceinline__ void vjp_fibers(const InstView& v, const Tables& T, u
     for (int m = 0; m < C0; ++m) {
       const int64_t f = (int64_t)m * s0 + q;
       const double2 gu = __ldg(gb + f);
-      a[0] = cfma(__ldg(G + f), gu, a[0]);
+      const double2 gf = __ldg(G + f);
+      a[0] = cfma(gf, gu, a[0]);
+      if constexpr (COPY) gout[f] = gf;
       if (m >= 1) {
         const double2 h0 = cscale(sq[m], gu);
         a[1] = cfma(__ldg(G + f - s0), h0, a[1]);
@@ -1215,12 +1222,13 @@ __device__ __forceinline__ void block_reduce_write(double2 (&tot)[NV], double2* 
 }
 
 // One CTA per work item; partial sums to partials[item * MM_NV_MAX + slot].
-template <int DLO, int DHI, class Src>
+template <int DLO, int DHI, class Src, bool COPY = false>
 __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, double2* __restrict__ partials,
                                                              int64_t item_base) {
   MM_SHARED(InstView, sv);
   MM_SHARED(uint32_t, sq0);
   MM_SHARED(uint32_t, sq1);
+  MM_SHARED(double2*, sgo);
   const int64_t item = item_base + blockIdx.x;
   if (threadIdx.x == 0) {
     int64_t k;
@@ -1229,6 +1237,7 @@ __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, 
     src.load(k, sv);
     sq0 = q0;
     sq1 = q1;
+    if constexpr (COPY) sgo = src.gout_of(k);
   }
   __syncthreads();
   const int D = sv.g.D;
@@ -1238,7 +1247,7 @@ __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, 
     if (D == DD) {                                            \
       double2 tot[vjp_nv(DD)];                                \
       for (int s = 0; s < vjp_nv(DD); ++s) tot[s] = cmk(0, 0); \
-      vjp_fibers<DD>(sv, T, sq0, sq1, tot);                   \
+      vjp_fibers<DD, COPY>(sv, T, sq0, sq1, tot, sgo);        \
       block_reduce_write<vjp_nv(DD)>(tot, out);               \
       return;                                                 \
     }                                                         \

@@ -122,40 +122,87 @@ class RaggedBatch:
         self._check("ragged forward")
         return G
 
-    def vjp(self, G, c, dLdG, out=None):
+    def vjp(self, G, c, dLdG, out=None, G_copy=None):
         """(dA_flat, db_flat, dc) of every instance (holomorphic VJP, as vanilla_vjp_numba).
 
-        ``dLdG`` may be a pinned host tensor: the kernels then read it through the host link."""
+        ``dLdG`` may be a pinned host tensor: the kernels then read it through the host link.
+        ``G_copy`` (optional, e.g. a pinned host tensor of ``self.total``) receives a copy of G
+        written by the VJP kernels from the values they load."""
         lib = _lib.load()
         G, c, dLdG = raw(G), raw(c), raw(dLdG)
+        if G_copy is not None:
+            if G_copy.dtype != torch.complex128 or not G_copy.is_contiguous() or G_copy.numel() != self.total:
+                raise ValueError("G_copy must be a contiguous complex128 tensor of self.total elements")
         if out is None:
             dA = torch.empty(self.n_a, dtype=torch.complex128, device=self.device)
             db = torch.empty(self.n_b, dtype=torch.complex128, device=self.device)
             dc = torch.empty(self.B, dtype=torch.complex128, device=self.device)
         else:
             dA, db, dc = out
-        _lib.check(lib.mm_ragged_vjp(self._plan, G.data_ptr(), c.data_ptr(), dLdG.data_ptr(), dA.data_ptr(),
-                                     db.data_ptr(), dc.data_ptr(), self.ws.ptr, self.ws.nbytes, _stream()),
-                   "mm_ragged_vjp")
+        _lib.check(lib.mm_ragged_vjp_copy_g(self._plan, G.data_ptr(), c.data_ptr(), dLdG.data_ptr(), dA.data_ptr(),
+                                            db.data_ptr(), dc.data_ptr(), G_copy.data_ptr() if G_copy is not None else None,
+                                            self.ws.ptr, self.ws.nbytes, _stream()), "mm_ragged_vjp")
         self._check("ragged vjp")
         return dA, db, dc
 
+    def _chunks(self, n_chunks: int):
+        """Contiguous instance ranges with about equal amplitude counts, each with its own plan
+        (same schedule settings) whose packed buffers are slices of this batch's buffers."""
+        key = int(n_chunks)
+        cache = getattr(self, "_chunk_cache", {})
+        if key in cache:
+            return cache[key]
+        g_pref = np.concatenate([[0], np.cumsum(self.sizes)])
+        a_pref = np.concatenate([[0], np.cumsum(self.D.astype(np.int64) ** 2)])
+        b_pref = np.concatenate([[0], np.cumsum(self.D.astype(np.int64))])
+        if not (np.array_equal(self.g_off, g_pref[:-1]) and np.array_equal(self.a_off, a_pref[:-1])
+                and np.array_equal(self.b_off, b_pref[:-1])):
+            raise RuntimeError("ragged packing is not in instance order; chunked steps need it")
+        cuts = [0]
+        for k in range(1, key):
+            cuts.append(int(np.searchsorted(g_pref, g_pref[-1] * k / key)))
+        cuts.append(self.B)
+        cuts = sorted(set(cuts))
+        chunks = []
+        for i0, i1 in zip(cuts[:-1], cuts[1:]):
+            if i1 <= i0:
+                continue
+            sub = RaggedBatch(self.shapes[i0:i1], device=self.device, team_min_amps=self.tuning["team_min_amps"],
+                              vjp_item_amps=self.tuning["vjp_item_amps"])
+            if self.tuning["team_cluster"] != sub.tuning["team_cluster"]:
+                sub.retune(team_cluster=self.tuning["team_cluster"])
+            chunks.append((i0, i1, int(g_pref[i0]), int(g_pref[i1]), int(a_pref[i0]), int(a_pref[i1]),
+                           int(b_pref[i0]), int(b_pref[i1]), sub))
+        cache[key] = chunks
+        self._chunk_cache = cache
+        return chunks
+
     def step_host(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable: bool = False,
-                  cotangent: str = "zero_copy"):
+                  cotangent: str = "zero_copy", chunks: int = 2):
         """One forward + VJP step with every input and output in pinned host memory.
 
         A, b, c (small) are copied to the device and the forward writes G in device memory; G is
         copied back on a second stream while the VJP runs.  The cotangent dL/dG reaches the VJP in
-        one of two ways, both overlapped with compute:
+        one of three ways, all overlapped with compute:
 
         * ``"prefetch"``: copied into device memory on the second stream while the forward runs;
         * ``"zero_copy"``: read by the VJP kernels straight from the pinned host buffer over the
-          host link (the GPU addresses pinned host memory directly; no device copy is kept).
+          host link (the GPU addresses pinned host memory directly; no device copy is kept);
+        * ``"pipelined"``: copied into device memory in ``chunks`` instance ranges on a third stream
+          while the forward runs, the VJP of each range starting as soon as its part has arrived,
+          so the cotangent upload, the G download and the kernels overlap;
+        * ``"fused"``: read zero-copy as in ``"zero_copy"``, and G is written to ``G_h`` by the VJP
+          kernels themselves (``mm_ragged_vjp_copy_g``) instead of a copy-engine transfer, so both
+          directions of the host link are driven by the kernels.
 
         Enqueued asynchronously on the current stream; synchronise before reading the outputs.
         """
-        if cotangent not in ("prefetch", "zero_copy"):
-            raise ValueError("cotangent must be 'prefetch' or 'zero_copy'")
+        if cotangent not in ("prefetch", "zero_copy", "pipelined", "fused"):
+            raise ValueError("cotangent must be 'prefetch', 'zero_copy', 'pipelined' or 'fused'")
+        if cotangent == "pipelined":
+            return self._step_host_pipelined(A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable, chunks)
+        if cotangent == "fused":
+            return self._step_host_fused(A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable)
         cur = torch.cuda.current_stream(self.device)
         if getattr(self, "_dev_bufs", None) is None:
             mk = lambda n: torch.empty(n, dtype=torch.complex128, device=self.device)  # noqa: E731
@@ -194,6 +241,70 @@ class RaggedBatch:
         db_h.copy_(grads[1], non_blocking=True)
         dc_h.copy_(grads[2], non_blocking=True)
         cur.wait_stream(cs)
+        return G_h, (dA_h, db_h, dc_h)
+
+    def _step_host_fused(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable):
+        if getattr(self, "_dev_bufs", None) is None:
+            mk = lambda n: torch.empty(n, dtype=torch.complex128, device=self.device)  # noqa: E731
+            self._dev_bufs = (mk(self.n_a), mk(self.n_b), mk(self.B), mk(self.total),
+                              (mk(self.n_a), mk(self.n_b), mk(self.B)))
+            self._copy_stream = torch.cuda.Stream(device=self.device)
+        for hbuf in (dLdG_h, G_h):
+            if hbuf.is_cuda or not hbuf.is_pinned():
+                raise ValueError("dLdG_h and G_h must be pinned host tensors")
+        A, b, c, G, grads = self._dev_bufs
+        A.copy_(A_h, non_blocking=True)
+        b.copy_(b_h, non_blocking=True)
+        c.copy_(c_h, non_blocking=True)
+        self.forward(A, b, c, stable, out=G)
+        self.vjp(G, c, dLdG_h, out=grads, G_copy=G_h)
+        dA_h.copy_(grads[0], non_blocking=True)
+        db_h.copy_(grads[1], non_blocking=True)
+        dc_h.copy_(grads[2], non_blocking=True)
+        return G_h, (dA_h, db_h, dc_h)
+
+    def _step_host_pipelined(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable, n_chunks):
+        cur = torch.cuda.current_stream(self.device)
+        if getattr(self, "_dev_bufs", None) is None:
+            mk = lambda n: torch.empty(n, dtype=torch.complex128, device=self.device)  # noqa: E731
+            self._dev_bufs = (mk(self.n_a), mk(self.n_b), mk(self.B), mk(self.total),
+                              (mk(self.n_a), mk(self.n_b), mk(self.B)))
+            self._copy_stream = torch.cuda.Stream(device=self.device)
+        if getattr(self, "_g_dev", None) is None:
+            self._g_dev = torch.empty(self.total, dtype=torch.complex128, device=self.device)
+        if getattr(self, "_up_stream", None) is None:
+            self._up_stream = torch.cuda.Stream(device=self.device)
+        for hbuf in (dLdG_h, G_h):
+            if hbuf.is_cuda or not hbuf.is_pinned():
+                raise ValueError("dLdG_h and G_h must be pinned host tensors")
+        A, b, c, G, (dA, db, dc) = self._dev_bufs
+        parts = self._chunks(n_chunks)
+        up, down = self._up_stream, self._copy_stream
+        up.wait_stream(cur)    # the previous step's VJPs have read the device cotangent
+        down.wait_stream(cur)  # and nothing still reads G
+        ready = []
+        with torch.cuda.stream(up):
+            for (_, _, g0, g1, *_rest) in parts:
+                self._g_dev[g0:g1].copy_(dLdG_h[g0:g1], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(up)
+                ready.append(ev)
+        A.copy_(A_h, non_blocking=True)
+        b.copy_(b_h, non_blocking=True)
+        c.copy_(c_h, non_blocking=True)
+        self.forward(A, b, c, stable, out=G)
+        fwd_done = torch.cuda.Event()
+        fwd_done.record(cur)
+        with torch.cuda.stream(down):
+            down.wait_event(fwd_done)
+            G_h.copy_(G, non_blocking=True)
+        for ev, (i0, i1, g0, g1, a0, a1, b0, b1, sub) in zip(ready, parts):
+            cur.wait_event(ev)
+            sub.vjp(G[g0:g1], c[i0:i1], self._g_dev[g0:g1], out=(dA[a0:a1], db[b0:b1], dc[i0:i1]))
+        dA_h.copy_(dA, non_blocking=True)
+        db_h.copy_(db, non_blocking=True)
+        dc_h.copy_(dc, non_blocking=True)
+        cur.wait_stream(down)
         return G_h, (dA_h, db_h, dc_h)
 
     def capture(self, A, b, c, dLdG, stable: bool = False, warmup: int = 1):

@@ -457,8 +457,9 @@ def test_launch_count_increments(cuda):
 
 
 def test_ragged_step_host_matches_device(cuda, oracle_lib):
-    """The host-buffer step (cotangent read from pinned host memory, G copied back while the
-    VJP runs) gives the same bits as the device-resident forward + VJP."""
+    """The host-buffer step (cotangent prefetched, read from pinned host memory, or uploaded in
+    instance chunks whose VJPs start as they arrive; G copied back while the VJP runs) gives the
+    same bits as the device-resident forward + VJP."""
     shapes, As, bs, cs = _ragged_case(48, 21, cmax=9)
     rb = mm.RaggedBatch(shapes)
     A, b, c = rb.pack(As, bs, cs)
@@ -469,12 +470,15 @@ def test_ragged_step_host_matches_device(cuda, oracle_lib):
     A_h, b_h, c_h, g_h = pin(A), pin(b), pin(c), pin(g)
     G_h = torch.empty(rb.total, dtype=torch.complex128).pin_memory()
     outs = [torch.empty(n, dtype=torch.complex128).pin_memory() for n in (rb.n_a, rb.n_b, rb.B)]
-    for mode in ("prefetch", "zero_copy", "prefetch"):
-        rb.step_host(A_h, b_h, c_h, g_h, G_h, *outs, cotangent=mode)
+    for mode, chunks in (("prefetch", 2), ("zero_copy", 2), ("pipelined", 2), ("pipelined", 3), ("prefetch", 2),
+                         ("pipelined", 5), ("fused", 2), ("zero_copy", 2), ("fused", 2)):
+        for o in (G_h, *outs):
+            o.fill_(float("nan"))
+        rb.step_host(A_h, b_h, c_h, g_h, G_h, *outs, cotangent=mode, chunks=chunks)
         torch.cuda.synchronize()
-        assert torch.equal(G_h, G_ref.cpu())
+        assert torch.equal(G_h, G_ref.cpu()), mode
         for o, r in zip(outs, ref):
-            assert torch.equal(o, r.cpu())
+            assert torch.equal(o, r.cpu()), (mode, chunks)
 
 
 def test_ragged_schedules_agree(cuda, oracle_lib):
