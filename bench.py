@@ -335,7 +335,10 @@ def run_gb300(args, rank, local_rank, world):
                          "algorithmic_bytes_per_launch": bytes_dom, "ms_per_launch": t_dom,
                          "fp64": {"achieved_dfma_per_s": ops_dom / (t_dom * 1e-3), "peak_dfma_per_s": dfma_peak,
                                   "frac": ops_dom / (t_dom * 1e-3) / dfma_peak,
-                                  "peak_kind": "measured (mm_probe_dfma)"}},
+                                  "peak_kind": "measured (mm_probe_dfma)"},
+                         "binding_pipe": "fp64",
+                         "note": "the recurrence and its VJP are FP64 arithmetic on a part with 1/64-rate FP64: "
+                                 "the FP64 pipe (fp64.frac, of the measured DFMA peak) binds, not HBM"},
             "kernels_ms": {"forward": t_fwd, "vjp": t_vjp},
             "plain_loop": {"value": plain_value, "unit": UNIT, "sample": "256 instances, device_fwd + device_vjp per "
                            "instance", "batched_over_plain": value / world / plain_value},
@@ -449,6 +452,8 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
     extras["binomial"] = run_binomial(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
     extras["diagonal"] = run_diagonal(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
     extras["einsum"] = run_einsum(dev, time_eager, with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
+    extras["plain_and_gradient"] = run_plain_and_gradient(dev, time_eager,
+                                                          with_cpu=(rank == 0 and world == 1 and not args.skip_cpu))
 
     extras["fock_contraction"] = run_contraction(dev, time_eager)
     return e2e_ms, h2d, d2h, plain_value, cpu, extras
@@ -723,6 +728,116 @@ def run_einsum(dev, time_eager, with_cpu=True):
     return res
 
 
+def run_plain_and_gradient(dev, time_eager, with_cpu=True):
+    """The plain and the differentiation configurations: one 3-mode pure state at cutoff 20 (8,000
+    amplitudes; latency of the public call with numpy in and out, and of the device call), one
+    4-mode triple at cutoff 30 through the autograd function (forward + backward with a complex
+    normal upstream gradient), and the 64-instance batched gradient step whose loss is the fidelity
+    of each state to a fixed random normalised target Fock tensor (forward, loss, backward).  CPU
+    oracle on one core for the single-instance ones (the reference's numba path is single-threaded
+    per instance)."""
+    import torch
+    from scipy.stats import unitary_group
+
+    import mrmustard_gb300 as mm
+
+    def takagi(D, smax, seed):
+        rng = np.random.default_rng(seed)
+        Q = unitary_group.rvs(D, random_state=rng)
+        A = (Q * rng.uniform(0.0, smax, D)) @ Q.T
+        b = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+        return A.astype(np.complex128), b.astype(np.complex128)
+
+    res = {}
+    # plain 3 x 20
+    A, b = takagi(3, 0.8, 7070)
+    shape = (20, 20, 20)
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        mm.hermite_renormalized(A, b, 1.0 + 0j, shape)
+        t_api = time_eager(lambda: mm.hermite_renormalized(A, b, 1.0 + 0j, shape), reps=50)
+        Ad, bd = torch.as_tensor(A, device=dev), torch.as_tensor(b, device=dev)
+        cd = torch.tensor(1.0 + 0j, dtype=torch.complex128, device=dev)
+        out = torch.empty(shape, dtype=torch.complex128, device=dev)
+        t_dev = time_eager(lambda: mm.device_fwd(Ad, bd, cd, shape, out=out), reps=50)
+    r = {"shape": list(shape), "amplitudes": 8000, "us_per_call_numpy_api": t_api * 1e3,
+         "us_per_call_device": t_dev * 1e3, "amplitudes_per_s_device": 8000 / (t_dev * 1e-3)}
+    if with_cpu:
+        import oracle
+
+        G = mm.hermite_renormalized(A, b, 1.0 + 0j, shape)
+        t0 = time.perf_counter()
+        for _ in range(20):
+            ref = oracle.vanilla(shape, A, b, 1.0 + 0j)
+        tc = (time.perf_counter() - t0) / 20
+        r["cpu_baseline"] = {"value": tc * 1e6, "unit": "us per call", "cores": 1, "kind": "port",
+                             "sample": "the same call, 20 passes", "max_rel_err_vs_gpu": oracle.rel_err(G, ref)}
+    res["plain_3x20"] = r
+    # autograd 4 x 30
+    A, b = takagi(4, 0.8, 7171)
+    shape = (30,) * 4
+    At = torch.as_tensor(A, device=dev).requires_grad_(True)
+    bt = torch.as_tensor(b, device=dev).requires_grad_(True)
+    ct = torch.tensor(1.0 + 0j, dtype=torch.complex128, device=dev, requires_grad=True)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(71)
+    gup = torch.complex(torch.randn(shape, generator=gen, device=dev, dtype=torch.float64),
+                        torch.randn(shape, generator=gen, device=dev, dtype=torch.float64))
+
+    def step():
+        G = mm.hermite_renormalized_autograd(At, bt, ct, shape)
+        G.backward(gup)
+
+    def wall_ms(fn, reps):
+        # autograd runs the backward on its own thread: time with a host clock between synchronisations
+        fn()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        t = wall_ms(step, reps=20)
+    r = {"shape": list(shape), "amplitudes": 30 ** 4, "ms_fwd_bwd": t, "amplitudes_per_s": 30 ** 4 / (t * 1e-3),
+         "timing": "host clock between device synchronisations"}
+    if with_cpu:
+        import oracle
+
+        t0 = time.perf_counter()
+        G = oracle.vanilla(shape, A, b, 1.0 + 0j)
+        oracle.vjp(G, 1.0 + 0j, gup.cpu().numpy())
+        tc = time.perf_counter() - t0
+        r["cpu_baseline"] = {"value": tc * 1e3, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": "forward + VJP of the same triple, one pass"}
+    res["autograd_4x30"] = r
+    # 64-instance batched fidelity gradient step
+    B = 64
+    trip = [takagi(4, 0.8, 7300 + k) for k in range(B)]
+    Ab = torch.as_tensor(np.stack([t[0] for t in trip]), device=dev).requires_grad_(True)
+    bb = torch.as_tensor(np.stack([t[1] for t in trip]), device=dev).requires_grad_(True)
+    cb = torch.ones(B, dtype=torch.complex128, device=dev, requires_grad=True)
+    T = torch.complex(torch.randn(shape, generator=gen, device=dev, dtype=torch.float64),
+                      torch.randn(shape, generator=gen, device=dev, dtype=torch.float64))
+    T = T / T.abs().pow(2).sum().sqrt()
+
+    def fid_step():
+        for x in (Ab, bb, cb):
+            x.grad = None
+        G = mm.hermite_renormalized_autograd(Ab, bb, cb, shape)
+        ov = (T.conj() * G).sum(dim=(1, 2, 3, 4))
+        loss = (1 - ov.abs() ** 2 / G.abs().pow(2).sum(dim=(1, 2, 3, 4))).sum()
+        loss.backward()
+
+    with mm.settings(CHECK_DEVICE_STATUS=False):
+        t = wall_ms(fid_step, reps=5)
+    res["fidelity_step_64x4x30"] = {"instances": B, "shape": list(shape), "amplitudes": B * 30 ** 4,
+                                    "ms_per_step": t, "amplitudes_per_s": B * 30 ** 4 / (t * 1e-3),
+                                    "note": "forward, fidelity loss (torch reductions), backward; host clock between "
+                                            "device synchronisations"}
+    return res
+
+
 def run_single(dev, time_eager, dfma_peak=None):
     """Single large recurrences on the whole GPU (4 modes at cutoff 40, pure state; 4-index
     density-matrix triple at cutoff 50), timed with CUDA events; HBM and FP64-pipe fractions."""
@@ -827,6 +942,8 @@ def main(argv=None):
                     help="run only the Fock-contraction leg (gate tensor on 256 kets) and print its figures")
     ap.add_argument("--only-binomial", action="store_true",
                     help="run only the binomial fill of a 4-mode state at cutoff 30 (GPU and CPU oracle)")
+    ap.add_argument("--only-plain-gradient", action="store_true",
+                    help="run only the plain 3 x 20 call, the autograd 4 x 30 step and the 64-instance fidelity step")
     ap.add_argument("--only-einsum", action="store_true",
                     help="run only the Fock-space einsum cases (GPU and numpy on the host)")
     ap.add_argument("--only-diagonal", action="store_true",
@@ -841,7 +958,7 @@ def main(argv=None):
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     rank, local_rank, world = dist_env()
     if (args.only_contraction or args.only_single or args.only_autoshape or args.only_binomial or args.only_diagonal
-            or args.only_einsum):
+            or args.only_einsum or args.only_plain_gradient):
         import torch
 
         dev = torch.device("cuda", local_rank)
@@ -858,7 +975,10 @@ def main(argv=None):
             torch.cuda.synchronize()
             return e0.elapsed_time(e1) / reps
 
-        if args.only_einsum:
+        if args.only_plain_gradient:
+            print(json.dumps({"plain_and_gradient": run_plain_and_gradient(dev, time_eager, not args.skip_cpu)}),
+                  flush=True)
+        elif args.only_einsum:
             print(json.dumps({"einsum": run_einsum(dev, time_eager, not args.skip_cpu)}), flush=True)
         elif args.only_diagonal:
             print(json.dumps({"diagonal": run_diagonal(dev, time_eager, not args.skip_cpu)}), flush=True)

@@ -18,7 +18,7 @@ namespace {
 thread_local char g_last_cuda_error[256] = "";
 std::atomic<int64_t> g_launches{0};
 
-constexpr int64_t kGridMinAmps = 8192;     // single instances at least this large use the whole grid
+constexpr int64_t kGridMinAmps = 4096;     // single instances at least this large use the whole grid (default)
 constexpr int kGridBlock = 512;            // threads per CTA of the cooperative stable kernel
 constexpr int kFlowBlock = 256;            // dataflow forward: threads per CTA
 constexpr int kFlowPerSm = 2;              // dataflow forward: CTAs per SM (capped by occupancy)
@@ -27,6 +27,17 @@ constexpr uint32_t kFlowMinAmps = 128;     // dataflow forward: fewest amplitude
 constexpr int64_t kVjpItemAmps = 65536;    // default amplitudes per VJP work item
 constexpr int kTeamCluster = 8;            // CTAs per cluster for the large instances of a ragged batch
 constexpr size_t kAlign = 256;
+
+// Smallest single instance that runs on the whole grid (dataflow / cooperative kernels) instead of
+// one CTA; MM_GRID_MIN_AMPS overrides it (read once).
+int64_t grid_min_amps() {
+  static const int64_t v = [] {
+    const char* e = getenv("MM_GRID_MIN_AMPS");
+    return e ? std::max<int64_t>(64, atoll(e)) : kGridMinAmps;
+  }();
+  return v;
+}
+
 
 int cuda_fail(cudaError_t e) {
   snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
@@ -182,7 +193,7 @@ int plan_uniform(int64_t B, int D, const int64_t* shape, UniformPlan& P, int sms
   vjp_split(P.g, target, P.fpi, P.items_per_inst);
   // progress words of the dataflow forward (one large instance)
   const int64_t n_flags =
-      (fwd && B == 1 && P.g.n >= kGridMinAmps)
+      (fwd && B == 1 && P.g.n >= grid_min_amps())
           ? 1 + (int64_t)MM_MAXD * kFlowMaxPerSm * std::max(sms, 1) + (int64_t)kFlowMaxSmid
           : 0;
   P.L = make_layout(P.g.maxC + 1, B * coef_entries(P.g), B * P.items_per_inst, 0, 0, n_flags);
@@ -260,7 +271,7 @@ int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, 
                          cudaStream_t st) {
   const double* rs = tables_of(ws, P.L).rs;
   WsHeader* h = reinterpret_cast<WsHeader*>(ws);
-  if (P.B == 1 && P.g.n >= kGridMinAmps && di.coop && stable) {
+  if (P.B == 1 && P.g.n >= grid_min_amps() && di.coop && stable) {
     int per_sm = 0;
     MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stable_grid_kernel<D>, kGridBlock, 0));
     if (per_sm >= 1) {
@@ -272,7 +283,7 @@ int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, 
       return MM_OK;
     }
   }
-  if (P.B == 1 && P.g.n >= kGridMinAmps && di.coop && !stable) {
+  if (P.B == 1 && P.g.n >= grid_min_amps() && di.coop && !stable) {
     const FlowTuning t = flow_tuning();
     int occ = 0;
     MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_flow_kernel<D>, t.block, 0));

@@ -178,14 +178,16 @@ def test_cfg2_large_single(cuda, oracle_lib, case):
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < tol
 
 
-# A single instance of at least 8192 amplitudes runs the dataflow forward (per-range progress
+# A single instance of at least 4096 amplitudes runs the dataflow forward (per-range progress
 # words, shared-memory small levels, lane-pair chains).  Shapes chosen for the corners of its plan:
 # a 1-D chain; 2-D; no shared-memory region (an axis longer than 2560); axes of length 1; D = 7, 8;
 # a whole tensor's face in shared memory; a level-1 chunk split over more than half the SMs (no
-# exclusive SMs).
+# exclusive SMs); the smallest instances on the grid (4096 .. 8000 amplitudes, the 3-mode cutoff-20
+# state among them).
 @pytest.mark.parametrize("shape", [(9000,), (300, 40), (4, 5, 3000), (10, 1, 30, 40, 2), (20, 30, 15),
                                    (4, 4, 4, 4, 4, 4, 4), (2, 2, 2, 2, 2, 2, 2, 64), (60, 1, 1, 200),
-                                   (3, 10, 10000)])
+                                   (3, 10, 10000), (20, 20, 20), (16, 16, 16), (8, 8, 8, 8), (4096,), (64, 70),
+                                   (2, 2048), (5, 9, 100)])
 def test_single_instance_dataflow_shapes(cuda, oracle_lib, shape):
     A, b, c = takagi(len(shape), 0.8, 900 + sum(shape))
     Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
@@ -193,9 +195,9 @@ def test_single_instance_dataflow_shapes(cuda, oracle_lib, shape):
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
 
 
-def test_stable_large_single(cuda, oracle_lib):
-    A, b, c = takagi(4, 0.85, 204)
-    shape = (24,) * 4
+@pytest.mark.parametrize("shape", [(24,) * 4, (20, 20, 20), (16, 16, 16), (4096,), (8, 8, 8, 8)])
+def test_stable_large_single(cuda, oracle_lib, shape):
+    A, b, c = takagi(len(shape), 0.85, 204 + len(shape))
     G = mm.stable_numba(shape, A, b, c)
     assert rel(G, oracle_lib.stable(shape, A, b, c)) < FWD_TOL
 
