@@ -94,6 +94,17 @@ MM_API int mm_hermite_fwd(int D, const int64_t *shape, const mm_c128 *A, const m
 MM_API int mm_hermite_fwd_batched(int64_t B, int D, const int64_t *shape, const mm_c128 *A, const mm_c128 *b,
                            const mm_c128 *c, int stable, mm_c128 *G, void *ws, size_t ws_bytes, mm_stream_t stream);
 
+/*
+ * vanilla_numba / stable_numba with HOST buffers in and out -- the call the reference's
+ * numpy-in / numpy-out strategy makes (core.py:25-213): A (D x D), b (D), c (1) and G
+ * (prod(shape)) are ordinary host memory.  The library stages them through a pinned buffer and a
+ * device buffer of its own (allocated on first use per device, grown as needed, reused), runs
+ * mm_hermite_fwd on `stream`, and returns after G has been copied back (one synchronisation,
+ * which also reads the device status word).  Calls on one device are serialised.
+ */
+MM_API int mm_hermite_fwd_host(int D, const int64_t *shape, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c,
+                               int stable, mm_c128 *G, mm_stream_t stream);
+
 /* ---------------------------------------------------------------------- VJP */
 
 /*
@@ -136,6 +147,13 @@ MM_API int mm_hermite_vjp_batched(int64_t B, int D, const int64_t *shape, const 
  */
 MM_API int mm_hermite_vjp_noalloc(int D, const int64_t *shape, const mm_c128 *G, const mm_c128 *c,
                                   const mm_c128 *dLdG, mm_c128 *dA, mm_c128 *db, mm_c128 *dc, mm_stream_t stream);
+
+/*
+ * vanilla_vjp_numba(G, c, dLdG) with HOST buffers (G, dLdG: prod(shape); c: 1; dA: D x D; db: D;
+ * dc: 1), staged like mm_hermite_fwd_host; returns after the gradients are back on the host.
+ */
+MM_API int mm_hermite_vjp_host(int D, const int64_t *shape, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG,
+                               mm_c128 *dA, mm_c128 *db, mm_c128 *dc, mm_stream_t stream);
 
 /* ------------------------------------------------------------ ragged batches */
 

@@ -56,6 +56,8 @@ SIGNATURES = {
     "mm_ragged_fwd": (I32, [P, P, P, P, I32, P, P, SZ, P]),
     "mm_ragged_vjp": (I32, [P, P, P, P, P, P, P, P, SZ, P]),
     "mm_ragged_vjp_copy_g": (I32, [P, P, P, P, P, P, P, P, P, SZ, P]),
+    "mm_hermite_fwd_host": (I32, [I32, P, P, P, P, I32, P, P]),
+    "mm_hermite_vjp_host": (I32, [I32, P, P, P, P, P, P, P, P]),
     "mm_test_wait_timeout": (I32, [P, SZ, U64, P]),
     "mm_probe_dfma": (I32, [P, I32, I32, P]),
     "mm_selftest": (I32, [P, SZ, P, ctypes.POINTER(I32)]),

@@ -484,6 +484,101 @@ int launch_ragged_team(const mm_ragged_plan* p, const RaggedSrc& src, char* w, c
 
 void mm::note_launches(int64_t n) { g_launches.fetch_add(n); }
 
+// ------------------------------------------------------- host-buffer entry points
+// Per device: one pinned staging area and one device buffer (workspace, inputs, outputs), grown
+// on demand and reused; a call holds the device's mutex from the first copy to the last.
+namespace {
+struct HostStage {
+  std::mutex mu;
+  char* pin = nullptr;
+  size_t pin_bytes = 0;
+  char* dev = nullptr;
+  size_t dev_bytes = 0;
+  bool ws_fresh = false;
+};
+HostStage g_stage[64];
+
+int stage_reserve(HostStage& s, size_t pin_need, size_t dev_need) {
+  if (s.pin_bytes < pin_need) {
+    if (s.pin) MM_CUDA(cudaFreeHost(s.pin));
+    s.pin = nullptr;
+    s.pin_bytes = 0;
+    MM_CUDA(cudaMallocHost(reinterpret_cast<void**>(&s.pin), pin_need));
+    s.pin_bytes = pin_need;
+  }
+  if (s.dev_bytes < dev_need) {
+    if (s.dev) MM_CUDA(cudaFree(s.dev));
+    s.dev = nullptr;
+    s.dev_bytes = 0;
+    MM_CUDA(cudaMalloc(reinterpret_cast<void**>(&s.dev), dev_need));
+    s.dev_bytes = dev_need;
+    s.ws_fresh = true;
+  }
+  return MM_OK;
+}
+
+// Runs `compute` on device copies of `ins` (host buffers, concatenated) and copies `outs` back;
+// the workspace sits at the start of the device buffer and its status word comes back with the
+// outputs in the same synchronisation.
+struct HostSeg {
+  const void* host;
+  size_t bytes;
+};
+struct HostOut {
+  void* host;
+  size_t bytes;
+};
+template <class F>
+int run_host_staged(size_t ws_bytes, const HostSeg* ins, int n_in, const HostOut* outs, int n_out, cudaStream_t st,
+                    F compute) {
+  int dev = 0;
+  MM_CUDA(cudaGetDevice(&dev));
+  HostStage& s = g_stage[dev & 63];
+  std::lock_guard<std::mutex> lk(s.mu);
+  size_t in_bytes = 0, out_bytes = 0;
+  for (int i = 0; i < n_in; ++i) in_bytes += align_up(ins[i].bytes);
+  for (int i = 0; i < n_out; ++i) out_bytes += align_up(outs[i].bytes);
+  const size_t d_in = align_up(ws_bytes), d_out = d_in + in_bytes;
+  const size_t p_status = in_bytes, p_out = p_status + kAlign;
+  int rc = stage_reserve(s, p_out + out_bytes, d_out + out_bytes);
+  if (rc) return rc;
+  if (s.ws_fresh) {
+    MM_CUDA(cudaMemsetAsync(s.dev, 0, sizeof(WsHeader), st));
+    s.ws_fresh = false;
+  }
+  std::vector<char*> din(n_in), dout(n_out);
+  size_t o = 0;
+  for (int i = 0; i < n_in; ++i) {
+    memcpy(s.pin + o, ins[i].host, ins[i].bytes);
+    din[i] = s.dev + d_in + o;
+    o += align_up(ins[i].bytes);
+  }
+  if (in_bytes) MM_CUDA(cudaMemcpyAsync(s.dev + d_in, s.pin, in_bytes, cudaMemcpyHostToDevice, st));
+  o = 0;
+  for (int i = 0; i < n_out; ++i) {
+    dout[i] = s.dev + d_out + o;
+    o += align_up(outs[i].bytes);
+  }
+  if ((rc = compute(s.dev, din.data(), dout.data()))) return rc;
+  if (out_bytes) MM_CUDA(cudaMemcpyAsync(s.pin + p_out, s.dev + d_out, out_bytes, cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaMemcpyAsync(s.pin + p_status, s.dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaStreamSynchronize(st));
+  int32_t status = 0;
+  memcpy(&status, s.pin + p_status, sizeof(status));
+  if (status != 0) {
+    MM_CUDA(cudaMemsetAsync(s.dev, 0, sizeof(int32_t), st));
+    MM_CUDA(cudaStreamSynchronize(st));
+    return status;
+  }
+  o = 0;
+  for (int i = 0; i < n_out; ++i) {
+    memcpy(outs[i].host, s.pin + p_out + o, outs[i].bytes);
+    o += align_up(outs[i].bytes);
+  }
+  return MM_OK;
+}
+}  // namespace
+
 extern "C" {
 
 const char* mm_status_string(int status) {
@@ -549,6 +644,42 @@ int mm_hermite_fwd_batched(int64_t B, int D, const int64_t* shape, const mm_c128
 int mm_hermite_fwd(int D, const int64_t* shape, const mm_c128* A, const mm_c128* b, const mm_c128* c, int stable,
                    mm_c128* G, void* ws, size_t ws_bytes, mm_stream_t stream) {
   return mm_hermite_fwd_batched(1, D, shape, A, b, c, stable, G, ws, ws_bytes, stream);
+}
+
+int mm_hermite_fwd_host(int D, const int64_t* shape, const mm_c128* A, const mm_c128* b, const mm_c128* c, int stable,
+                        mm_c128* G, mm_stream_t stream) {
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  UniformPlan P;
+  if ((rc = plan_uniform(1, D, shape, P, di.sms))) return rc;
+  if (!A || !b || !c || !G) return MM_ERR_INVALID_ARG;
+  const size_t wsb = mm_hermite_workspace_bytes(D, shape, 1);
+  const HostSeg ins[3] = {{A, (size_t)D * D * sizeof(mm_c128)}, {b, (size_t)D * sizeof(mm_c128)}, {c, sizeof(mm_c128)}};
+  const HostOut outs[1] = {{G, (size_t)P.g.n * sizeof(mm_c128)}};
+  return run_host_staged(wsb, ins, 3, outs, 1, (cudaStream_t)stream, [&](char* ws, char** din, char** dout) {
+    return mm_hermite_fwd(D, shape, (const mm_c128*)din[0], (const mm_c128*)din[1], (const mm_c128*)din[2], stable,
+                          (mm_c128*)dout[0], ws, wsb, stream);
+  });
+}
+
+int mm_hermite_vjp_host(int D, const int64_t* shape, const mm_c128* G, const mm_c128* c, const mm_c128* dLdG,
+                        mm_c128* dA, mm_c128* db, mm_c128* dc, mm_stream_t stream) {
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  UniformPlan P;
+  if ((rc = plan_uniform(1, D, shape, P, di.sms, false))) return rc;
+  if (!G || !c || !dLdG || !dA || !db || !dc) return MM_ERR_INVALID_ARG;
+  const size_t wsb = mm_hermite_workspace_bytes(D, shape, 1);
+  const size_t nb = (size_t)P.g.n * sizeof(mm_c128);
+  const HostSeg ins[3] = {{G, nb}, {dLdG, nb}, {c, sizeof(mm_c128)}};
+  const HostOut outs[3] = {{dA, (size_t)D * D * sizeof(mm_c128)}, {db, (size_t)D * sizeof(mm_c128)},
+                           {dc, sizeof(mm_c128)}};
+  return run_host_staged(wsb, ins, 3, outs, 3, (cudaStream_t)stream, [&](char* ws, char** din, char** dout) {
+    return mm_hermite_vjp(D, shape, (const mm_c128*)din[0], (const mm_c128*)din[2], (const mm_c128*)din[1],
+                          (mm_c128*)dout[0], (mm_c128*)dout[1], (mm_c128*)dout[2], ws, wsb, stream);
+  });
 }
 
 // Binomial fill: the forward's workspace, then the per-weight sums of |G|^2

@@ -214,8 +214,37 @@ def _deliver(res: torch.Tensor, out, dev_mode: bool):
     return res if dev_mode else res.cpu().numpy()
 
 
+def _np_c128(x) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+
+
+def _fwd_host(shape, A, b, c, stable_flag, out):
+    """Unbatched forward with host (numpy) buffers: one library call that stages the inputs and the
+    result through its own pinned and device buffers (mm_hermite_fwd_host)."""
+    shape, sh = _shape_arr(shape)
+    D = len(shape)
+    A_h, b_h = _np_c128(A), _np_c128(b)
+    c_h = _np_c128(c).reshape(-1)[:1]
+    if A_h.shape != (D, D) or b_h.shape != (D,) or c_h.size != 1:
+        raise ValueError(f"A {A_h.shape} / b {b_h.shape} do not match the {D} axes of shape {shape}")
+    direct = (isinstance(out, np.ndarray) and out.dtype == np.complex128 and out.flags.c_contiguous
+              and out.size == int(np.prod(shape)))
+    target = out if direct else np.empty(shape, np.complex128)
+    if target.size:
+        ensure_device_ready(require_cuda())
+        _lib.check(_lib.load().mm_hermite_fwd_host(D, sh, A_h.ctypes.data, b_h.ctypes.data, c_h.ctypes.data,
+                                                   int(bool(stable_flag)), target.ctypes.data, _stream()),
+                   "mm_hermite_fwd_host")
+    if out is not None and not direct:
+        out[...] = target.reshape(out.shape)
+        return out
+    return target if out is None else out
+
+
 def _fwd_common(shape, A, b, c, stable_flag, out, batched):
     dev_mode, device = _host_or_dev(A, b, c, out)
+    if not dev_mode and not batched and not isinstance(out, torch.Tensor):
+        return _fwd_host(shape, A, b, c, stable_flag, out)
     A_d, b_d, c_d = _to_dev(A, device), _to_dev(b, device), _to_dev(c, device)
     direct = (
         isinstance(out, torch.Tensor) and out.is_cuda and out.is_contiguous() and out.dtype == torch.complex128
@@ -240,8 +269,33 @@ def vanilla_batch(shape, A, b, c, stable=False, out=None):
     return _fwd_common(shape, A, b, c, bool(stable), out, batched=True)
 
 
+def _vjp_host(G, c, dLdG):
+    """Unbatched VJP with host (numpy) buffers through mm_hermite_vjp_host."""
+    G_h, g_h = _np_c128(G), _np_c128(dLdG)
+    c_h = _np_c128(c).reshape(-1)[:1]
+    if G_h.shape != g_h.shape:
+        raise ValueError(f"dLdG shape {g_h.shape} must equal G shape {G_h.shape}")
+    shape, sh = _shape_arr(G_h.shape)
+    D = len(shape)
+    dA = np.empty((D, D), np.complex128)
+    db = np.empty(D, np.complex128)
+    dc = np.empty(1, np.complex128)
+    if G_h.size:
+        ensure_device_ready(require_cuda())
+        _lib.check(_lib.load().mm_hermite_vjp_host(D, sh, G_h.ctypes.data, c_h.ctypes.data, g_h.ctypes.data,
+                                                   dA.ctypes.data, db.ctypes.data, dc.ctypes.data, _stream()),
+                   "mm_hermite_vjp_host")
+    else:
+        dA[...] = 0
+        db[...] = 0
+        dc[...] = 0
+    return dA, db, complex(dc[0])
+
+
 def _vjp_common(G, c, dLdG, batched):
     dev_mode, device = _host_or_dev(G, c, dLdG)
+    if not dev_mode and not batched:
+        return _vjp_host(G, c, dLdG)
     G_d, c_d, g_d = _to_dev(G, device), _to_dev(c, device), _to_dev(dLdG, device)
     dA, db, dc = device_vjp(G_d, c_d, g_d, batched)
     if dev_mode:

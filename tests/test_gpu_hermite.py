@@ -579,3 +579,27 @@ def test_cfg4_batched_fidelity_step(cuda):
             E[k, i, j] = E[k, j, i] = h
             fd = (loss(A + E, b, c) - loss(A - E, b, c)).item() / (2 * h)
             assert abs(fd - (A.grad[k, i, j] + A.grad[k, j, i]).real.item()) < 1e-6
+
+
+@pytest.mark.parametrize("shape", [(20, 20, 20), (6, 5, 7), (30, 30, 30, 30), (4097,)])
+def test_host_buffer_entry_points_match_device(cuda, shape):
+    """mm_hermite_fwd_host / mm_hermite_vjp_host (numpy in, numpy out, staged through the library's
+    own pinned and device buffers) give the same bits as the device-tensor calls, into a caller's
+    `out` too (the reference returns `out` itself, test_vanilla.py:177-186)."""
+    D = len(shape)
+    A, b, c = takagi(D, 0.8, 1700 + D)
+    for stable in (False, True):
+        G_host = (mm.stable_numba if stable else mm.vanilla_numba)(shape, A, b, c)
+        G_dev = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
+                              torch.tensor(c, dtype=torch.complex128, device=cuda), shape, stable).cpu().numpy()
+        assert isinstance(G_host, np.ndarray) and G_host.shape == shape
+        assert np.array_equal(G_host, G_dev), stable
+        out = np.empty(shape, np.complex128)
+        assert (mm.stable_numba if stable else mm.vanilla_numba)(shape, A, b, c, out=out) is out
+        assert np.array_equal(out, G_dev)
+    g = cn(shape, 1701)
+    dA, db, dc = mm.vanilla_vjp_numba(G_host, c, g)
+    dA_d, db_d, dc_d = mm.device_vjp(torch.as_tensor(G_host, device=cuda), torch.tensor(c, dtype=torch.complex128,
+                                     device=cuda), torch.as_tensor(g, device=cuda), batched=False)
+    assert np.array_equal(dA, dA_d.cpu().numpy()) and np.array_equal(db, db_d.cpu().numpy())
+    assert dc == complex(dc_d.item())
