@@ -1548,6 +1548,7 @@ MM_API int mm_leftover_vjp(int M, const int64_t* cutoffs, const mm_c128* J, cons
   if (!J || !W || !G0 || !g || !dA || !dB || !dG0) return MM_ERR_INVALID_ARG;
   // arr0's Jacobian is [block entry][component] with the entries (m, n, params) flat, the layout
   // the diagonal strategy's VJP contracts: reuse it with 2M rows and q^2 P' entries.
+  if ((int64_t)q * q * L.P > INT32_MAX) return MM_ERR_TOO_LARGE;  // arr0 entries are counted in 32 bits
   DiagLat V;
   memset(&V, 0, sizeof(V));
   V.M = M;
