@@ -240,6 +240,10 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
  * max_l2 (or up to global_cutoff - 1), zeros elsewhere; *norm_out (device,
  * optional) that sum.  Pass max_l2 = +inf for no early stop.  Amplitudes equal
  * the vanilla recurrence's (same pivot rule).  ws: mm_binomial_workspace_bytes.
+ * With a finite max_l2 only the weights up to the stop are computed, weight by
+ * weight (one CTA, one thread-block cluster or a cooperative grid per weight,
+ * picked from the weight's size); with max_l2 = +inf the vanilla forward fills
+ * the tensor and the weights above global_cutoff - 1 are zeroed.
  */
 MM_API size_t mm_binomial_workspace_bytes(int D, const int64_t *shape);
 MM_API int mm_binomial(int D, const int64_t *shape, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c,

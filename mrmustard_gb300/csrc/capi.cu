@@ -1,6 +1,7 @@
 // C ABI of the GB300 Hermite library: argument checks, workspace layout,
 // ragged-batch planning and kernel launches.  See include/mm_gb300.h.
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -579,6 +580,208 @@ int run_host_staged(size_t ws_bytes, const HostSeg* ins, int n_in, const HostOut
 }
 }  // namespace
 
+// Binomial fill: the forward's workspace (setup tables), then the fill state,
+// the composition-count table and the per-CTA wave sums.  The waves run in up
+// to three launches picked from their sizes n_w (known on the host): waves of
+// at most MM_BLOCK amplitudes on one CTA, waves of at most one amplitude per
+// thread of a cluster on one thread-block cluster, larger waves on a
+// cooperative grid; each launch continues from the fill state the previous one
+// left (and returns at once when that state says the fill has stopped).
+namespace {
+constexpr int64_t kBnMaxW1 = 1 << 24;
+constexpr int kBnMaxTeam = 16;
+constexpr int kBnMaxPerSm = 2;
+constexpr size_t kBnStageBytes = 48 * 1024;
+
+struct BinomialPlan {
+  int64_t W1 = 0;      // max weight + 1
+  int64_t last = 0;    // last wave the reference would fill: global cutoff - 1, capped at the max weight
+  int64_t w_team = 0;  // first wave of the cluster launch
+  int64_t w_grid = 0;  // first wave of the grid launch
+  size_t off_state = 0, off_table = 0, off_part = 0, total = 0;
+};
+
+int binomial_env(const char* name, int dflt) {
+  const char* e = getenv(name);
+  return e ? atoi(e) : dflt;
+}
+
+// Workspace layout (team / grid only bound the wave-sum buffer).
+int binomial_layout(const UniformPlan& P, int sms, BinomialPlan& B) {
+  int64_t wmax = 0;
+  for (int i = 0; i < P.g.D; ++i) wmax += P.g.shape[i] - 1;
+  B.W1 = wmax + 1;
+  if (B.W1 > kBnMaxW1) return MM_ERR_TOO_LARGE;
+  const int parts = std::max(kBnMaxTeam, kBnMaxPerSm * sms);
+  B.off_state = align_up(P.L.total);
+  B.off_table = B.off_state + align_up(sizeof(BinomialState));
+  B.off_part = B.off_table + align_up((size_t)(P.g.D + 1) * (size_t)B.W1 * sizeof(int64_t));
+  B.total = B.off_part + align_up((size_t)2 * parts * sizeof(double));
+  return MM_OK;
+}
+
+// Wave sizes n_w = number of indices inside the cutoffs with |k| = w.
+std::vector<int64_t> binomial_wave_sizes(const Geom& g, int64_t W1) {
+  std::vector<int64_t> cnt((size_t)W1, 0), nxt((size_t)W1, 0);
+  cnt[0] = 1;
+  for (int j = g.D - 1; j >= 0; --j) {
+    int64_t run = 0;
+    for (int64_t x = 0; x < W1; ++x) {
+      run += cnt[(size_t)x];
+      if (x >= g.shape[j]) run -= cnt[(size_t)(x - g.shape[j])];
+      nxt[(size_t)x] = run;
+    }
+    cnt.swap(nxt);
+  }
+  return cnt;
+}
+
+cudaLaunchConfig_t cluster_config(cudaLaunchAttribute* attr, int cl, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)cl);
+  cfg.blockDim = dim3(MM_BLOCK);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+// Largest cluster (16, 8, 4, 2 CTAs) of which one can be resident, 0 if none.
+template <int D>
+int binomial_team_ctas() {
+  static std::atomic<int> cached{-1};
+  int v = cached.load();
+  if (v >= 0) return v;
+  auto kern = binomial_wave_kernel<D, 1>;
+  int best = 0;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    for (int cl : {16, 8, 4, 2}) {
+      cudaLaunchAttribute attr[1];
+      cudaLaunchConfig_t cfg = cluster_config(attr, cl, nullptr);
+      int ncl = 0;
+      if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) == cudaSuccess && ncl >= 1) {
+        best = cl;
+        break;
+      }
+    }
+  }
+  cudaGetLastError();
+  cached.store(best);
+  return best;
+}
+
+// No early stop: the vanilla forward over the whole tensor (every amplitude of
+// weight <= last is the binomial fill's), then the mask above `last` and the
+// norm of what is kept.
+int launch_binomial_nostop(const UniformPlan& P, const BinomialPlan& B, const UniformSrc& src, char* w,
+                           double* norm_out, const DevInfo& di, cudaStream_t st) {
+  int rc;
+  if ((rc = launch_fwd_uniform(P, src, w, 0, di, st))) return rc;
+  double* part = reinterpret_cast<double*>(w + B.off_part);
+  const int blocks = (int)std::min<int64_t>((P.g.n + 255) / 256, (int64_t)4 * di.sms);
+  double2* G = src.G;
+  switch (P.g.D) {
+#define MM_BN_CASE(DD)                                                                                    \
+  case DD:                                                                                                \
+    binomial_mask_norm_kernel<DD><<<(unsigned)blocks, 256, 0, st>>>(G, P.g, B.last, part);              \
+    break;
+    MM_BN_CASE(1)
+    MM_BN_CASE(2)
+    MM_BN_CASE(3)
+    MM_BN_CASE(4)
+    MM_BN_CASE(5)
+    MM_BN_CASE(6)
+    MM_BN_CASE(7)
+    MM_BN_CASE(8)
+#undef MM_BN_CASE
+    default:
+      return MM_ERR_UNSUPPORTED;
+  }
+  MM_LAUNCHED();
+  binomial_norm_final_kernel<<<1, 32, 0, st>>>(part, blocks, norm_out);
+  MM_LAUNCHED();
+  return MM_OK;
+}
+
+template <int D>
+int launch_binomial_D(const UniformPlan& P, const BinomialPlan& B, const UniformSrc& src, char* w, double max_l2,
+                      double* norm_out, const DevInfo& di, cudaStream_t st) {
+  const double* rs = tables_of(w, P.L).rs;
+  const int64_t* S = reinterpret_cast<const int64_t*>(w + B.off_table);
+  BinomialState* state = reinterpret_cast<BinomialState*>(w + B.off_state);
+  double* part = reinterpret_cast<double*>(w + B.off_part);
+  WsHeader* h = reinterpret_cast<WsHeader*>(w);
+  const int32_t W1 = (int32_t)B.W1;
+  uint64_t budget = wait_budget_ns();
+  // stage the read-only operands in shared memory when they fit the default 48 KiB
+  BinomialStage stage;
+  stage.table_n = (int32_t)((P.g.D + 1) * B.W1);
+  stage.coef_n = (int32_t)std::min<int64_t>(coef_entries(P.g), INT32_MAX);
+  stage.rs_n = P.g.maxC + 1;
+  if (bn_stage_bytes(stage) > kBnStageBytes) stage.coef_n = stage.rs_n = 0;
+  if (bn_stage_bytes(stage) > kBnStageBytes) stage.table_n = 0;
+  if (!binomial_env("MM_BINOMIAL_STAGE", 1)) stage.table_n = stage.coef_n = stage.rs_n = 0;
+  const size_t smem = bn_stage_bytes(stage);
+  binomial_table_kernel<<<1, 256, 0, st>>>(P.g, W1, const_cast<int64_t*>(S));
+  MM_LAUNCHED();
+
+  // launch split
+  int team = binomial_env("MM_BINOMIAL_TEAM", -1);
+  team = team < 0 ? binomial_team_ctas<D>() : std::min(team, binomial_team_ctas<D>());
+  int grid = 0;
+  if (di.coop && binomial_env("MM_BINOMIAL_GRID", 1)) {
+    int occ = 0;
+    MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, binomial_wave_kernel<D, 2>, MM_BLOCK, smem));
+    const int per_sm = std::min({occ, kBnMaxPerSm, std::max(1, binomial_env("MM_BINOMIAL_GRID_PER_SM", 1))});
+    grid = per_sm >= 1 ? per_sm * di.sms : 0;
+  }
+  const std::vector<int64_t> n = binomial_wave_sizes(P.g, B.W1);
+  const int64_t last = B.last;
+  // threads of the one-CTA and cluster launches (64, 128 or 256)
+  int nt = binomial_env("MM_BINOMIAL_BLOCK", MM_BLOCK);
+  nt = nt <= 64 ? 64 : nt <= 128 ? 128 : MM_BLOCK;
+  const int64_t cta_items = std::max(1, binomial_env("MM_BINOMIAL_CTA_ITEMS", nt));
+  const int64_t team_items = std::max<int64_t>(cta_items, binomial_env("MM_BINOMIAL_TEAM_ITEMS", team * nt));
+  int64_t w_team = 1;
+  while (w_team <= last && n[(size_t)w_team] <= cta_items) ++w_team;
+  int64_t w_grid = w_team;
+  if (team > 0)
+    while (w_grid <= last && n[(size_t)w_grid] <= team_items) ++w_grid;
+  if (grid <= 0) w_grid = last + 1;               // no cooperative grid: the cluster (or the CTA) goes on
+  if (team <= 0 && grid <= 0) w_team = last + 1;  // neither: one CTA fills every wave
+  if (team <= 0) w_team = w_grid;
+
+  binomial_wave_kernel<D, 0><<<1, nt, smem, st>>>(src, rs, S, W1, stage, 1, (int32_t)w_team, max_l2, part,
+                                                        state, norm_out, h, budget);
+  MM_LAUNCHED();
+  if (w_team < w_grid) {
+    auto kern = binomial_wave_kernel<D, 1>;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_config(attr, team, st);
+    cfg.blockDim = dim3((unsigned)nt);
+    cfg.dynamicSmemBytes = smem;
+    const int32_t wb = (int32_t)w_team, we = (int32_t)w_grid;
+    MM_CUDA(cudaLaunchKernelEx(&cfg, kern, src, rs, S, W1, stage, wb, we, max_l2, part, state, norm_out, h, budget));
+    g_launches.fetch_add(1);
+  }
+  if (w_grid <= last) {
+    UniformSrc s = src;
+    int32_t wb = (int32_t)w_grid, we = (int32_t)(last + 1);
+    void* args[] = {&s,  (void*)&rs, (void*)&S, (void*)&W1,     &stage, &wb, &we,
+                    &max_l2, &part,     &state,    &norm_out, &h,     &budget};
+    MM_CUDA(cudaLaunchCooperativeKernel((void*)binomial_wave_kernel<D, 2>, dim3((unsigned)grid), dim3(MM_BLOCK), args,
+                                        smem, st));
+    g_launches.fetch_add(1);
+  }
+  return MM_OK;
+}
+}  // namespace
+
 extern "C" {
 
 const char* mm_status_string(int status) {
@@ -682,22 +885,14 @@ int mm_hermite_vjp_host(int D, const int64_t* shape, const mm_c128* G, const mm_
   });
 }
 
-// Binomial fill: the forward's workspace, then the per-weight sums of |G|^2
-// and the stop weight.
-namespace {
-int64_t binomial_weights(const Geom& g) {
-  int64_t W = 1;
-  for (int i = 0; i < g.D; ++i) W += g.shape[i] - 1;
-  return W;
-}
-}  // namespace
-
 size_t mm_binomial_workspace_bytes(int D, const int64_t* shape) {
   DevInfo di;
   int sms = device_info(di) == MM_OK ? di.sms : 152;
   UniformPlan P;
   if (plan_uniform(1, D, shape, P, sms)) return 0;
-  return align_up(P.L.total) + align_up((size_t)(binomial_weights(P.g) + 2) * sizeof(double));
+  BinomialPlan B;
+  if (binomial_layout(P, sms, B)) return 0;
+  return B.total;
 }
 
 int mm_binomial(int D, const int64_t* shape, const mm_c128* A, const mm_c128* b, const mm_c128* c, double max_l2,
@@ -708,42 +903,31 @@ int mm_binomial(int D, const int64_t* shape, const mm_c128* A, const mm_c128* b,
   UniformPlan P;
   if ((rc = plan_uniform(1, D, shape, P, di.sms))) return rc;
   if (!A || !b || !c || !G) return MM_ERR_INVALID_ARG;
-  const size_t need = mm_binomial_workspace_bytes(D, shape);
-  if ((rc = check_ws(ws, ws_bytes, need))) return rc;
+  BinomialPlan B;
+  if ((rc = binomial_layout(P, di.sms, B))) return rc;
+  if ((rc = check_ws(ws, ws_bytes, B.total))) return rc;
   if (P.g.n > (int64_t)INT32_MAX * 256) return MM_ERR_TOO_LARGE;
+  int64_t wmax = B.W1 - 1;
+  B.last = std::max<int64_t>(0, std::min<int64_t>(global_cutoff - 1, wmax));
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   UniformSrc src = uniform_src(P, (const double2*)A, (const double2*)b, (const double2*)c, (double2*)G, nullptr, w);
   if ((rc = reset_launch_state(w, st))) return rc;
   if ((rc = launch_setup(src, 1, w, P.L, 1, st))) return rc;
-  if ((rc = launch_fwd_uniform(P, src, w, 0, di, st))) return rc;
-  const int64_t W = binomial_weights(P.g);
-  double* subnorm = reinterpret_cast<double*>(w + align_up(P.L.total));
-  int64_t* stop = reinterpret_cast<int64_t*>(subnorm + W + 1);
-  const unsigned mask_blocks = (unsigned)std::min<int64_t>((P.g.n + 255) / 256, (int64_t)di.sms * 8);
+  if (!(max_l2 < HUGE_VAL)) return launch_binomial_nostop(P, B, src, w, norm_out, di, st);
+  // amplitudes above the stop wave are never written: zero the whole tensor first
+  MM_CUDA(cudaMemsetAsync(G, 0, (size_t)P.g.n * sizeof(double2), st));
   switch (D) {
-#define MM_BN_CASE(DD)                                                                                        \
-  case DD:                                                                                                    \
-    weight_norm_kernel<DD><<<(unsigned)W, MM_BLOCK, 0, st>>>((const double2*)G, P.g, subnorm);               \
-    binomial_stop_kernel<<<1, 32, 0, st>>>(subnorm, (int)W, (const double2*)c, max_l2, global_cutoff, norm_out, \
-                                          stop);                                                              \
-    binomial_mask_kernel<DD><<<mask_blocks, 256, 0, st>>>((double2*)G, P.g, stop);                           \
-    break;
-    MM_BN_CASE(1)
-    MM_BN_CASE(2)
-    MM_BN_CASE(3)
-    MM_BN_CASE(4)
-    MM_BN_CASE(5)
-    MM_BN_CASE(6)
-    MM_BN_CASE(7)
-    MM_BN_CASE(8)
-#undef MM_BN_CASE
-    default:
-      return MM_ERR_UNSUPPORTED;
+    case 1: return launch_binomial_D<1>(P, B, src, w, max_l2, norm_out, di, st);
+    case 2: return launch_binomial_D<2>(P, B, src, w, max_l2, norm_out, di, st);
+    case 3: return launch_binomial_D<3>(P, B, src, w, max_l2, norm_out, di, st);
+    case 4: return launch_binomial_D<4>(P, B, src, w, max_l2, norm_out, di, st);
+    case 5: return launch_binomial_D<5>(P, B, src, w, max_l2, norm_out, di, st);
+    case 6: return launch_binomial_D<6>(P, B, src, w, max_l2, norm_out, di, st);
+    case 7: return launch_binomial_D<7>(P, B, src, w, max_l2, norm_out, di, st);
+    case 8: return launch_binomial_D<8>(P, B, src, w, max_l2, norm_out, di, st);
   }
-  g_launches.fetch_add(3);
-  MM_CUDA(cudaGetLastError());
-  return MM_OK;
+  return MM_ERR_UNSUPPORTED;
 }
 
 int mm_hermite_vjp_batched(int64_t B, int D, const int64_t* shape, const mm_c128* G, const mm_c128* c,

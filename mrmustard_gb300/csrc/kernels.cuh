@@ -1046,73 +1046,315 @@ __global__ void wait_timeout_test_kernel(WsHeader* h, uint64_t budget_ns) { grid
 
 // ============================================================== binomial fill
 // Binomial strategy (reference: strategies/binomial.py:30-70): the tensor is
-// filled by total photon number w = |k| and stops after the first w whose
-// running sum of |G|^2 exceeds max_l2.  Every amplitude of weight <= w obeys
-// the same recurrence as the vanilla one (steps.vanilla_step takes the first
-// non-zero axis as pivot), so the GPU runs the vanilla forward, then
-// weight_norm_kernel sums |G|^2 per weight, binomial_stop_kernel finds the stop
-// weight, and binomial_mask_kernel zeroes every amplitude above it.
+// filled wave by wave, wave w holding every amplitude of total photon number
+// |k| = w, and the fill stops after the first wave whose running sum of |G|^2
+// exceeds max_l2.  Each amplitude obeys the vanilla recurrence with the first
+// non-zero axis as pivot (steps.vanilla_step), computed as fwd_chunk does.
+//
+// Only the waves up to the stop are computed.  Wave w's amplitudes are taken
+// by lexicographic rank r in [0, n_w) (the order of paths.binomial_subspace_basis)
+// and unranked through cumulative composition counts: S_j[x] = number of
+// (k_j, ..., k_{D-1}) inside the cutoffs with sum <= x, rows j = 0..D of W1 =
+// (max weight + 1) entries each (S_D[x] = 1), so n_w = S_0[w] - S_0[w-1].
+struct BinomialState {
+  double norm;      // |c|^2 plus the sums of the waves filled so far
+  int32_t stopped;  // 1 once the running norm exceeded max_l2
+  int32_t pad;
+};
 
-// CTA w: sum of |G[k]|^2 over |k| = w (prefixes over axes 0..D-2 strided over
-// the CTA, the last axis fixed by w), reduced in a fixed order.
-template <int D>
-__global__ void __launch_bounds__(256) weight_norm_kernel(const double2* __restrict__ G, Geom g,
-                                                          double* __restrict__ subnorm) {
-  const int w = (int)blockIdx.x;
-  const int32_t CL = (int32_t)g.shape[D - 1];
-  const uint32_t P = (uint32_t)(g.n / CL);
-  double acc = 0.0;
-  for (uint32_t p = threadIdx.x; p < P; p += blockDim.x) {
-    uint32_t q = p;
-    int32_t sum = 0;
-#pragma unroll
-    for (int j = D - 2; j >= 0; --j) {
-      const uint32_t c = (uint32_t)g.shape[j];
-      sum += (int32_t)(q % c);
-      q /= c;
-    }
-    const int32_t kl = w - sum;
-    if (kl >= 0 && kl < CL) {
-      const double2 v = G[(int64_t)p * CL + kl];
-      const double h = hypot(v.x, v.y);
-      acc += h * h;
-    }
-  }
-  typedef double PartT[MM_BLOCK / 32];
-  MM_SHARED(PartT, part);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+// One CTA: rows S_D .. S_0 of the table (row j from row j+1: the count of
+// weight x is S_{j+1}[x] - S_{j+1}[x - C_j], then an inclusive scan).  Each
+// thread scans a contiguous chunk; warp 0 scans the chunk totals with shuffles.
+__global__ void __launch_bounds__(256) binomial_table_kernel(Geom g, int32_t W1, int64_t* __restrict__ S) {
+  MM_SHARED(int64_t, s_tot[256]);
+  const int D = g.D;
+  const int t = (int)threadIdx.x, nt = (int)blockDim.x;
+  for (int32_t x = t; x < W1; x += nt) S[(int64_t)D * W1 + x] = 1;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = part[0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) t += part[i];
-    subnorm[w] = t;
+  const int32_t chunk = (W1 + nt - 1) / nt;
+  const int32_t lo = min(W1, t * chunk), hi = min(W1, lo + chunk);
+  const int per_lane = (nt + 31) / 32;  // chunk totals per lane of warp 0
+  for (int j = D - 1; j >= 0; --j) {
+    const int64_t C = g.shape[j];
+    const int64_t* nxt = S + (int64_t)(j + 1) * W1;
+    int64_t* row = S + (int64_t)j * W1;
+    int64_t sum = 0;
+    for (int32_t x = lo; x < hi; ++x) {
+      const int64_t cnt = nxt[x] - (x >= C ? nxt[x - C] : 0);
+      row[x] = cnt;
+      sum += cnt;
+    }
+    s_tot[t] = sum;
+    __syncthreads();
+    if (t < 32) {
+      // exclusive prefix of the totals: per-lane serial sums, a shuffle scan across lanes
+      int64_t part = 0;
+      for (int u = t * per_lane; u < min(nt, (t + 1) * per_lane); ++u) part += s_tot[u];
+      int64_t inc = part;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (t >= o) inc += v;
+      }
+      int64_t acc = inc - part;
+      for (int u = t * per_lane; u < min(nt, (t + 1) * per_lane); ++u) {
+        const int64_t v = s_tot[u];
+        s_tot[u] = acc;
+        acc += v;
+      }
+    }
+    __syncthreads();
+    int64_t run = s_tot[t];
+    for (int32_t x = lo; x < hi; ++x) {
+      run += row[x];
+      row[x] = run;
+    }
+    __syncthreads();
   }
 }
 
-// One thread: norm = |c|^2, then weights 1 .. global_cutoff-1 in order until
-// norm > max_l2; writes the norm and the last weight kept.
-__global__ void binomial_stop_kernel(const double* __restrict__ subnorm, int W, const double2* __restrict__ c,
-                                     double max_l2, int64_t global_cutoff, double* norm_out, int64_t* stop_out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const double h = hypot(c->x, c->y);
-  double norm = h * h;
-  int64_t stop = 0;
-  for (int64_t w = 1; w < global_cutoff; ++w) {
-    if (w < W) norm += subnorm[w];
-    stop = w;
-    if (norm > max_l2) break;
-  }
-  *stop_out = stop;
-  if (norm_out) *norm_out = norm;
+__device__ __forceinline__ int64_t bn_S(const int64_t* S, int32_t W1, int j, int32_t x) {
+  return x < 0 ? 0 : S[(int64_t)j * W1 + min(x, W1 - 1)];
 }
 
-// Zero every amplitude whose total photon number exceeds the stop weight.
+struct BinomialSmem {
+  double warp[MM_BLOCK / 32];
+  double sub;
+  double mine[2];  // this CTA's wave sums by wave parity (read by the cluster's CTAs)
+};
+
+// Read-only operands staged in dynamic shared memory when they fit (0: read
+// them from global memory): the count table, the coefficient block, the
+// 1/sqrt table.  The barriers' acquire side may discard L1 lines, so the
+// unranking's dependent table reads would otherwise go to L2 on every wave.
+struct BinomialStage {
+  int32_t table_n;  // int64 entries of the count table, (D + 1) * W1
+  int32_t coef_n;   // double2 entries of the coefficient block, D * sumC
+  int32_t rs_n;     // double entries of the 1/sqrt table, maxC + 1
+};
+
+// Byte offsets of the staged operands (the coefficient block 16-byte aligned).
+__host__ __device__ __forceinline__ size_t bn_stage_coef_offset(const BinomialStage& st) {
+  return ((size_t)st.table_n * sizeof(int64_t) + 15) & ~(size_t)15;
+}
+__host__ __device__ __forceinline__ size_t bn_stage_bytes(const BinomialStage& st) {
+  return bn_stage_coef_offset(st) + (size_t)st.coef_n * sizeof(double2) + (size_t)st.rs_n * sizeof(double);
+}
+
+__device__ __forceinline__ double bn_cluster_peer_load(const double* local, uint32_t peer) {
+#if defined(__CUDA_ARCH__)
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(local), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(peer));
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(r) : "memory");
+  return v;
+#else
+  (void)peer;
+  return *local;
+#endif
+}
+
+// Waves [w_begin, w_end) of one tensor.  MODE 0: one CTA (CTA barriers);
+// MODE 1: one thread-block cluster (cluster barriers, wave sums exchanged
+// through distributed shared memory); MODE 2: a cooperative grid (bounded
+// grid barriers, wave sums through part[(w & 1) * nranks + rank]).  Wave w's
+// ranks are strided over the launch's threads; every CTA sums its |G|^2 in a
+// fixed order, and after the barrier every CTA adds the wave's per-CTA sums
+// in CTA order to its own copy of the norm, so all CTAs take the same stop
+// decision.  With w_begin == 1 the launch writes G[0] = c and starts the norm
+// at |c|^2; otherwise it continues from *state (left by the previous launch).
+template <int D, int MODE>
+__global__ void __launch_bounds__(MM_BLOCK) binomial_wave_kernel(UniformSrc src, const double* __restrict__ rs_g,
+                                                                 const int64_t* __restrict__ S_g, int32_t W1,
+                                                                 BinomialStage stage, int32_t w_begin, int32_t w_end,
+                                                                 double max_l2, double* __restrict__ part,
+                                                                 BinomialState* state, double* __restrict__ norm_out,
+                                                                 WsHeader* h, uint64_t budget_ns) {
+  MM_SHARED(InstView, sv);
+  MM_SHARED(BinomialSmem, sm);
+  extern __shared__ __align__(16) unsigned char bn_dyn[];
+  // a launch that continues a fill which has already stopped only republishes the norm
+  if (w_begin > 1 && state->stopped) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && norm_out) *norm_out = state->norm;
+    return;
+  }
+  if (threadIdx.x == 0) src.load(0, sv);
+  __syncthreads();
+  const Geom& g = sv.g;
+  // staging
+  int64_t* s_tab = reinterpret_cast<int64_t*>(bn_dyn);
+  double2* s_coef = reinterpret_cast<double2*>(bn_dyn + bn_stage_coef_offset(stage));
+  double* s_rs = reinterpret_cast<double*>(s_coef + stage.coef_n);
+  for (int32_t e = threadIdx.x; e < stage.table_n; e += blockDim.x) s_tab[e] = S_g[e];
+  for (int32_t e = threadIdx.x; e < stage.coef_n; e += blockDim.x) s_coef[e] = ldCoef(sv, sv.coef + e, 5);
+  for (int32_t e = threadIdx.x; e < stage.rs_n; e += blockDim.x) s_rs[e] = rs_g[e];
+  __syncthreads();
+  const int64_t* S = stage.table_n ? s_tab : S_g;
+  const double2* coef = stage.coef_n ? s_coef : sv.coef;
+  const double* rs = stage.rs_n ? s_rs : rs_g;
+  uint32_t rank, nranks;
+  if constexpr (MODE == 1) {
+    rank = cluster_rank();
+    nranks = cluster_size();
+  } else {
+    rank = blockIdx.x;
+    nranks = gridDim.x;
+  }
+  uint32_t epoch = 0;
+  auto sync_all = [&]() -> bool {
+    if constexpr (MODE == 0) {
+      __syncthreads();
+      return true;
+    } else if constexpr (MODE == 1) {
+      cluster_sync();
+      return true;
+    } else {
+      return grid_barrier(h, ++epoch, budget_ns, 0);
+    }
+  };
+  double2* G = sv.G;
+  double norm;
+  int32_t stopped;
+  if (w_begin == 1) {
+    const double hc = hypot(sv.c.x, sv.c.y);
+    norm = hc * hc;
+    stopped = 0;
+    if (rank == 0 && threadIdx.x == 0) stG(sv, 0, sv.c, 7);
+    if (!sync_all()) return;
+  } else {
+    norm = state->norm;
+    stopped = 0;
+  }
+  int64_t sj[D];
+  int32_t pj[D], cj[D];
+  double2 bj[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    sj[j] = g.strides[j];
+    pj[j] = g.prefC[j];
+    cj[j] = (int32_t)g.shape[j];
+    bj[j] = __ldg(sv.b + j);
+  }
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const int64_t T = (int64_t)nranks * blockDim.x;
+  const int64_t r0 = (int64_t)rank * blockDim.x + threadIdx.x;
+  // rank r of wave w -> index k (lexicographic order)
+  auto unrank = [&](int64_t rr, int32_t w, int32_t(&k)[D]) {
+    int32_t R = w;
+#pragma unroll
+    for (int j = 0; j < D - 1; ++j) {
+      const int64_t tot = bn_S(S, W1, j + 1, R);
+      int32_t lo = 0, hi = min(cj[j] - 1, R);
+      while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (tot - bn_S(S, W1, j + 1, R - mid) <= rr) lo = mid;
+        else hi = mid - 1;
+      }
+      rr -= tot - bn_S(S, W1, j + 1, R - lo);
+      k[j] = lo;
+      R -= lo;
+    }
+    k[D - 1] = R;
+  };
+  // this thread's first index of the next wave, unranked ahead of the wave's barrier
+  int32_t kn[D];
+  if (w_begin < w_end && r0 < bn_S(S, W1, 0, w_begin) - bn_S(S, W1, 0, w_begin - 1)) unrank(r0, w_begin, kn);
+  for (int32_t w = w_begin; w < w_end && !stopped; ++w) {
+    const int64_t nw = bn_S(S, W1, 0, w) - bn_S(S, W1, 0, w - 1);
+    double local = 0.0;
+    for (int64_t r = r0; r < nw; r += T) {
+      int32_t k[D];
+      if (r == r0) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) k[j] = kn[j];
+      } else {
+        unrank(r, w, k);
+      }
+      int64_t f = 0;
+#pragma unroll
+      for (int j = 0; j < D; ++j) f += (int64_t)k[j] * sj[j];
+      // pivot: the first non-zero axis
+      int piv = 0, kp = 0, pp = 0;
+      int64_t sp = 0;
+      double2 bp = cmk(0.0, 0.0);
+      bool found = false;
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        if (!found && k[j] > 0) {
+          found = true;
+          piv = j;
+          kp = k[j];
+          pp = pj[j];
+          sp = sj[j];
+          bp = bj[j];
+        }
+      }
+      const double2* crow = coef + (int64_t)piv * g.sumC;
+      const int64_t p = f - sp;
+      // one CTA: its own earlier writes, plain (L1) loads; otherwise L2 loads
+      constexpr bool kCG = MODE != 0;
+      double2 acc = cmul(bp, ldGc<kCG>(sv, G + p, 4));
+      if (kp >= 2) acc = cfma(crow[pp + kp], ldGc<kCG>(sv, G + p - sp, 4), acc);
+#pragma unroll
+      for (int j = 1; j < D; ++j) {
+        if (j > piv && k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldGc<kCG>(sv, G + p - sj[j], 4), acc);
+      }
+      const double2 val = cscale(rs[kp], acc);
+      stG(sv, f, val, 6);
+      local += fma(val.x, val.x, val.y * val.y);
+    }
+    if (w + 1 < w_end && r0 < bn_S(S, W1, 0, w + 1) - bn_S(S, W1, 0, w)) unrank(r0, w + 1, kn);
+    // fixed-order CTA sum; warps without ranks in this wave hold exactly 0
+    const bool warp_busy = (r0 - lane) < nw;
+    if (warp_busy) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    }
+    if (lane == 0) sm.warp[warp] = local;
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t nwarps = blockDim.x >> 5;  // a power of two
+      double x = lane < nwarps ? sm.warp[lane] : 0.0;
+      for (uint32_t o = nwarps >> 1; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0) {
+        if constexpr (MODE == 0) sm.sub = x;
+        else if constexpr (MODE == 1) sm.mine[w & 1] = x;
+        else part[(w & 1) * nranks + rank] = x;
+      }
+    }
+    if (!sync_all()) return;
+    if constexpr (MODE != 0) {
+      if (warp == 0) {
+        double x = 0.0;
+        for (uint32_t q = lane; q < nranks; q += 32) {
+          if constexpr (MODE == 1) x += bn_cluster_peer_load(&sm.mine[w & 1], q);
+          else x += __ldcg(part + (w & 1) * nranks + q);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) sm.sub = x;
+      }
+      __syncthreads();
+    }
+    norm += sm.sub;
+    if (norm > max_l2) stopped = 1;
+  }
+  if constexpr (MODE == 1) cluster_sync();  // no CTA leaves while a peer may still read its wave sums
+  if (rank == 0 && threadIdx.x == 0) {
+    state->norm = norm;
+    state->stopped = stopped;
+    if (norm_out) *norm_out = norm;
+  }
+}
+
+// No early stop (max_l2 = +inf): the fill is the vanilla forward's, kept up to
+// wave `last`.  Zeroes every amplitude of weight > last and writes each CTA's
+// fixed-order sum of |G|^2 over the kept ones to part[blockIdx.x].
 template <int D>
-__global__ void __launch_bounds__(256) binomial_mask_kernel(double2* __restrict__ G, Geom g,
-                                                            const int64_t* __restrict__ stop) {
-  const int64_t s = *stop;
+__global__ void __launch_bounds__(256) binomial_mask_norm_kernel(double2* __restrict__ G, Geom g, int64_t last,
+                                                                 double* __restrict__ part) {
+  MM_SHARED(double, s_warp[8]);
+  double acc = 0.0;
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < g.n; f += (int64_t)gridDim.x * blockDim.x) {
     int64_t q = f, w = 0;
 #pragma unroll
@@ -1121,8 +1363,32 @@ __global__ void __launch_bounds__(256) binomial_mask_kernel(double2* __restrict_
       w += q % c;
       q /= c;
     }
-    if (w > s) G[f] = cmk(0.0, 0.0);
+    if (w > last) {
+      G[f] = cmk(0.0, 0.0);
+    } else {
+      const double2 v = G[f];
+      acc += fma(v.x, v.x, v.y * v.y);
+    }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = threadIdx.x < (blockDim.x >> 5) ? s_warp[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = x;
+  }
+}
+
+// One warp: the CTAs' sums in CTA order (lane-strided, then a fixed tree).
+__global__ void binomial_norm_final_kernel(const double* __restrict__ part, int n, double* __restrict__ norm_out) {
+  double x = 0.0;
+  for (int q = (int)threadIdx.x; q < n; q += 32) x += part[q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if (threadIdx.x == 0 && norm_out) *norm_out = x;
 }
 
 // ============================================================== VJP

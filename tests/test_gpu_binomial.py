@@ -64,6 +64,37 @@ def test_no_early_stop_is_vanilla_up_to_global_cutoff(cuda, oracle_lib):
     assert rel(G, V) < 1e-13
 
 
+@pytest.mark.parametrize("shape,gc", [((8, 9, 7), 12), ((6, 5, 7, 4), 19), ((30,), 40), ((12, 13), 5)])
+def test_no_early_stop_norm(cuda, oracle_lib, shape, gc):
+    """max_l2 = None: the fill is the vanilla one up to global_cutoff - 1 (the mask and the norm of
+    the kept amplitudes come from the no-stop kernels)."""
+    A, b, c = ket(len(shape), 900 + sum(shape), smax=0.5, sigma=0.4)
+    G, norm = mm.binomial(shape, A, b, c, None, gc)
+    ref, rnorm, _ = oracle_lib.binomial(shape, A, b, c, float("inf"), gc)
+    assert np.array_equal(G == 0, ref == 0)
+    assert rel(G, ref) < 1e-13
+    assert abs(norm - rnorm) < 1e-14 * rnorm
+
+
+def test_wave_launch_split_is_invisible(cuda, oracle_lib, monkeypatch):
+    """The waves' split over one CTA, one cluster and the cooperative grid (picked from the wave
+    sizes) changes only the order of the norm's additions: every split gives the oracle's tensor."""
+    A, b, c = ket(3, 4242, smax=0.6, sigma=0.5)
+    shape = (20, 20, 30)
+    ref, rnorm, _ = oracle_lib.binomial(shape, A, b, c, 0.99999, sum(shape) - 2)
+    for env in ({}, {"MM_BINOMIAL_TEAM": "0"}, {"MM_BINOMIAL_GRID": "0"}, {"MM_BINOMIAL_CTA_ITEMS": "16"},
+                {"MM_BINOMIAL_TEAM_ITEMS": "300"}, {"MM_BINOMIAL_STAGE": "0"}, {"MM_BINOMIAL_BLOCK": "64"}):
+        for k in ("MM_BINOMIAL_TEAM", "MM_BINOMIAL_GRID", "MM_BINOMIAL_CTA_ITEMS", "MM_BINOMIAL_TEAM_ITEMS",
+                  "MM_BINOMIAL_STAGE", "MM_BINOMIAL_BLOCK"):
+            monkeypatch.delenv(k, raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        G, norm = mm.binomial(shape, A, b, c, 0.99999, sum(shape) - 2)
+        assert np.array_equal(G == 0, ref == 0), env
+        assert rel(G, ref) < 1e-13, env
+        assert abs(norm - rnorm) < 1e-14 * rnorm, env
+
+
 def test_backend_defaults_and_device_mode(cuda, oracle_lib):
     A, b, c = ket(2, 78)
     shape = (15, 12)
