@@ -95,6 +95,27 @@ def test_wave_launch_split_is_invisible(cuda, oracle_lib, monkeypatch):
         assert abs(norm - rnorm) < 1e-14 * rnorm, env
 
 
+@pytest.mark.parametrize("mode_env", [{}, {"MM_BINOMIAL_TEAM": "0", "MM_BINOMIAL_GRID": "0"},
+                                      {"MM_BINOMIAL_CTA_ITEMS": "8", "MM_BINOMIAL_TEAM_ITEMS": "40"}])
+def test_stop_test_at_the_threshold(cuda, oracle_lib, monkeypatch, mode_env):
+    """max_l2 within 1e-12 of the running norm after a weight: the per-weight FP32 estimate cannot
+    settle the test there, so the exact norm decides; the fill must stop after that weight when
+    max_l2 is just below the norm, after the next one when it is just above."""
+    for k, v in mode_env.items():
+        monkeypatch.setenv(k, v)
+    A, b, c = ket(3, 515, smax=0.5, sigma=0.5)
+    shape = (10, 11, 12)
+    gc = sum(shape) - 2
+    full, _, _ = oracle_lib.binomial(shape, A, b, c, float("inf"), gc)
+    w = np.indices(shape).sum(axis=0)
+    cum = np.cumsum([np.sum(np.abs(full[w == k]) ** 2) for k in range(gc)])
+    for w0 in (3, 7, 12):
+        for scale, stop in ((1 - 1e-12, w0), (1 + 1e-12, w0 + 1)):
+            G, norm = mm.binomial(shape, A, b, c, float(cum[w0] * scale), gc)
+            assert int(w[G != 0].max()) == stop, (w0, scale)
+            assert abs(norm - cum[stop]) < 1e-13 * cum[stop]
+
+
 def test_backend_defaults_and_device_mode(cuda, oracle_lib):
     A, b, c = ket(2, 78)
     shape = (15, 12)
