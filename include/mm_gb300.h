@@ -413,6 +413,15 @@ MM_API int mm_test_wait_timeout(void *ws, size_t ws_bytes, uint64_t budget_ns, m
  */
 MM_API int mm_probe_dfma(double *out, int blocks, int iters, mm_stream_t stream);
 
+/*
+ * Self-check of the division used by autoshape's recurrence (a / sqrt(k) as three
+ * FP64 operations from a correctly rounded reciprocal, Markstein's theorem): n
+ * pseudo-random quotients (seeded) are compared bit for bit with the correctly
+ * rounded division; *bad (device, caller-zeroed) receives the number that differ.
+ * Test infrastructure for the kernels' arithmetic; not a compute entry point.
+ */
+MM_API int mm_probe_division(int64_t n, uint64_t seed, unsigned long long *bad, mm_stream_t stream);
+
 /* Number of kernel launches issued by this library since load (all threads). */
 MM_API int64_t mm_launch_count(void);
 

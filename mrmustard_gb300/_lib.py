@@ -60,6 +60,7 @@ SIGNATURES = {
     "mm_hermite_vjp_host": (I32, [I32, P, P, P, P, P, P, P, P]),
     "mm_test_wait_timeout": (I32, [P, SZ, U64, P]),
     "mm_probe_dfma": (I32, [P, I32, I32, P]),
+    "mm_probe_division": (I32, [I64, U64, P, P]),
     "mm_selftest": (I32, [P, SZ, P, ctypes.POINTER(I32)]),
     "mm_fock_gemm_workspace_bytes": (SZ, [I32, I64, I64, I64, I32]),
     "mm_fock_gemm": (I32, [I32, I64, I64, I64, P, P, P, I32, P, SZ, P]),

@@ -17,8 +17,11 @@
 // pairs.  Every product and sum is an explicitly rounded FP64 operation (no
 // fused multiply-add), in the reference's order, so the results follow the
 // reference's arithmetic term by term; the LU pivots on |re| + |im| as LAPACK
-// does.  A reduction whose matrix is singular (the reference raises
-// LinAlgError) yields shape -1 for every mode of that state.
+// does.  The recurrence's divisions by sqrt(k) give the correctly rounded
+// quotient from a correctly rounded reciprocal (div_by_recip, Markstein's
+// theorem; checked bit for bit against the division by mm_probe_division).
+// A reduction whose matrix is singular (the reference raises LinAlgError)
+// yields shape -1 for every mode of that state.
 #include <cstdint>
 
 #include "common.cuh"
@@ -41,9 +44,11 @@ __device__ __forceinline__ cx csub(cx a, cx b) { return mk(__dsub_rn(a.r, b.r), 
 __device__ __forceinline__ cx cmulr(cx a, double s) {
   return mk(__dsub_rn(__dmul_rn(a.r, s), __dmul_rn(a.i, 0.0)), __dadd_rn(__dmul_rn(a.r, 0.0), __dmul_rn(a.i, s)));
 }
-// complex / real: each part divided (numba's lowering of the reference's "/ SQRT[k]")
-__device__ __forceinline__ cx cdivr(cx a, double d) {
-  return mk(__ddiv_rn(__dadd_rn(a.r, __dmul_rn(a.i, 0.0)), d), __ddiv_rn(__dsub_rn(a.i, __dmul_rn(a.r, 0.0)), d));
+// complex / real: each part divided (numba's lowering of the reference's "/ SQRT[k]"); y = RN(1/d)
+// makes each correctly rounded quotient three FP64 operations (div_by_recip)
+__device__ __forceinline__ cx cdivr(cx a, double d, double y) {
+  return mk(mm::div_by_recip(__dadd_rn(a.r, __dmul_rn(a.i, 0.0)), d, y),
+            mm::div_by_recip(__dsub_rn(a.i, __dmul_rn(a.r, 0.0)), d, y));
 }
 // complex / complex: Smith's algorithm (numpy's complex division loop)
 __device__ __forceinline__ cx cdiv(cx a, cx b) {
@@ -200,26 +205,29 @@ __global__ void __launch_bounds__(128) autoshape_kernel(int64_t B, const double2
   double norm = hypot(c1.r, c1.i);
   int64_t k = 0;
   double s0 = 0.0, s1 = 1.0, s2 = sqrt(2.0);  // sqrt(k), sqrt(k + 1), sqrt(k + 2), carried over steps
+  double y1 = 1.0, y2 = __drcp_rn(s2);          // RN(1 / s1), RN(1 / s2)
   while (norm < max_prob && k < max_shape) {
     const int o = (int)(k & 1), n1 = o ^ 1;
     for (int i = 0; i < 2; ++i) {
       const cx Av = cadd(cmul(A1[i * 2 + 0], buf2[o][0]), cmul(A1[i * 2 + 1], buf2[o][1]));
-      buf2[n1][i] = cdivr(cadd(cmul(b1[i], buf3[o][1]), cmulr(Av, s0)), s1);
+      buf2[n1][i] = cdivr(cadd(cmul(b1[i], buf3[o][1]), cmulr(Av, s0)), s1, y1);
     }
     buf3[n1][0] = cdivr(
         cadd(cadd(cmul(b1[0], buf2[n1][0]), cmulr(cmul(A1[0], buf3[o][1]), s1)), cmulr(cmul(A1[1], buf3[o][0]), s0)),
-        s2);
+        s2, y2);
     buf3[n1][1] = cdivr(
         cadd(cadd(cmul(b1[1], buf2[n1][0]), cmulr(cmul(A1[2], buf3[o][1]), s1)), cmulr(cmul(A1[3], buf3[o][0]), s0)),
-        s1);
+        s1, y1);
     buf3[n1][2] = cdivr(
         cadd(cadd(cmul(b1[1], buf2[n1][1]), cmulr(cmul(A1[2], buf3[o][2]), s0)), cmulr(cmul(A1[3], buf3[o][1]), s1)),
-        s2);
+        s2, y2);
     norm = __dadd_rn(norm, hypot(buf3[n1][1].r, buf3[n1][1].i));
     ++k;
     s0 = s1;
     s1 = s2;
+    y1 = y2;
     s2 = sqrt((double)(k + 2));
+    y2 = __drcp_rn(s2);
   }
   if (k < min_shape) k = min_shape;
   if (k > max_shape) k = max_shape;

@@ -63,6 +63,21 @@ __device__ __forceinline__ double2 cdiv_smith(double2 a, double2 b) {
   return cmk((a.x * rat + a.y) * scl, (a.y * rat - a.x) * scl);
 }
 
+// a / b correctly rounded, for b > 0 with y = RN(1/b), by Markstein's theorem
+// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): q0 = RN(a y) is within one ulp of
+// a/b, so the remainder r = a - q0 b is exact in one FMA, and RN(q0 + r y) is
+// RN(a/b).  Three FP64 operations instead of a division sequence.  The theorem
+// assumes no underflow or overflow on the way: when q0 is zero, below 2^-959,
+// above 2^977 or not finite, the quotient comes from the division itself.
+__device__ __forceinline__ double div_by_recip(double a, double b, double y) {
+  const double q0 = __dmul_rn(a, y);
+  const uint32_t e = (uint32_t)(__double_as_longlong(q0) >> 52) & 0x7ffu;
+  if (e < 64u || e > 2000u) return __ddiv_rn(a, b);
+  const double r = __fma_rn(-q0, b, a);
+  return __fma_rn(r, y, q0);
+}
+
 // L2-only load (bypasses L1) for data written by other CTAs of the same launch.
 __device__ __forceinline__ double2 ld_cg(const double2* p) { return __ldcg(p); }
 

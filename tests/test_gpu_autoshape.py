@@ -97,3 +97,18 @@ def test_too_many_modes_and_launch_count(cuda):
     x = torch.zeros((1, 18, 18), dtype=torch.complex128, device=cuda)
     rc = lib.mm_autoshape_batched(1, 9, x.data_ptr(), x.data_ptr(), x.data_ptr(), 0.9, 10, 1, x.data_ptr(), 0)
     assert rc == 2  # MM_ERR_UNSUPPORTED
+
+
+def test_division_by_reciprocal_is_correctly_rounded(cuda):
+    """The recurrence divides by sqrt(k) with three FP64 operations from the correctly rounded
+    reciprocal (Markstein's theorem); 2^28 seeded quotients match the correctly rounded division
+    bit for bit (exponents 2^-1000..2^1000, both signs, zeros; divisors sqrt(1..100000))."""
+    from mrmustard_gb300 import _lib
+
+    lib = _lib.load()
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    for seed in (1, 2):
+        _lib.check(lib.mm_probe_division(1 << 27, seed, bad.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                   "mm_probe_division")
+    torch.cuda.synchronize()
+    assert int(bad.item()) == 0
