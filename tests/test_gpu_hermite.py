@@ -603,3 +603,15 @@ def test_host_buffer_entry_points_match_device(cuda, shape):
                                      device=cuda), torch.as_tensor(g, device=cuda), batched=False)
     assert np.array_equal(dA, dA_d.cpu().numpy()) and np.array_equal(db, db_d.cpu().numpy())
     assert dc == complex(dc_d.item())
+
+
+def test_empty_batches(cuda):
+    """A batch of zero triples (the reference's loop over an empty batch axis, batch.py:52-61 and
+    gradients.py:85-116) gives empty outputs of the reference's shapes."""
+    A = np.zeros((0, 2, 2), np.complex128)
+    b = np.zeros((0, 2), np.complex128)
+    c = np.zeros((0,), np.complex128)
+    G = mm.vanilla_batch_numba((3, 4), A, b, c)
+    assert G.shape == (0, 3, 4) and G.dtype == np.complex128
+    dA, db, dc = mm.vanilla_batch_vjp_numba(G, c, np.zeros((0, 3, 4), np.complex128))
+    assert dA.shape == (0, 2, 2) and db.shape == (0, 2) and dc.shape == (0,)
