@@ -308,7 +308,7 @@ def run_gb300(args, rank, local_rank, world):
         dom, t_dom, bytes_dom, ops_dom = "fwd_cta_kernel", t_fwd, 16.0 * total, fwd_ops
     achieved_gbs = bytes_dom / (t_dom * 1e-3) / 1e9
     # DRAM bytes per launch from one ncu capture of the VJP on a 1024-triple batch
-    # (profiles/ncu_vjp_items_d4_ragged1024.md: 50.3 B per amplitude), scaled by amplitudes
+    # (50.3 B per amplitude: dram__bytes_read.sum + dram__bytes_write.sum), scaled by amplitudes
     traffic = VJP_DRAM_BYTES_PER_AMP * total if dom == "vjp_items_kernel" else None
 
     extras = {}

@@ -5,10 +5,10 @@ MrMustard dispatches ``math.hermite_renormalized`` by name to the active backend
 backend calls ``hermite_renormalized`` / ``hermite_renormalized_batched``
 (mrmustard/math/backend_numpy.py:381-403), ``math.hermite_renormalized_binomial`` to
 ``hermite_renormalized_binomial`` (backend_numpy.py:405-421), and
-``math.hermite_renormalized_diagonal`` / ``math.hermite_renormalized_1leftoverMode`` to the methods
-of those names (backend_numpy.py:423-446).  ``BackendGB300`` provides those
-methods with the same signatures; a maintainer mixes it into the numpy backend (see
-INTEGRATION.md) so every other op keeps its numpy implementation.
+``math.hermite_renormalized_diagonal`` / ``math.hermite_renormalized_1leftoverMode`` to the
+methods of those names (backend_numpy.py:423-446), which use ``reorder_AB_bargmann``
+(:367-375).  ``BackendGB300`` provides those methods with the same signatures; a maintainer
+mixes it into the numpy backend so every other op keeps its numpy implementation.
 """
 
 from __future__ import annotations
@@ -16,6 +16,7 @@ from __future__ import annotations
 from .binomial import hermite_renormalized_binomial as _binomial
 from .diagonal import hermite_renormalized_1leftoverMode as _leftover
 from .diagonal import hermite_renormalized_diagonal as _diagonal
+from .diagonal import reorder_AB_bargmann as _reorder
 from .hermite import stable_numba, vanilla_batch_numba, vanilla_numba
 
 
@@ -39,3 +40,8 @@ class BackendGB300:
     def hermite_renormalized_1leftoverMode(self, A, b, c, output_cutoff, pnr_cutoffs, stable=False,
                                            reorderedAB=True):
         return _leftover(A, b, c, output_cutoff, tuple(pnr_cutoffs), stable, reorderedAB)
+
+    def reorder_AB_bargmann(self, A, B):
+        """(m0..m_{M-1}, m0'..) -> (m0, m0', m1, m1', ...) on A's rows and columns and B
+        (backend_numpy.py:367-375)."""
+        return _reorder(A, B)
