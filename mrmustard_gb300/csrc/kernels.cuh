@@ -258,9 +258,95 @@ __device__ __forceinline__ void fwd_chunk(const InstView& v, const double* __res
   }
 }
 
-// Whole instance on one CTA (chunks separated by __syncthreads).
+// Chunk (i, m) with the pivot row of the coefficient block and b_i already
+// multiplied by 1/sqrt(m) (`row`, built by build_scaled_row): the amplitude is
+// the sum of the terms itself, without the final scaling of fwd_chunk (two FP64
+// instructions fewer per amplitude; each term is rounded once more instead of
+// the sum).  Rows of at most kScaledRow entries (sumC) fit the shared buffers.
+constexpr int kScaledRow = 320;
+struct ScaledRow {
+  double2 c[kScaledRow];
+  double2 b;
+};
+
+// The two row buffers of a CTA (one static shared array for every caller).
+__device__ __forceinline__ ScaledRow* scaled_rows() {
+  __shared__ ScaledRow rows[2];
+  return rows;
+}
+
+__device__ __forceinline__ void build_scaled_row(const InstView& v, const double* __restrict__ rs, int i, int m,
+                                                 ScaledRow& row) {
+  const double r = MM_CHK(rs + m, rs, v.g.maxC + 1, double, 3) ? rs[m] : 0.0;
+  const double2* __restrict__ crow = v.coef + (int64_t)i * v.g.sumC;
+  for (int e = (int)threadIdx.x; e < (int)v.g.sumC; e += (int)blockDim.x) row.c[e] = cscale(r, ldCoef(v, crow + e, 5));
+  if (threadIdx.x == blockDim.x - 1)
+    row.b = cscale(r, MM_CHK(v.b + i, v.b, v.g.D, double2, 1) ? __ldg(v.b + i) : cmk(0.0, 0.0));
+}
+
+template <int D, bool CG>
+__device__ __forceinline__ void fwd_chunk_scaled(const InstView& v, const ScaledRow& row, int i, int m,
+                                                 uint32_t q_begin, uint32_t q_end, uint32_t q_step, uint32_t t) {
+  const Geom& g = v.g;
+  const int64_t si = g.strides[i];
+  const double2 bi = row.b;
+  const double2 cd = (m >= 2) ? row.c[g.prefC[i] + m] : cmk(0.0, 0.0);
+  const double2* G = v.G;
+  const int64_t base = (int64_t)m * si;
+  int64_t sj[D];
+  int32_t pj[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    sj[j] = g.strides[j];
+    pj[j] = g.prefC[j];
+  }
+  for (uint32_t q = q_begin + t; q < q_end; q += q_step) {
+    int32_t k[D];
+    decompose<D>(q, i + 1, g, k);
+    const int64_t f = base + q;
+    const int64_t p = f - si;
+    double2 acc = cmul(bi, ldGc<CG>(v, G + p, 4));
+    if (m >= 2) acc = cfma(cd, ldGc<CG>(v, G + p - si, 4), acc);
+#pragma unroll
+    for (int j = 1; j < D; ++j) {
+      if (j > i && k[j] > 0) acc = cfma(row.c[pj[j] + k[j]], ldGc<CG>(v, G + p - sj[j], 4), acc);
+    }
+    stG(v, f, acc, 6);
+  }
+}
+
+// The chunk after (i, m) in the forward's order (levels D-1 .. 0, m = 1 .. C_i - 1); i < 0 at the end.
+__device__ __forceinline__ void next_chunk(const Geom& g, int& i, int& m) {
+  ++m;
+  while (i >= 0 && m >= (int)g.shape[i]) {
+    --i;
+    m = 1;
+  }
+}
+
+// Whole instance on one CTA (chunks separated by __syncthreads).  With a short
+// enough pivot row, the next chunk's scaled row is built while the CTA
+// finishes the current chunk (double buffer), so it costs no extra barrier.
 template <int D>
 __device__ void fwd_instance_cta(const InstView& v, const double* rs) {
+  if (v.g.sumC <= kScaledRow) {
+    ScaledRow* rows = scaled_rows();
+    if (threadIdx.x == 0) stG(v, 0, v.c, 7);
+    int i = D - 1, m = 0;
+    next_chunk(v.g, i, m);
+    if (i >= 0) build_scaled_row(v, rs, i, m, rows[0]);
+    __syncthreads();
+    for (int buf = 0; i >= 0; buf ^= 1) {
+      int ni = i, nm = m;
+      next_chunk(v.g, ni, nm);
+      fwd_chunk_scaled<D, false>(v, rows[buf], i, m, 0u, (uint32_t)v.g.strides[i], blockDim.x, threadIdx.x);
+      if (ni >= 0) build_scaled_row(v, rs, ni, nm, rows[buf ^ 1]);
+      __syncthreads();
+      i = ni;
+      m = nm;
+    }
+    return;
+  }
   if (threadIdx.x == 0) stG(v, 0, v.c, 7);
   __syncthreads();
   for (int i = D - 1; i >= 0; --i) {
@@ -410,6 +496,28 @@ void cluster_sync();
 // identical in every CTA of the cluster, so every barrier is reached by all.
 template <int D>
 __device__ void fwd_instance_team(const InstView& v, const double* rs, uint32_t rank, uint32_t nranks) {
+  if (v.g.sumC <= kScaledRow) {
+    // as fwd_instance_cta: every CTA builds its own copy of the next chunk's scaled row
+    ScaledRow* rows = scaled_rows();
+    if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
+    int i = D - 1, m = 0;
+    next_chunk(v.g, i, m);
+    if (i >= 0) build_scaled_row(v, rs, i, m, rows[0]);
+    cluster_sync();
+    for (int buf = 0; i >= 0; buf ^= 1) {
+      int ni = i, nm = m;
+      next_chunk(v.g, ni, nm);
+      const uint32_t si = (uint32_t)v.g.strides[i];
+      const uint32_t per = (si + nranks - 1) / nranks;
+      const uint32_t lo = min(si, per * rank), hi = min(si, lo + per);
+      fwd_chunk_scaled<D, true>(v, rows[buf], i, m, lo, hi, blockDim.x, threadIdx.x);
+      if (ni >= 0) build_scaled_row(v, rs, ni, nm, rows[buf ^ 1]);
+      cluster_sync();
+      i = ni;
+      m = nm;
+    }
+    return;
+  }
   if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
   cluster_sync();
   for (int i = D - 1; i >= 0; --i) {
