@@ -519,8 +519,9 @@ def run_autoshape(dev, time_eager, As, bs, with_cpu=True):
 def run_binomial(dev, time_eager, with_cpu=True):
     """Binomial fill of one 4-mode pure state at local cutoff 30 (810 k amplitudes) with the
     reference's default max_l2 (0.99999) and global cutoff (sum(shape) - D + 1): GPU time of
-    mm_binomial (forward, per-weight norms, stop search, mask) against the C oracle on one core
-    (the reference's strategy is sequential over weights)."""
+    mm_binomial against the C oracle on one core (the reference's strategy is sequential over
+    weights).  `ms` is the device time of the fill (mm_binomial on preallocated buffers, back to
+    back); `api_ms` the same through mm.device_binomial (allocation, workspace, Python)."""
     import torch
     from scipy.stats import unitary_group
 
@@ -539,14 +540,33 @@ def run_binomial(dev, time_eager, with_cpu=True):
     cd = torch.tensor(complex(c0), dtype=torch.complex128, device=dev)
     shape = (cut,) * D
     gc = sum(shape) - D + 1
+    from mrmustard_gb300 import _lib
+    from mrmustard_gb300.hermite import Workspace, _shape_arr
+
+    lib = _lib.load()
+    _, sh = _shape_arr(shape)
+    Gd = torch.empty(shape, dtype=torch.complex128, device=dev)
+    nd = torch.empty((), dtype=torch.float64, device=dev)
+    ws = Workspace(lib.mm_binomial_workspace_bytes(D, sh), dev)
+    cd1 = cd.reshape(1)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def fill():
+        _lib.check(lib.mm_binomial(D, sh, Ad.data_ptr(), bd.data_ptr(), cd1.data_ptr(), 0.99999, gc, Gd.data_ptr(),
+                                   nd.data_ptr(), ws.ptr, ws.nbytes, stream), "mm_binomial")
+
+    t = time_eager(fill, reps=20)
+    ws.check_status("binomial")
     with mm.settings(CHECK_DEVICE_STATUS=False):
-        t = time_eager(lambda: mm.device_binomial(Ad, bd, cd, shape, 0.99999, gc), reps=10)
+        t_api = time_eager(lambda: mm.device_binomial(Ad, bd, cd, shape, 0.99999, gc), reps=10)
     G, norm = mm.device_binomial(Ad, bd, cd, shape, 0.99999, gc)
     Gh = G.cpu().numpy()
+    if not np.array_equal(Gh, Gd.cpu().numpy()):
+        raise RuntimeError("binomial: the buffered and the API fill differ")
     w = np.indices(shape).sum(axis=0)
     kept = int(w[Gh != 0].max()) if np.any(Gh != 0) else 0
     out = {"shape": list(shape), "amplitudes": cut ** D, "ms": t, "amplitudes_per_s": cut ** D / (t * 1e-3),
-           "norm": float(norm), "stop_weight": kept}
+           "api_ms": t_api, "norm": float(norm), "stop_weight": kept}
     if with_cpu:
         import oracle
 

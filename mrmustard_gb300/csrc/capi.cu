@@ -591,14 +591,19 @@ namespace {
 constexpr int64_t kBnMaxW1 = 1 << 24;
 constexpr int kBnMaxTeam = 16;
 constexpr int kBnMaxPerSm = 2;
+// Staged operands per CTA: every CTA copies them at launch, so a large prefix
+// permutation (108 KB at 30^4) costs more to stage than its L2 reads (measured).
 constexpr size_t kBnStageBytes = 48 * 1024;
+constexpr int64_t kBnMaxPerm = 1 << 24;  // prefixes beyond this: no permutation (binary-search unranking)
 
 struct BinomialPlan {
   int64_t W1 = 0;      // max weight + 1
+  int64_t W1p = 0;     // max weight of the prefix axes 0 .. D-2, + 1
+  int64_t P = 0;       // prefixes (flat index over the axes 0 .. D-2); 0: no prefix permutation
   int64_t last = 0;    // last wave the reference would fill: global cutoff - 1, capped at the max weight
   int64_t w_team = 0;  // first wave of the cluster launch
   int64_t w_grid = 0;  // first wave of the grid launch
-  size_t off_state = 0, off_table = 0, off_part = 0, total = 0;
+  size_t off_state = 0, off_table = 0, off_sp = 0, off_perm = 0, off_part = 0, total = 0;
 };
 
 int binomial_env(const char* name, int dflt) {
@@ -612,10 +617,15 @@ int binomial_layout(const UniformPlan& P, int sms, BinomialPlan& B) {
   for (int i = 0; i < P.g.D; ++i) wmax += P.g.shape[i] - 1;
   B.W1 = wmax + 1;
   if (B.W1 > kBnMaxW1) return MM_ERR_TOO_LARGE;
+  B.W1p = B.W1 - (P.g.shape[P.g.D - 1] - 1);
+  B.P = P.g.n / P.g.shape[P.g.D - 1];
+  if (B.P > kBnMaxPerm) B.P = 0;  // the waves then unrank their indices by binary search
   const int parts = std::max(kBnMaxTeam, kBnMaxPerSm * sms);
   B.off_state = align_up(P.L.total);
   B.off_table = B.off_state + align_up(sizeof(BinomialState));
-  B.off_part = B.off_table + align_up((size_t)(P.g.D + 1) * (size_t)B.W1 * sizeof(int64_t));
+  B.off_sp = B.off_table + align_up((size_t)(P.g.D + 1) * (size_t)B.W1 * sizeof(int64_t));
+  B.off_perm = B.off_sp + (B.P ? align_up((size_t)P.g.D * (size_t)B.W1p * sizeof(int64_t)) : 0);
+  B.off_part = B.off_perm + (B.P ? align_up((size_t)B.P * sizeof(uint32_t)) : 0);
   B.total = B.off_part + align_up((size_t)2 * parts * sizeof(double));
   return MM_OK;
 }
@@ -663,6 +673,7 @@ int binomial_team_ctas() {
     for (int cl : {16, 8, 4, 2}) {
       cudaLaunchAttribute attr[1];
       cudaLaunchConfig_t cfg = cluster_config(attr, cl, nullptr);
+      cfg.dynamicSmemBytes = kBnStageBytes;  // the most a launch stages
       int ncl = 0;
       if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) == cudaSuccess && ncl >= 1) {
         best = cl;
@@ -716,19 +727,41 @@ int launch_binomial_D(const UniformPlan& P, const BinomialPlan& B, const Uniform
   BinomialState* state = reinterpret_cast<BinomialState*>(w + B.off_state);
   double* part = reinterpret_cast<double*>(w + B.off_part);
   WsHeader* h = reinterpret_cast<WsHeader*>(w);
-  const int32_t W1 = (int32_t)B.W1;
+  const int32_t W1 = (int32_t)B.W1, W1p = (int32_t)B.W1p;
+  int64_t* Sp = B.P ? reinterpret_cast<int64_t*>(w + B.off_sp) : nullptr;
+  uint32_t* perm = B.P ? reinterpret_cast<uint32_t*>(w + B.off_perm) : nullptr;
+  if (!binomial_env("MM_BINOMIAL_PERM", 1)) perm = nullptr;
   uint64_t budget = wait_budget_ns();
-  // stage the read-only operands in shared memory when they fit the default 48 KiB
-  BinomialStage stage;
-  stage.table_n = (int32_t)((P.g.D + 1) * B.W1);
-  stage.coef_n = (int32_t)std::min<int64_t>(coef_entries(P.g), INT32_MAX);
-  stage.rs_n = P.g.maxC + 1;
-  if (bn_stage_bytes(stage) > kBnStageBytes) stage.coef_n = stage.rs_n = 0;
-  if (bn_stage_bytes(stage) > kBnStageBytes) stage.table_n = 0;
-  if (!binomial_env("MM_BINOMIAL_STAGE", 1)) stage.table_n = stage.coef_n = stage.rs_n = 0;
-  const size_t smem = bn_stage_bytes(stage);
-  binomial_table_kernel<<<1, 256, 0, st>>>(P.g, W1, const_cast<int64_t*>(S));
+  // stage the read-only operands in shared memory as far as they fit kBnStageBytes,
+  // the most frequently read first
+  BinomialStage stage = {};
+  const int32_t table_n = (int32_t)((P.g.D + 1) * B.W1);
+  const int32_t sp_n = perm ? (int32_t)(P.g.D * B.W1p) : 0;
+  const int32_t coef_n = (int32_t)std::min<int64_t>(coef_entries(P.g), INT32_MAX);
+  const int32_t rs_n = P.g.maxC + 1;
+  const int32_t perm_n = perm ? (int32_t)B.P : 0;
+  if (binomial_env("MM_BINOMIAL_STAGE", 1)) {
+    auto fits = [&](const BinomialStage& t) { return bn_stage_bytes(t) <= kBnStageBytes; };
+    BinomialStage t = stage;
+    t.table_n = table_n;
+    t.sp_n = sp_n;
+    if (fits(t)) stage = t;
+    t = stage;
+    t.coef_n = coef_n;
+    t.rs_n = rs_n;
+    if (fits(t)) stage = t;
+    t = stage;
+    t.perm_n = perm_n;
+    if (fits(t)) stage = t;
+  }
+  const size_t smem = bn_stage_bytes(stage);  // <= 48 KB: no opt-in attribute needed
+  binomial_table_kernel<<<perm ? 2 : 1, 256, 0, st>>>(P.g, W1, const_cast<int64_t*>(S), W1p, Sp);
   MM_LAUNCHED();
+  if (perm) {
+    const unsigned pb = (unsigned)std::min<int64_t>((B.P + 255) / 256, (int64_t)4 * di.sms);
+    binomial_perm_kernel<<<pb, 256, 0, st>>>(P.g, Sp, W1p, perm, B.P);
+    MM_LAUNCHED();
+  }
 
   // launch split
   int team = binomial_env("MM_BINOMIAL_TEAM", -1);
@@ -756,8 +789,8 @@ int launch_binomial_D(const UniformPlan& P, const BinomialPlan& B, const Uniform
   if (team <= 0 && grid <= 0) w_team = last + 1;  // neither: one CTA fills every wave
   if (team <= 0) w_team = w_grid;
 
-  binomial_wave_kernel<D, 0><<<1, nt, smem, st>>>(src, rs, S, W1, stage, 1, (int32_t)w_team, max_l2, part,
-                                                        state, norm_out, h, budget);
+  binomial_wave_kernel<D, 0><<<1, nt, smem, st>>>(src, rs, S, W1, Sp, W1p, perm, stage, 1, (int32_t)w_team,
+                                                        max_l2, part, state, norm_out, h, budget);
   MM_LAUNCHED();
   if (w_team < w_grid) {
     auto kern = binomial_wave_kernel<D, 1>;
@@ -766,14 +799,19 @@ int launch_binomial_D(const UniformPlan& P, const BinomialPlan& B, const Uniform
     cfg.blockDim = dim3((unsigned)nt);
     cfg.dynamicSmemBytes = smem;
     const int32_t wb = (int32_t)w_team, we = (int32_t)w_grid;
-    MM_CUDA(cudaLaunchKernelEx(&cfg, kern, src, rs, S, W1, stage, wb, we, max_l2, part, state, norm_out, h, budget));
+    const int64_t* Spc = Sp;
+    const uint32_t* permc = perm;
+    MM_CUDA(cudaLaunchKernelEx(&cfg, kern, src, rs, S, W1, Spc, W1p, permc, stage, wb, we, max_l2, part, state,
+                               norm_out, h, budget));
     g_launches.fetch_add(1);
   }
   if (w_grid <= last) {
     UniformSrc s = src;
     int32_t wb = (int32_t)w_grid, we = (int32_t)(last + 1);
-    void* args[] = {&s,  (void*)&rs, (void*)&S, (void*)&W1,     &stage, &wb, &we,
-                    &max_l2, &part,     &state,    &norm_out, &h,     &budget};
+    const int64_t* Spc = Sp;
+    const uint32_t* permc = perm;
+    void* args[] = {&s,      (void*)&rs, (void*)&S, (void*)&W1, (void*)&Spc, (void*)&W1p, (void*)&permc, &stage,
+                    &wb,     &we,        &max_l2,   &part,      &state,      &norm_out,   &h,            &budget};
     MM_CUDA(cudaLaunchCooperativeKernel((void*)binomial_wave_kernel<D, 2>, dim3((unsigned)grid), dim3(MM_BLOCK), args,
                                         smem, st));
     g_launches.fetch_add(1);

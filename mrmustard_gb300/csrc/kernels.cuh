@@ -1170,22 +1170,22 @@ struct BinomialState {
   int32_t pad;
 };
 
-// One CTA: rows S_D .. S_0 of the table (row j from row j+1: the count of
-// weight x is S_{j+1}[x] - S_{j+1}[x - C_j], then an inclusive scan).  Each
-// thread scans a contiguous chunk; warp 0 scans the chunk totals with shuffles.
-__global__ void __launch_bounds__(256) binomial_table_kernel(Geom g, int32_t W1, int64_t* __restrict__ S) {
-  MM_SHARED(int64_t, s_tot[256]);
-  const int D = g.D;
+// Rows T_nax .. T_0 of a count table over the axes 0 .. nax-1 (T_j[x] = number
+// of (k_j, ..., k_{nax-1}) inside the cutoffs with sum <= x; row j from row j+1:
+// the count of weight x is T_{j+1}[x] - T_{j+1}[x - C_j], then an inclusive
+// scan).  One CTA: each thread scans a contiguous chunk of a row, warp 0 scans
+// the chunk totals with shuffles.
+__device__ void binomial_counts(const Geom& g, int nax, int32_t W, int64_t* __restrict__ T, int64_t* s_tot) {
   const int t = (int)threadIdx.x, nt = (int)blockDim.x;
-  for (int32_t x = t; x < W1; x += nt) S[(int64_t)D * W1 + x] = 1;
+  for (int32_t x = t; x < W; x += nt) T[(int64_t)nax * W + x] = 1;
   __syncthreads();
-  const int32_t chunk = (W1 + nt - 1) / nt;
-  const int32_t lo = min(W1, t * chunk), hi = min(W1, lo + chunk);
+  const int32_t chunk = (W + nt - 1) / nt;
+  const int32_t lo = min(W, t * chunk), hi = min(W, lo + chunk);
   const int per_lane = (nt + 31) / 32;  // chunk totals per lane of warp 0
-  for (int j = D - 1; j >= 0; --j) {
+  for (int j = nax - 1; j >= 0; --j) {
     const int64_t C = g.shape[j];
-    const int64_t* nxt = S + (int64_t)(j + 1) * W1;
-    int64_t* row = S + (int64_t)j * W1;
+    const int64_t* nxt = T + (int64_t)(j + 1) * W;
+    int64_t* row = T + (int64_t)j * W;
     int64_t sum = 0;
     for (int32_t x = lo; x < hi; ++x) {
       const int64_t cnt = nxt[x] - (x >= C ? nxt[x - C] : 0);
@@ -1221,6 +1221,46 @@ __global__ void __launch_bounds__(256) binomial_table_kernel(Geom g, int32_t W1,
   }
 }
 
+// CTA 0: the table S over all D axes (W1 = max weight + 1); CTA 1 (when Sp is
+// given): the table Sp over the prefix axes 0 .. D-2 (W1p = their max weight + 1).
+__global__ void __launch_bounds__(256) binomial_table_kernel(Geom g, int32_t W1, int64_t* __restrict__ S, int32_t W1p,
+                                                             int64_t* __restrict__ Sp) {
+  MM_SHARED(int64_t, s_tot[256]);
+  if (blockIdx.x == 0) binomial_counts(g, g.D, W1, S, s_tot);
+  else if (Sp) binomial_counts(g, g.D - 1, W1p, Sp, s_tot);
+}
+
+// The prefixes p (flat index over the axes 0 .. D-2, last of them fastest)
+// sorted by their weight s, lexicographic within a weight: perm[pos] = p with
+// pos = #{prefixes of weight < s} + the prefix's lexicographic rank among those
+// of weight s (sum over its axes of Sp_{j+1}[R_j] - Sp_{j+1}[R_j - k_j]).  The
+// indices of wave w are then the prefixes of weights max(0, w - C_{D-1} + 1) ..
+// min(w, max prefix weight), a contiguous run of perm, completed by
+// k_{D-1} = w - s.
+__global__ void __launch_bounds__(256) binomial_perm_kernel(Geom g, const int64_t* __restrict__ Sp, int32_t W1p,
+                                                            uint32_t* __restrict__ perm, int64_t P) {
+  const int D = g.D;
+  auto T = [&](int j, int32_t x) -> int64_t { return x < 0 ? 0 : Sp[(int64_t)j * W1p + min(x, W1p - 1)]; };
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+    int32_t k[MM_MAXD];
+    int64_t q = p;
+    int32_t s = 0;
+    for (int j = D - 2; j >= 0; --j) {
+      const int64_t C = g.shape[j];
+      k[j] = (int32_t)(q % C);
+      q /= C;
+      s += k[j];
+    }
+    int64_t rank = 0;
+    int32_t R = s;
+    for (int j = 0; j < D - 1; ++j) {
+      rank += T(j + 1, R) - T(j + 1, R - k[j]);
+      R -= k[j];
+    }
+    perm[T(0, s - 1) + rank] = (uint32_t)p;
+  }
+}
+
 __device__ __forceinline__ int64_t bn_S(const int64_t* S, int32_t W1, int j, int32_t x) {
   return x < 0 ? 0 : S[(int64_t)j * W1 + min(x, W1 - 1)];
 }
@@ -1232,21 +1272,27 @@ struct BinomialSmem {
 };
 
 // Read-only operands staged in dynamic shared memory when they fit (0: read
-// them from global memory): the count table, the coefficient block, the
-// 1/sqrt table.  The barriers' acquire side may discard L1 lines, so the
-// unranking's dependent table reads would otherwise go to L2 on every wave.
+// them from global memory): the count tables, the coefficient block, the
+// 1/sqrt table and the prefix permutation.  The barriers' acquire side may
+// discard L1 lines, so their dependent reads would otherwise go to L2 on every
+// wave.
 struct BinomialStage {
-  int32_t table_n;  // int64 entries of the count table, (D + 1) * W1
+  int32_t table_n;  // int64 entries of the count table S, (D + 1) * W1
+  int32_t sp_n;     // int64 entries of the prefix count table Sp, D * W1p
   int32_t coef_n;   // double2 entries of the coefficient block, D * sumC
   int32_t rs_n;     // double entries of the 1/sqrt table, maxC + 1
+  int32_t perm_n;   // uint32 entries of the prefix permutation
 };
 
-// Byte offsets of the staged operands (the coefficient block 16-byte aligned).
+// Byte offsets of the staged operands: S | Sp | coefficients (16-byte aligned) | 1/sqrt | permutation.
 __host__ __device__ __forceinline__ size_t bn_stage_coef_offset(const BinomialStage& st) {
-  return ((size_t)st.table_n * sizeof(int64_t) + 15) & ~(size_t)15;
+  return ((size_t)(st.table_n + st.sp_n) * sizeof(int64_t) + 15) & ~(size_t)15;
+}
+__host__ __device__ __forceinline__ size_t bn_stage_perm_offset(const BinomialStage& st) {
+  return bn_stage_coef_offset(st) + (size_t)st.coef_n * sizeof(double2) + (size_t)st.rs_n * sizeof(double);
 }
 __host__ __device__ __forceinline__ size_t bn_stage_bytes(const BinomialStage& st) {
-  return bn_stage_coef_offset(st) + (size_t)st.coef_n * sizeof(double2) + (size_t)st.rs_n * sizeof(double);
+  return bn_stage_perm_offset(st) + (size_t)st.perm_n * sizeof(uint32_t);
 }
 
 __device__ __forceinline__ double bn_cluster_peer_load(const double* local, uint32_t peer) {
@@ -1274,6 +1320,8 @@ __device__ __forceinline__ double bn_cluster_peer_load(const double* local, uint
 template <int D, int MODE>
 __global__ void __launch_bounds__(MM_BLOCK) binomial_wave_kernel(UniformSrc src, const double* __restrict__ rs_g,
                                                                  const int64_t* __restrict__ S_g, int32_t W1,
+                                                                 const int64_t* __restrict__ Sp_g, int32_t W1p,
+                                                                 const uint32_t* __restrict__ perm_g,
                                                                  BinomialStage stage, int32_t w_begin, int32_t w_end,
                                                                  double max_l2, double* __restrict__ part,
                                                                  BinomialState* state, double* __restrict__ norm_out,
@@ -1291,15 +1339,21 @@ __global__ void __launch_bounds__(MM_BLOCK) binomial_wave_kernel(UniformSrc src,
   const Geom& g = sv.g;
   // staging
   int64_t* s_tab = reinterpret_cast<int64_t*>(bn_dyn);
+  int64_t* s_sp = s_tab + stage.table_n;
   double2* s_coef = reinterpret_cast<double2*>(bn_dyn + bn_stage_coef_offset(stage));
   double* s_rs = reinterpret_cast<double*>(s_coef + stage.coef_n);
+  uint32_t* s_perm = reinterpret_cast<uint32_t*>(bn_dyn + bn_stage_perm_offset(stage));
   for (int32_t e = threadIdx.x; e < stage.table_n; e += blockDim.x) s_tab[e] = S_g[e];
+  for (int32_t e = threadIdx.x; e < stage.sp_n; e += blockDim.x) s_sp[e] = Sp_g[e];
   for (int32_t e = threadIdx.x; e < stage.coef_n; e += blockDim.x) s_coef[e] = ldCoef(sv, sv.coef + e, 5);
   for (int32_t e = threadIdx.x; e < stage.rs_n; e += blockDim.x) s_rs[e] = rs_g[e];
+  for (int32_t e = threadIdx.x; e < stage.perm_n; e += blockDim.x) s_perm[e] = perm_g[e];
   __syncthreads();
   const int64_t* S = stage.table_n ? s_tab : S_g;
+  const int64_t* Sp = stage.sp_n ? s_sp : Sp_g;
   const double2* coef = stage.coef_n ? s_coef : sv.coef;
   const double* rs = stage.rs_n ? s_rs : rs_g;
+  const uint32_t* perm = stage.perm_n ? s_perm : perm_g;  // null: unrank by binary search
   uint32_t rank, nranks;
   if constexpr (MODE == 1) {
     rank = cluster_rank();
@@ -1364,9 +1418,27 @@ __global__ void __launch_bounds__(MM_BLOCK) binomial_wave_kernel(UniformSrc src,
     }
     k[D - 1] = R;
   };
+  // the same index from the prefix permutation: one table read and the prefix's digits
+  auto from_perm = [&](int64_t rr, int32_t w, int32_t(&k)[D]) {
+    const int32_t lo_s = max(0, w - (cj[D - 1] - 1));
+    uint32_t q = perm[bn_S(Sp, W1p, 0, lo_s - 1) + rr];
+    int32_t sum = 0;
+#pragma unroll
+    for (int j = D - 2; j >= 0; --j) {
+      const uint32_t c = (uint32_t)cj[j];
+      k[j] = (int32_t)(q % c);
+      q /= c;
+      sum += k[j];
+    }
+    k[D - 1] = w - sum;
+  };
+  auto index_of = [&](int64_t rr, int32_t w, int32_t(&k)[D]) {
+    if (perm) from_perm(rr, w, k);
+    else unrank(rr, w, k);
+  };
   // this thread's first index of the next wave, unranked ahead of the wave's barrier
   int32_t kn[D];
-  if (w_begin < w_end && r0 < bn_S(S, W1, 0, w_begin) - bn_S(S, W1, 0, w_begin - 1)) unrank(r0, w_begin, kn);
+  if (w_begin < w_end && r0 < bn_S(S, W1, 0, w_begin) - bn_S(S, W1, 0, w_begin - 1)) index_of(r0, w_begin, kn);
   for (int32_t w = w_begin; w < w_end && !stopped; ++w) {
     const int64_t nw = bn_S(S, W1, 0, w) - bn_S(S, W1, 0, w - 1);
     double local = 0.0;
@@ -1376,7 +1448,7 @@ __global__ void __launch_bounds__(MM_BLOCK) binomial_wave_kernel(UniformSrc src,
 #pragma unroll
         for (int j = 0; j < D; ++j) k[j] = kn[j];
       } else {
-        unrank(r, w, k);
+        index_of(r, w, k);
       }
       int64_t f = 0;
 #pragma unroll
@@ -1411,7 +1483,7 @@ __global__ void __launch_bounds__(MM_BLOCK) binomial_wave_kernel(UniformSrc src,
       stG(sv, f, val, 6);
       local += fma(val.x, val.x, val.y * val.y);
     }
-    if (w + 1 < w_end && r0 < bn_S(S, W1, 0, w + 1) - bn_S(S, W1, 0, w)) unrank(r0, w + 1, kn);
+    if (w + 1 < w_end && r0 < bn_S(S, W1, 0, w + 1) - bn_S(S, W1, 0, w)) index_of(r0, w + 1, kn);
     // fixed-order CTA sum; warps without ranks in this wave hold exactly 0
     const bool warp_busy = (r0 - lane) < nw;
     if (warp_busy) {

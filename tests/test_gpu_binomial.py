@@ -83,9 +83,10 @@ def test_wave_launch_split_is_invisible(cuda, oracle_lib, monkeypatch):
     shape = (20, 20, 30)
     ref, rnorm, _ = oracle_lib.binomial(shape, A, b, c, 0.99999, sum(shape) - 2)
     for env in ({}, {"MM_BINOMIAL_TEAM": "0"}, {"MM_BINOMIAL_GRID": "0"}, {"MM_BINOMIAL_CTA_ITEMS": "16"},
-                {"MM_BINOMIAL_TEAM_ITEMS": "300"}, {"MM_BINOMIAL_STAGE": "0"}, {"MM_BINOMIAL_BLOCK": "64"}):
+                {"MM_BINOMIAL_TEAM_ITEMS": "300"}, {"MM_BINOMIAL_STAGE": "0"}, {"MM_BINOMIAL_BLOCK": "64"},
+                {"MM_BINOMIAL_PERM": "0"}, {"MM_BINOMIAL_PERM": "0", "MM_BINOMIAL_STAGE": "0"}):
         for k in ("MM_BINOMIAL_TEAM", "MM_BINOMIAL_GRID", "MM_BINOMIAL_CTA_ITEMS", "MM_BINOMIAL_TEAM_ITEMS",
-                  "MM_BINOMIAL_STAGE", "MM_BINOMIAL_BLOCK"):
+                  "MM_BINOMIAL_STAGE", "MM_BINOMIAL_BLOCK", "MM_BINOMIAL_PERM"):
             monkeypatch.delenv(k, raising=False)
         for k, v in env.items():
             monkeypatch.setenv(k, v)
