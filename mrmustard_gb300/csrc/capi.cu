@@ -593,7 +593,9 @@ constexpr int kBnMaxTeam = 16;
 constexpr int kBnMaxPerSm = 2;
 // Staged operands per CTA: every CTA copies them at launch, so a large prefix
 // permutation (108 KB at 30^4) costs more to stage than its L2 reads (measured).
-constexpr size_t kBnStageBytes = 48 * 1024;
+// With the kernel's static shared memory this stays under the 48 KB a launch may
+// use without opting in.
+constexpr size_t kBnStageBytes = 40 * 1024;
 constexpr int64_t kBnMaxPerm = 1 << 24;  // prefixes beyond this: no permutation (binary-search unranking)
 
 struct BinomialPlan {
@@ -754,7 +756,7 @@ int launch_binomial_D(const UniformPlan& P, const BinomialPlan& B, const Uniform
     t.perm_n = perm_n;
     if (fits(t)) stage = t;
   }
-  const size_t smem = bn_stage_bytes(stage);  // <= 48 KB: no opt-in attribute needed
+  const size_t smem = bn_stage_bytes(stage);  // <= kBnStageBytes: no opt-in attribute needed
   binomial_table_kernel<<<perm ? 2 : 1, 256, 0, st>>>(P.g, W1, const_cast<int64_t*>(S), W1p, Sp);
   MM_LAUNCHED();
   if (perm) {
