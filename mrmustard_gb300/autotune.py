@@ -27,7 +27,7 @@ from .settings import settings
 
 TEAM_MIN = (0, 1 << 17, 1 << 18, 1 << 19, 1 << 20)
 TEAM_CLUSTER = (4, 8, 16)
-VJP_ITEMS = (1 << 14, 1 << 15, 1 << 16, 1 << 17)
+VJP_ITEMS = (1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18, 1 << 19)
 
 
 def cache_path() -> Path:
