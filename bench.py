@@ -379,19 +379,22 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
 
     e2e_steps = max(2, min(args.steps, 5))
     e2e_modes = {}
-    for mode in ("prefetch", "zero_copy", "pipelined", "fused"):
+    # fused_sN: the forward writes the host copy of G for the instances k % 8 < N, the VJP the rest
+    for name, mode, split in (("prefetch", "prefetch", 0), ("zero_copy", "zero_copy", 0),
+                              ("pipelined", "pipelined", 0), ("fused", "fused", 0), ("fused_s2", "fused", 2),
+                              ("fused_s3", "fused", 3), ("fused_s4", "fused", 4)):
         with mm.settings(CHECK_DEVICE_STATUS=False):
-            rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode)
+            rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode, copy_split=split)
             torch.cuda.synchronize()
             barrier()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             for _ in range(e2e_steps):
-                rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode)
+                rb.step_host(A_h, b_h, c_h, g_h, G_h, dA_h, db_h, dc_h, cotangent=mode, copy_split=split)
             e1.record(stream)
             torch.cuda.synchronize()
             barrier()
-        e2e_modes[mode] = e0.elapsed_time(e1) / e2e_steps
+        e2e_modes[name] = e0.elapsed_time(e1) / e2e_steps
     e2e_mode = min(e2e_modes, key=e2e_modes.get)
     e2e_ms = e2e_modes[e2e_mode]
     rb.ws.check_status("e2e")

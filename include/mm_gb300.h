@@ -187,20 +187,31 @@ MM_API int mm_ragged_plan_offsets(const mm_ragged_plan *plan, int64_t *g_off, in
 MM_API int mm_ragged_plan_set_tuning(mm_ragged_plan *plan, int64_t team_min_amps, int64_t vjp_item_amps);
 /* CTAs per cluster team for the large instances: 1 (no teams), 2, 4, 8 (default) or 16. */
 MM_API int mm_ragged_plan_set_team_size(mm_ragged_plan *plan, int cluster_ctas);
+/* Split of a host copy of G between mm_ragged_fwd_copy_g and mm_ragged_vjp_copy_g: instances k
+ * with (k mod 8) < eighths get it from the forward, the others from the VJP (0..8, default 0).
+ * A host-buffer step uses it to drive the host link during the forward too. */
+MM_API int mm_ragged_plan_set_copy_split(mm_ragged_plan *plan, int eighths);
 /* Copy the plan's descriptors and work queues into ws (blocks the host until copied). */
 MM_API int mm_ragged_plan_upload(const mm_ragged_plan *plan, void *ws, size_t ws_bytes, mm_stream_t stream);
 
 /* Forward of every instance of an uploaded plan (vanilla or stable). */
 MM_API int mm_ragged_fwd(const mm_ragged_plan *plan, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c, int stable,
                   mm_c128 *G, void *ws, size_t ws_bytes, mm_stream_t stream);
+/* mm_ragged_fwd that also writes the forward's share (mm_ragged_plan_set_copy_split) of a copy
+ * of G to G_copy, which may be pinned host memory; G_copy = NULL is mm_ragged_fwd.  (No
+ * counterpart in the reference.) */
+MM_API int mm_ragged_fwd_copy_g(const mm_ragged_plan *plan, const mm_c128 *A, const mm_c128 *b, const mm_c128 *c,
+                                int stable, mm_c128 *G, mm_c128 *G_copy, void *ws, size_t ws_bytes,
+                                mm_stream_t stream);
 /* VJP of every instance of an uploaded plan.  G and dLdG may be any device-accessible
  * addresses, including pinned host memory (read by the kernels over the host link). */
 MM_API int mm_ragged_vjp(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG, mm_c128 *dA,
                   mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
-/* mm_ragged_vjp that also writes a copy of G (every amplitude, once) to G_copy, which may be
- * pinned host memory: the VJP kernels store the G values they load anyway, so a host-buffer
- * step gets G back over the host link while the VJP runs, without a copy-engine transfer.
- * G_copy = NULL is mm_ragged_vjp.  (No counterpart in the reference.) */
+/* mm_ragged_vjp that also writes a copy of G to G_copy, which may be pinned host memory: the
+ * VJP kernels store the G values they load anyway, so a host-buffer step gets G back over the
+ * host link while the VJP runs, without a copy-engine transfer.  Every amplitude of the
+ * instances outside the forward's share (mm_ragged_plan_set_copy_split; all of them by
+ * default) is written once.  G_copy = NULL is mm_ragged_vjp.  (No counterpart in the reference.) */
 MM_API int mm_ragged_vjp_copy_g(const mm_ragged_plan *plan, const mm_c128 *G, const mm_c128 *c, const mm_c128 *dLdG,
                                 mm_c128 *dA, mm_c128 *db, mm_c128 *dc, mm_c128 *G_copy, void *ws, size_t ws_bytes,
                                 mm_stream_t stream);

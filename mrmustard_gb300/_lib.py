@@ -54,6 +54,8 @@ SIGNATURES = {
     "mm_ragged_plan_set_team_size": (I32, [P, I32]),
     "mm_ragged_plan_upload": (I32, [P, P, SZ, P]),
     "mm_ragged_fwd": (I32, [P, P, P, P, I32, P, P, SZ, P]),
+    "mm_ragged_fwd_copy_g": (I32, [P, P, P, P, I32, P, P, P, SZ, P]),
+    "mm_ragged_plan_set_copy_split": (I32, [P, I32]),
     "mm_ragged_vjp": (I32, [P, P, P, P, P, P, P, P, SZ, P]),
     "mm_ragged_vjp_copy_g": (I32, [P, P, P, P, P, P, P, P, P, SZ, P]),
     "mm_hermite_fwd_host": (I32, [I32, P, P, P, P, I32, P, P]),

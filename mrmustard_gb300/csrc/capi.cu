@@ -385,6 +385,7 @@ struct mm_ragged_plan {
   int64_t team_min_amps = 0;
   int team_cluster = kTeamCluster;  // CTAs per cluster team (1 = no teams)
   int64_t vjp_item_amps = kVjpItemAmps;
+  int copy_split = 0;  // eighths of the instances whose host copy of G the forward writes
   Layout L;
 };
 
@@ -440,6 +441,7 @@ RaggedSrc ragged_src(const mm_ragged_plan* p, char* ws, const double2* A, const 
   s.coef = reinterpret_cast<double2*>(ws + p->L.coef);
   s.items = reinterpret_cast<const VjpItem*>(ws + p->L.items);
   s.Gout = nullptr;
+  s.fwd_copy_eighths = p->copy_split;
   return s;
 }
 }  // namespace
@@ -1060,6 +1062,12 @@ int mm_ragged_plan_set_tuning(mm_ragged_plan* plan, int64_t team_min_amps, int64
   return ragged_build(plan);
 }
 
+int mm_ragged_plan_set_copy_split(mm_ragged_plan* plan, int eighths) {
+  if (!plan || eighths < 0 || eighths > 8) return MM_ERR_INVALID_ARG;
+  plan->copy_split = eighths;
+  return MM_OK;
+}
+
 int mm_ragged_plan_set_team_size(mm_ragged_plan* plan, int cluster_ctas) {
   if (!plan || (cluster_ctas != 1 && cluster_ctas != 2 && cluster_ctas != 4 && cluster_ctas != 8 &&
                 cluster_ctas != 16))
@@ -1095,6 +1103,11 @@ int mm_ragged_plan_upload(const mm_ragged_plan* plan, void* ws, size_t ws_bytes,
 
 int mm_ragged_fwd(const mm_ragged_plan* plan, const mm_c128* A, const mm_c128* b, const mm_c128* c, int stable,
                   mm_c128* G, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  return mm_ragged_fwd_copy_g(plan, A, b, c, stable, G, nullptr, ws, ws_bytes, stream);
+}
+
+int mm_ragged_fwd_copy_g(const mm_ragged_plan* plan, const mm_c128* A, const mm_c128* b, const mm_c128* c,
+                         int stable, mm_c128* G, mm_c128* G_copy, void* ws, size_t ws_bytes, mm_stream_t stream) {
   if (!plan) return MM_ERR_INVALID_ARG;
   DevInfo di;
   int rc = device_info(di);
@@ -1105,6 +1118,7 @@ int mm_ragged_fwd(const mm_ragged_plan* plan, const mm_c128* A, const mm_c128* b
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   RaggedSrc src = ragged_src(plan, w, (const double2*)A, (const double2*)b, (const double2*)c, (double2*)G, nullptr);
+  src.Gout = (double2*)G_copy;  // the instances of the forward's share (copy_split) also go there
   if ((rc = reset_launch_state(w, st))) return rc;
   if ((rc = launch_setup(src, plan->B, w, plan->L, 1, st))) return rc;
   const double* rs = tables_of(w, plan->L).rs;

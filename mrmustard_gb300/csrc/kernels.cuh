@@ -46,6 +46,7 @@ struct InstView {
   double2* G;
   const double2* dLdG;
   const double2* coef;
+  double2* Gh;  // optional second destination of the forward's G (e.g. pinned host memory), or null
 };
 
 // Field-by-field geometry copy.  Views are never built by whole-struct
@@ -99,6 +100,7 @@ struct UniformSrc {
     v.G = G + k * g.n;
     v.dLdG = dLdG ? dLdG + k * g.n : nullptr;
     v.coef = coef + k * coef_stride;
+    v.Gh = nullptr;
   }
   __device__ __forceinline__ const Geom& geom(int64_t) const { return g; }
   __device__ __forceinline__ double2* coef_of(int64_t k) const { return coef + k * coef_stride; }
@@ -130,10 +132,16 @@ struct RaggedSrc {
   const double2* dLdG;
   double2* coef;
   const VjpItem* items;
-  double2* Gout;  // optional copy of G written by the VJP (may be pinned host memory), or null
+  double2* Gout;  // optional copy of G (may be pinned host memory), or null
+  // instances k with (k & 7) < fwd_copy_eighths get their copy of G from the
+  // forward (InstView::Gh), the others from the VJP (gout_of)
+  int32_t fwd_copy_eighths;
   __device__ __forceinline__ int64_t n_inst() const { return B; }
   __device__ __forceinline__ int64_t sched(int64_t t) const { return order[t]; }
-  __device__ __forceinline__ double2* gout_of(int64_t k) const { return Gout ? Gout + desc[k].g_off : nullptr; }
+  __device__ __forceinline__ bool fwd_copies(int64_t k) const { return (int32_t)(k & 7) < fwd_copy_eighths; }
+  __device__ __forceinline__ double2* gout_of(int64_t k) const {
+    return (Gout && !fwd_copies(k)) ? Gout + desc[k].g_off : nullptr;
+  }
   __device__ __forceinline__ void load(int64_t k, InstView& v) const {
     const InstDesc& d = desc[k];
     copy_geom(v.g, d.g);
@@ -143,6 +151,7 @@ struct RaggedSrc {
     v.G = G + d.g_off;
     v.dLdG = dLdG ? dLdG + d.g_off : nullptr;
     v.coef = coef + d.coef_off;
+    v.Gh = (Gout && fwd_copies(k)) ? Gout + d.g_off : nullptr;
   }
   __device__ __forceinline__ const Geom& geom(int64_t k) const { return desc[k].g; }
   __device__ __forceinline__ double2* coef_of(int64_t k) const { return coef + desc[k].coef_off; }
@@ -177,7 +186,10 @@ __device__ __forceinline__ double2 ldCoef(const InstView& v, const double2* p, i
   return *p;
 }
 __device__ __forceinline__ void stG(const InstView& v, int64_t f, double2 x, int tag) {
-  if (MM_CHK(v.G + f, v.G, v.g.n, double2, tag)) v.G[f] = x;
+  if (MM_CHK(v.G + f, v.G, v.g.n, double2, tag)) {
+    v.G[f] = x;
+    if (v.Gh) v.Gh[f] = x;
+  }
 }
 
 // ============================================================== setup kernel
@@ -411,13 +423,13 @@ __device__ __forceinline__ void stable_wave(const InstView& v, const double* __r
         vals = crfma(rs[k[i]], acc, vals);
       }
     }
-    G[f] = cscale(c_inv_n[npiv], vals);
+    stG(v, f, cscale(c_inv_n[npiv], vals), 6);
   }
 }
 
 template <int D>
 __device__ void stable_instance_cta(const InstView& v, const double* rs) {
-  if (threadIdx.x == 0) v.G[0] = v.c;
+  if (threadIdx.x == 0) stG(v, 0, v.c, 7);
   __syncthreads();
   int wmax = 0;
   for (int i = 0; i < D; ++i) wmax += (int)v.g.shape[i] - 1;
@@ -499,7 +511,7 @@ __device__ void fwd_instance_team(const InstView& v, const double* rs, uint32_t 
   if (v.g.sumC <= kScaledRow) {
     // as fwd_instance_cta: every CTA builds its own copy of the next chunk's scaled row
     ScaledRow* rows = scaled_rows();
-    if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
+    if (rank == 0 && threadIdx.x == 0) stG(v, 0, v.c, 7);
     int i = D - 1, m = 0;
     next_chunk(v.g, i, m);
     if (i >= 0) build_scaled_row(v, rs, i, m, rows[0]);
@@ -518,7 +530,7 @@ __device__ void fwd_instance_team(const InstView& v, const double* rs, uint32_t 
     }
     return;
   }
-  if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
+  if (rank == 0 && threadIdx.x == 0) stG(v, 0, v.c, 7);
   cluster_sync();
   for (int i = D - 1; i >= 0; --i) {
     const uint32_t si = (uint32_t)v.g.strides[i];
@@ -533,7 +545,7 @@ __device__ void fwd_instance_team(const InstView& v, const double* rs, uint32_t 
 
 template <int D>
 __device__ void stable_instance_team(const InstView& v, const double* rs, uint32_t rank, uint32_t nranks) {
-  if (rank == 0 && threadIdx.x == 0) v.G[0] = v.c;
+  if (rank == 0 && threadIdx.x == 0) stG(v, 0, v.c, 7);
   cluster_sync();
   int wmax = 0;
   for (int i = 0; i < D; ++i) wmax += (int)v.g.shape[i] - 1;
@@ -1140,6 +1152,7 @@ __global__ void view_selftest_kernel(Src src, int64_t k, const InstView* __restr
     nbad += sv.G != e.G;
     nbad += sv.dLdG != e.dLdG;
     nbad += sv.coef != e.coef;
+    nbad += sv.Gh != e.Gh;
     nbad += sv.c.x != e.c.x || sv.c.y != e.c.y;
     nbad += sv.g.D != e.g.D || sv.g.maxC != e.g.maxC || sv.g.n != e.g.n || sv.g.sumC != e.g.sumC;
     for (int j = 0; j < MM_MAXD; ++j)
@@ -1683,7 +1696,7 @@ __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, 
     src.load(k, sv);
     sq0 = q0;
     sq1 = q1;
-    if constexpr (COPY) sgo = src.gout_of(k);
+    sgo = COPY ? src.gout_of(k) : nullptr;  // null also when the forward made this instance's copy
   }
   __syncthreads();
   const int D = sv.g.D;
@@ -1693,7 +1706,8 @@ __global__ void __launch_bounds__(MM_BLOCK) vjp_items_kernel(Src src, Tables T, 
     if (D == DD) {                                            \
       double2 tot[vjp_nv(DD)];                                \
       for (int s = 0; s < vjp_nv(DD); ++s) tot[s] = cmk(0, 0); \
-      vjp_fibers<DD, COPY>(sv, T, sq0, sq1, tot, sgo);        \
+      if (COPY && sgo) vjp_fibers<DD, COPY>(sv, T, sq0, sq1, tot, sgo); \
+      else vjp_fibers<DD, false>(sv, T, sq0, sq1, tot);       \
       block_reduce_write<vjp_nv(DD)>(tot, out);               \
       return;                                                 \
     }                                                         \

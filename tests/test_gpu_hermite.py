@@ -481,6 +481,15 @@ def test_ragged_step_host_matches_device(cuda, oracle_lib):
         assert torch.equal(G_h, G_ref.cpu()), mode
         for o, r in zip(outs, ref):
             assert torch.equal(o, r.cpu()), (mode, chunks)
+    # the host copy of G split between the forward (instances k % 8 < s) and the VJP
+    for split in (3, 8, 1, 0):
+        for o in (G_h, *outs):
+            o.fill_(float("nan"))
+        rb.step_host(A_h, b_h, c_h, g_h, G_h, *outs, cotangent="fused", copy_split=split)
+        torch.cuda.synchronize()
+        assert torch.equal(G_h, G_ref.cpu()), split
+        for o, r in zip(outs, ref):
+            assert torch.equal(o, r.cpu()), split
 
 
 def test_ragged_schedules_agree(cuda, oracle_lib):
