@@ -58,6 +58,11 @@ def test_ragged_plan_on_host():
         assert lib.mm_ragged_plan_workspace_bytes(plan) > 512
         assert lib.mm_ragged_plan_set_tuning(plan, 0, 1000) == 0
         assert lib.mm_ragged_plan_set_tuning(plan, -1, 1000) == 1
+        # split of the host copy of G between forward and VJP: eighths 0..8
+        for s in (0, 2, 8):
+            assert lib.mm_ragged_plan_set_copy_split(plan, s) == 0
+        assert lib.mm_ragged_plan_set_copy_split(plan, 9) == 1
+        assert lib.mm_ragged_plan_set_copy_split(plan, -1) == 1
     finally:
         lib.mm_ragged_plan_destroy(plan)
     bad = np.array([2, 0], np.int64)
