@@ -192,7 +192,7 @@ class RaggedBatch:
         return chunks
 
     def step_host(self, A_h, b_h, c_h, dLdG_h, G_h, dA_h, db_h, dc_h, stable: bool = False,
-                  cotangent: str = "zero_copy", chunks: int = 2, copy_split: int = 2):
+                  cotangent: str = "fused", chunks: int = 2, copy_split: int = 2):
         """One forward + VJP step with every input and output in pinned host memory.
 
         A, b, c (small) are copied to the device and the forward writes G in device memory; G is
