@@ -195,9 +195,10 @@ class RaggedBatch:
                   cotangent: str = "fused", chunks: int = 2, copy_split: int = 2):
         """One forward + VJP step with every input and output in pinned host memory.
 
-        A, b, c (small) are copied to the device and the forward writes G in device memory; G is
-        copied back on a second stream while the VJP runs.  The cotangent dL/dG reaches the VJP in
-        one of three ways, all overlapped with compute:
+        A, b, c (small) are copied to the device and the forward writes G in device memory.  The
+        two large tensors (dL/dG in, G out) move in one of four ways, all overlapped with compute
+        (the default, ``"fused"`` with ``copy_split=2``, measured fastest); in the first three, G
+        goes back by copy engine on a second stream while the VJP runs:
 
         * ``"prefetch"``: copied into device memory on the second stream while the forward runs;
         * ``"zero_copy"``: read by the VJP kernels straight from the pinned host buffer over the
