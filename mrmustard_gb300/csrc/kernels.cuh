@@ -1172,11 +1172,14 @@ __global__ void wait_timeout_test_kernel(WsHeader* h, uint64_t budget_ns) { grid
 // exceeds max_l2.  Each amplitude obeys the vanilla recurrence with the first
 // non-zero axis as pivot (steps.vanilla_step), computed as fwd_chunk does.
 //
-// Only the waves up to the stop are computed.  Wave w's amplitudes are taken
-// by lexicographic rank r in [0, n_w) (the order of paths.binomial_subspace_basis)
-// and unranked through cumulative composition counts: S_j[x] = number of
-// (k_j, ..., k_{D-1}) inside the cutoffs with sum <= x, rows j = 0..D of W1 =
-// (max weight + 1) entries each (S_D[x] = 1), so n_w = S_0[w] - S_0[w-1].
+// Only the waves up to the stop are computed.  Wave w has n_w = S_0[w] -
+// S_0[w-1] amplitudes, from cumulative composition counts S_j[x] = number of
+// (k_j, ..., k_{D-1}) inside the cutoffs with sum <= x (rows j = 0..D of W1 =
+// max weight + 1 entries, S_D[x] = 1).  Its rank r in [0, n_w) maps to an
+// index either through the weight-sorted prefix permutation
+// (binomial_perm_kernel: one read) or, for very many prefixes, by unranking
+// the lexicographic order of paths.binomial_subspace_basis (a binary search
+// per axis in S).  The rank order only fixes the order of the norm's sums.
 struct BinomialState {
   double norm;      // |c|^2 plus the sums of the waves filled so far
   int32_t stopped;  // 1 once the running norm exceeded max_l2
