@@ -21,6 +21,8 @@ Cases (each cites the reference test it mirrors):
 * ``dm4``: 4-index density-matrix style triple (complex symmetric A, spectral norm 0.89), shape 6^4.
 * ``dgate``: displacement gate alpha = 4+4j at 60x60, vanilla + stable + the reference's
   closed-form ``displacement`` strategy (tests/test_math/test_lattice/test_lattice_functions.py:141-152).
+* ``many5``..``many8`` (in ``hermite_golden_many.npz``): ``random_triple(D)`` at D = 5..8 with small
+  uneven shapes, vanilla + stable + VJP.
 
 Usage (from the repository root)::
 
@@ -207,6 +209,17 @@ def main(ref_root: str):
 
     np.savez_compressed(HERE / "hermite_golden.npz", **out)
     print("wrote", HERE / "hermite_golden.npz", "with", len(out), "arrays")
+
+    # D = 5..8 (the GPU library's largest mode counts), small uneven shapes, in a second file read
+    # only by the oracle's tests: the GPU is checked against the oracle at these D.  (`single`
+    # writes into whatever `out` is bound to.)
+    out = {}
+    for D, shape, seed in ((5, (3, 2, 3, 1, 2), 51), (6, (2, 2, 3, 2, 1, 2), 52), (7, (2, 1, 2, 2, 2, 1, 2), 53),
+                           (8, (2, 2, 1, 2, 2, 1, 2, 2), 54)):
+        A, b, c = random_triple(D, (), seed=seed)
+        single(f"many{D}", A, b, c, shape, seed=50 + D)
+    np.savez_compressed(HERE / "hermite_golden_many.npz", **out)
+    print("wrote", HERE / "hermite_golden_many.npz", "with", len(out), "arrays")
 
 
 if __name__ == "__main__":

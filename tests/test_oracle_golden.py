@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 from scipy.special import eval_hermite, factorial
 
-from conftest import golden_cases
+from conftest import ROOT, golden_cases
 
 import oracle
 
@@ -52,6 +52,26 @@ def test_vjp_matches_reference(golden):
         assert oracle.rel_err(dA, golden[f"{n}/dA"]) < 1e-14, n
         assert oracle.rel_err(db, golden[f"{n}/db"]) < 1e-14, n
         assert abs(dc - golden[f"{n}/dc"]) <= 1e-13 * max(1.0, abs(golden[f"{n}/dc"])), n
+
+
+def test_many_modes_match_reference():
+    """D = 5..8 (the largest mode counts of the GPU library, whose GPU tests compare with the
+    oracle): the oracle's forward is bit-exact with the reference source under numpy's division
+    lowering, its stable forward and VJP agree to the usual tolerances."""
+    z = np.load(ROOT / "tests" / "golden" / "hermite_golden_many.npz")
+    names = sorted({k.split("/")[0] for k in z.files})
+    assert names == ["many5", "many6", "many7", "many8"]
+    for n in names:
+        sh = tuple(z[f"{n}/shape"])
+        A, b, c = z[f"{n}/A"], z[f"{n}/b"], z[f"{n}/c"]
+        oracle.set_numpy_division(True)
+        assert np.array_equal(oracle.vanilla(sh, A, b, c), z[f"{n}/G"]), n
+        assert np.array_equal(oracle.stable(sh, A, b, c), z[f"{n}/G_stable"]), n
+        oracle.set_numpy_division(False)
+        dA, db, dc = oracle.vjp(z[f"{n}/G"], c, z[f"{n}/dLdG"])
+        assert oracle.rel_err(dA, z[f"{n}/dA"]) < 1e-14, n
+        assert oracle.rel_err(db, z[f"{n}/db"]) < 1e-14, n
+        assert abs(dc - z[f"{n}/dc"]) <= 1e-13 * max(1.0, abs(z[f"{n}/dc"])), n
 
 
 def test_batch_matches_reference(golden):
