@@ -62,3 +62,44 @@ def test_einsum_subscript_parsing():
         parse_subscripts("...a->a", 1)
     with pytest.raises(ValueError):
         parse_subscripts("ab,bc->ac", 3)
+
+
+def test_diagonal_input_validation_raises_before_device_work():
+    """The compactFock entry points check their inputs as inputValidation.py:25-58 and :61-100
+    do (same exceptions and messages), before any device work."""
+    A = np.eye(4, dtype=complex) * 0.1
+    B = np.zeros(4, complex)
+    with pytest.raises(ValueError, match="must be square"):
+        mm.hermite_multidimensional_diagonal(np.zeros((4, 3), complex), B, 1.0, (3, 3))
+    bad = A.copy()
+    bad[0, 1] = np.nan
+    with pytest.raises(ValueError, match="must not contain NaNs"):
+        mm.hermite_multidimensional_diagonal(bad, B, 1.0, (3, 3))
+    asym = A.copy()
+    asym[0, 1] = 0.5
+    with pytest.raises(ValueError, match="must be symmetric"):
+        mm.hermite_multidimensional_diagonal(asym, B, 1.0, (3, 3))
+    with pytest.raises(ValueError, match="unbactched or two dimensional"):
+        mm.hermite_multidimensional_diagonal(A, np.zeros((4, 2, 2), complex), 1.0, (3, 3))
+    with pytest.raises(ValueError, match="incompatible dimensions"):
+        mm.hermite_multidimensional_diagonal(A, np.zeros(6, complex), 1.0, (3, 3))
+    with pytest.raises(ValueError, match="array like of length M"):
+        mm.hermite_multidimensional_diagonal(A, B, 1.0, 3)
+    with pytest.raises(ValueError, match="A and cutoffs have incompatible"):
+        mm.hermite_multidimensional_diagonal(A, B, 1.0, (3, 3, 3))
+    with pytest.raises(TypeError, match="NumPy array"):
+        mm.hermite_multidimensional_diagonal([[0.1, 0], [0, 0.1]], B, 1.0, (3,))
+
+
+def test_leftover_input_validation_raises_before_device_work():
+    """hermite_multidimensional_1leftoverMode's checks (inputValidation.py:103-119)."""
+    A = np.eye(4, dtype=complex) * 0.1
+    B = np.zeros(4, complex)
+    with pytest.raises(ValueError, match="incompatible dimensions"):
+        mm.hermite_multidimensional_1leftoverMode(A, np.zeros(6, complex), 1.0, (3, 3))
+    with pytest.raises(ValueError, match="array like of length M"):
+        mm.hermite_multidimensional_1leftoverMode(A, B, 1.0, 3)
+    with pytest.raises(ValueError, match="A and cutoffs have incompatible"):
+        mm.hermite_multidimensional_1leftoverMode(A, B, 1.0, (3, 3, 3))
+    with pytest.raises(ValueError, match="greater than 1"):
+        mm.hermite_multidimensional_1leftoverMode(np.eye(2, dtype=complex) * 0.1, np.zeros(2, complex), 1.0, (3,))
