@@ -18,6 +18,7 @@ Cases:
 * ``thermal*``: mixed states with a Hermitian bra-ket block.
 * ``clip*``, ``prob*``: the max_shape / min_shape clips and other max_prob thresholds.
 * ``rand*``: random pure states (M = 1..5) and pure states with an added bra-ket block.
+* ``sq6``..``sq8``, ``coh6``..``coh8`` (in ``autoshape_golden_many.npz``): M = 6..8.
 
 Usage (from the repository root)::
 
@@ -160,6 +161,25 @@ def main(ref_root: str):
 
     out["names"] = np.array(names)
     np.savez(HERE / "autoshape_golden.npz", **out)
+    for n in names:
+        print(n, tuple(out[f"{n}/shape"]))
+
+    # M = 6..8 (the GPU library's largest mode counts), in a second file read only by the oracle's
+    # tests: squeezed vacua and coherent products rotated by a passive unitary (closed-form norms).
+    # (`case` writes into whatever `out` and `names` are bound to.)
+    out, names = {}, []
+    for M in (6, 7, 8):
+        rng = np.random.default_rng(1300 + M)
+        r = rng.uniform(0.1, 0.6, M)
+        phi = rng.uniform(0, 2 * np.pi, M)
+        U = haar(M, 1400 + M)
+        A = U @ np.diag(-np.exp(1j * phi) * np.tanh(r)) @ U.T
+        case(f"sq{M}", *ket_to_dm(A, np.zeros(M), np.prod(np.cosh(r) ** -0.5)))
+        alpha = 0.8 * (rng.normal(0, 1.0, M) + 1j * rng.normal(0, 1.0, M))
+        V = haar(M, 1500 + M)
+        case(f"coh{M}", *ket_to_dm(np.zeros((M, M)), V @ alpha, np.exp(-np.sum(np.abs(alpha) ** 2) / 2)))
+    out["names"] = np.array(names)
+    np.savez(HERE / "autoshape_golden_many.npz", **out)
     for n in names:
         print(n, tuple(out[f"{n}/shape"]))
 

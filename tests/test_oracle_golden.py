@@ -141,6 +141,22 @@ def test_autoshape_oracle_matches_reference(autoshape_golden):
         oracle.set_numpy_division(False)
 
 
+def test_autoshape_oracle_matches_reference_many_modes():
+    """M = 6..8 (squeezed vacua and coherent products, tests/golden/autoshape_golden_many.npz): the
+    oracle gives the reference source's cutoffs; the GPU kernel is checked against the oracle there."""
+    z = np.load(ROOT / "tests" / "golden" / "autoshape_golden_many.npz")
+    assert sorted(str(n) for n in z["names"]) == ["coh6", "coh7", "coh8", "sq6", "sq7", "sq8"]
+    try:
+        for numpy_div in (True, False):
+            oracle.set_numpy_division(numpy_div)
+            for n in z["names"]:
+                p, hi, lo = z[f"{n}/params"]
+                got = oracle.autoshape(z[f"{n}/A"], z[f"{n}/b"], z[f"{n}/c"], p, int(hi), int(lo))
+                assert np.array_equal(got, z[f"{n}/shape"]), (n, numpy_div, got, z[f"{n}/shape"])
+    finally:
+        oracle.set_numpy_division(False)
+
+
 def test_autoshape_oracle_ragged_equals_single(autoshape_golden):
     g = autoshape_golden
     names = list(g["names"])
