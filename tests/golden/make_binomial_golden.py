@@ -108,7 +108,7 @@ def main(ref_root: str):
         U = unitary_group.rvs(M, random_state=seed) if M > 1 else np.exp(1j * rng.uniform(0, 6, (1, 1)))
         A = (U * rng.uniform(0.0, smax, M)) @ U.T
         b = sigma * (rng.standard_normal(M) + 1j * rng.standard_normal(M)) / np.sqrt(2)
-        cut = {1: 150, 2: 80, 3: 40, 4: 24}[M]
+        cut = {1: 150, 2: 80, 3: 40, 4: 24, 5: 14, 6: 9, 8: 5}[M]
         G = oracle.vanilla((cut,) * M, A, b, 1.0 + 0j)
         return A, b, 1.0 / np.sqrt(np.sum(np.abs(G) ** 2))
 
@@ -121,12 +121,27 @@ def main(ref_root: str):
             case(f"ket{M}_{k}", cut, A, b, c, l2, gc)
         case(f"full{M}", cut, A, b, c, 2.0, sum(cut) - M + 1)
 
-    out["names"] = np.array(names)
-    np.savez(HERE / "binomial_golden.npz", **out)
-    for n in names:
-        G = out[f"{n}/G"]
-        filled = int(np.count_nonzero(G))
-        print(n, tuple(out[f"{n}/shape"]), "norm", float(out[f"{n}/norm"]), "filled", filled, "of", G.size)
+    def save(fname):
+        out["names"] = np.array(names)
+        np.savez(HERE / fname, **out)
+        for n in names:
+            G = out[f"{n}/G"]
+            filled = int(np.count_nonzero(G))
+            print(n, tuple(out[f"{n}/shape"]), "norm", float(out[f"{n}/norm"]), "filled", filled, "of", G.size)
+
+    save("binomial_golden.npz")
+
+    # D = 5, 6, 8 in a second file read only by the oracle's tests (the GPU is checked against the
+    # oracle there).  (`case` writes into whatever `out` and `names` are bound to.)
+    out, names = {}, []
+    for M, cut in ((5, (3, 2, 3, 2, 3)), (6, (2, 3, 2, 2, 3, 2)), (8, (2, 2, 2, 2, 2, 2, 2, 2))):
+        A, b, c = ket(M, 100 + M)
+        gc = sum(cut) - M + 1
+        case(f"full{M}", cut, A, b, c, 2.0, gc)
+        full = float(out[f"full{M}/norm"])  # the small cutoffs hold only part of the state's norm
+        for k, (l2, g) in enumerate(((0.3 * full, gc), (0.7 * full, gc), (0.95 * full, gc), (2.0, sum(cut) // 2))):
+            case(f"ket{M}_{k}", cut, A, b, c, l2, g)
+    save("binomial_golden_many.npz")
 
 
 if __name__ == "__main__":

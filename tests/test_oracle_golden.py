@@ -190,6 +190,29 @@ def test_binomial_oracle_matches_reference(binomial_golden):
         oracle.set_numpy_division(False)
 
 
+def test_binomial_oracle_matches_reference_many_modes():
+    """D = 5, 6, 8 (tests/golden/binomial_golden_many.npz: full fills and early stops at 30 %, 70 %
+    and 95 % of the reachable norm): the oracle gives the reference source's tensors bit for bit
+    under numpy's division lowering and its stop weights; the GPU is checked against the oracle."""
+    z = np.load(ROOT / "tests" / "golden" / "binomial_golden_many.npz")
+    assert len(z["names"]) == 15
+    try:
+        for numpy_div in (True, False):
+            oracle.set_numpy_division(numpy_div)
+            for n in z["names"]:
+                l2, gc = z[f"{n}/params"]
+                G, norm, _ = oracle.binomial(tuple(z[f"{n}/shape"]), z[f"{n}/A"], z[f"{n}/b"], z[f"{n}/c"], l2, int(gc))
+                ref = z[f"{n}/G"]
+                assert np.array_equal(G == 0, ref == 0), n
+                if numpy_div:
+                    assert np.array_equal(G, ref), n
+                else:
+                    assert np.abs(G - ref).max() <= 1e-15 * np.abs(ref).max(), n
+                assert abs(norm - float(z[f"{n}/norm"])) <= 1e-15 * abs(float(z[f"{n}/norm"])), n
+    finally:
+        oracle.set_numpy_division(False)
+
+
 def test_binomial_oracle_equals_vanilla_prefix(binomial_golden):
     """test_lattice_functions.py:122-138: binomial with local cutoffs (5, 5) equals the vanilla
     tensor's [:5, :5] block where it is filled."""
