@@ -131,6 +131,29 @@ def main(ref_root: str):
     for n in names:
         print(n, str(out[f"{n}/kind"]))
 
+    # M = 5, 6 in a second file read only by the oracle's tests (the GPU is checked against the
+    # oracle there).  (`put` writes into whatever `out` and `names` are bound to.)
+    out, names = {}, []
+    for M, cut in ((5, (3, 2, 2, 3, 2)), (6, (2, 2, 2, 2, 2, 2))):
+        A, b, c = dm_triple(M, 700 + M)
+        Ai, bi = interleave(A, b)
+        r = iv.hermite_multidimensional_diagonal(Ai, bi, c, cut)
+        put(f"amps{len(names)}", "amps", A=Ai, B=bi, G0=c, cutoffs=np.array(cut), arr0=r[0], arr2=r[1],
+            arr1010=r[2], arr1001=r[3], arr1=r[4])
+        g = iv.grad_hermite_multidimensional_diagonal(Ai, bi, c, *r)
+        put(f"grad{len(names)}", "grad", A=Ai, B=bi, G0=c, cutoffs=np.array(cut), dG0=g[0], dA=g[1], dB=g[2])
+    for M, cut in ((5, (3, 2, 2, 2, 2)),):
+        A, b, c = dm_triple(M, 800 + M)
+        Ai, bi = interleave(A, b)
+        r = iv.hermite_multidimensional_1leftoverMode(Ai, bi, c, cut)
+        g = iv.grad_hermite_multidimensional_1leftoverMode(Ai, bi, c, *r)
+        put(f"lo{len(names)}", "lo", A=Ai, B=bi, G0=c, cutoffs=np.array(cut), arr0=r[0], arr2=r[1], arr1010=r[2],
+            arr1001=r[3], arr1=r[4], dG0=g[0], dA=g[1], dB=g[2])
+    out["names"] = np.array(names)
+    np.savez_compressed(HERE / "diagonal_golden_many.npz", **out)
+    for n in names:
+        print(n, str(out[f"{n}/kind"]))
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

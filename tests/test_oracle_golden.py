@@ -268,6 +268,38 @@ def test_diagonal_grad_oracle_matches_reference(diagonal_golden):
         oracle.set_numpy_division(False)
 
 
+def test_diagonal_and_leftover_oracle_match_reference_many_modes():
+    """M = 5, 6 (tests/golden/diagonal_golden_many.npz): the diagonal amplitudes and Jacobians and
+    the leftover-mode blocks and Jacobians of the oracle against the reference source, with the
+    tolerances of the M <= 4 tests; the GPU kernels are checked against the oracle there."""
+    from conftest import diagonal_cases
+
+    z = np.load(ROOT / "tests" / "golden" / "diagonal_golden_many.npz")
+    assert sorted(str(z[f"{n}/kind"]) for n in z["names"]) == ["amps", "amps", "grad", "grad", "lo"]
+    try:
+        oracle.set_numpy_division(True)
+        for n in diagonal_cases(z, "amps"):
+            got = oracle.diagonal_amps(z[f"{n}/A"], z[f"{n}/B"], z[f"{n}/G0"], tuple(z[f"{n}/cutoffs"]))
+            for name, x in zip(("arr0", "arr2", "arr1010", "arr1001", "arr1"), got):
+                ref = z[f"{n}/{name}"]
+                assert x.shape == ref.shape and np.array_equal(x == 0, ref == 0), (n, name)
+                assert _rel(x, ref) <= 1e-14, (n, name, _rel(x, ref))
+        for n in diagonal_cases(z, "grad"):
+            got = oracle.diagonal_grad(z[f"{n}/A"], z[f"{n}/B"], z[f"{n}/G0"], tuple(z[f"{n}/cutoffs"]))
+            for name, x in zip(("dG0", "dA", "dB"), got):
+                assert _rel(x, z[f"{n}/{name}"]) <= 1e-13, (n, name)
+        for n in diagonal_cases(z, "lo"):
+            A, B, G0, cut = z[f"{n}/A"], z[f"{n}/B"], z[f"{n}/G0"], tuple(z[f"{n}/cutoffs"])
+            for name, x in zip(("arr0", "arr2", "arr1010", "arr1001", "arr1"), oracle.leftover_amps(A, B, G0, cut)):
+                ref = z[f"{n}/{name}"]
+                assert x.shape == ref.shape and np.array_equal(x == 0, ref == 0), (n, name)
+                assert _rel(x, ref) <= 1e-14, (n, name, _rel(x, ref))
+            for name, x in zip(("dG0", "dA", "dB"), oracle.leftover_grad(A, B, G0, cut)):
+                assert _rel(x, z[f"{n}/{name}"]) <= 1e-13, (n, name)
+    finally:
+        oracle.set_numpy_division(False)
+
+
 def test_diagonal_amps_equal_vanilla_diagonal(diagonal_golden):
     """tests/test_math/test_compactFock.py:19-43: arr0[k] = G[k0, k0, k1, k1, ...] of the vanilla
     tensor on the interleaved triple."""
