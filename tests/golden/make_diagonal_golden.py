@@ -149,6 +149,12 @@ def main(ref_root: str):
         g = iv.grad_hermite_multidimensional_1leftoverMode(Ai, bi, c, *r)
         put(f"lo{len(names)}", "lo", A=Ai, B=bi, G0=c, cutoffs=np.array(cut), arr0=r[0], arr2=r[1], arr1010=r[2],
             arr1001=r[3], arr1=r[4], dG0=g[0], dA=g[1], dB=g[2])
+    for L, oc, pnr, seed in ((5, 2, (2, 1, 2, 1), 21), (6, 1, (1, 1, 1, 1, 1), 22)):
+        A, b, c = dm_triple(L, 900 + seed)
+        for stable in (False, True):
+            G = fd.fast_diagonal(A, b, c, oc, pnr, stable=stable)
+            put(f"fd{len(names)}", "fd", A=A, b=b, c=c, oc=np.int64(oc), pnr=np.array(pnr), stable=np.int64(stable),
+                out=G)
     out["names"] = np.array(names)
     np.savez_compressed(HERE / "diagonal_golden_many.npz", **out)
     for n in names:

@@ -269,13 +269,14 @@ def test_diagonal_grad_oracle_matches_reference(diagonal_golden):
 
 
 def test_diagonal_and_leftover_oracle_match_reference_many_modes():
-    """M = 5, 6 (tests/golden/diagonal_golden_many.npz): the diagonal amplitudes and Jacobians and
-    the leftover-mode blocks and Jacobians of the oracle against the reference source, with the
-    tolerances of the M <= 4 tests; the GPU kernels are checked against the oracle there."""
+    """M = 5, 6 (tests/golden/diagonal_golden_many.npz): the diagonal amplitudes and Jacobians, the
+    leftover-mode blocks and Jacobians and fast_diagonal of the oracle against the reference source,
+    with the tolerances of the M <= 4 tests; the GPU kernels are checked against the oracle there."""
     from conftest import diagonal_cases
 
     z = np.load(ROOT / "tests" / "golden" / "diagonal_golden_many.npz")
-    assert sorted(str(z[f"{n}/kind"]) for n in z["names"]) == ["amps", "amps", "grad", "grad", "lo"]
+    assert sorted(str(z[f"{n}/kind"]) for n in z["names"]) == ["amps", "amps", "fd", "fd", "fd", "fd", "grad", "grad",
+                                                                  "lo"]
     try:
         oracle.set_numpy_division(True)
         for n in diagonal_cases(z, "amps"):
@@ -296,6 +297,12 @@ def test_diagonal_and_leftover_oracle_match_reference_many_modes():
                 assert _rel(x, ref) <= 1e-14, (n, name, _rel(x, ref))
             for name, x in zip(("dG0", "dA", "dB"), oracle.leftover_grad(A, B, G0, cut)):
                 assert _rel(x, z[f"{n}/{name}"]) <= 1e-13, (n, name)
+        for n in diagonal_cases(z, "fd"):  # fast_diagonal at L = 5, 6, vanilla and stable first block
+            got = oracle.fast_diagonal(z[f"{n}/A"], z[f"{n}/b"], z[f"{n}/c"], int(z[f"{n}/oc"]),
+                                       tuple(z[f"{n}/pnr"]), bool(z[f"{n}/stable"]))
+            ref = z[f"{n}/out"]
+            assert got.shape == ref.shape and np.array_equal(got == 0, ref == 0), n
+            assert _rel(got, ref) <= 1e-14, (n, _rel(got, ref))
     finally:
         oracle.set_numpy_division(False)
 
