@@ -32,30 +32,58 @@ METRIC = "Fock amplitudes/s fwd+VJP (c128, <=1e-12 rel) batched vs plain, 1 GB30
 UNIT = "amplitudes/s"
 N_INST = 4096
 VJP_DRAM_BYTES_PER_AMP = 50.3  # dram read + write per amplitude, ncu capture of the VJP items kernel
+ERR_TOL = 1e-12                # max |x - oracle| / max |oracle| per instance, G and every gradient
+MIN_BATCHED_OVER_PLAIN = 10.0  # one batched launch vs a loop of per-instance launches
 
 
 # ------------------------------------------------------------------ workload
-def make_workload(base_seed: int, n: int = N_INST):  # noqa: C901
-    """Per-instance seeded triples: (shapes, As, bs, cs)."""
+BASE_SEED = 20260000
+
+
+def _instance(base_seed: int, k: int, with_triple: bool):
+    rng = np.random.default_rng(base_seed + k)
+    D = int(rng.integers(1, 5))
+    shape = tuple(int(x) for x in rng.integers(5, 41, D))
+    if not with_triple:
+        return shape, None, None
     from scipy.stats import unitary_group
 
+    if D == 1:
+        Q = np.exp(1j * rng.uniform(0, 2 * np.pi, (1, 1)))
+    else:
+        Q = unitary_group.rvs(D, random_state=rng)
+    s = rng.uniform(0.0, 0.8, D)
+    A = (Q * s) @ Q.T
+    b = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+    return shape, A.astype(np.complex128), b.astype(np.complex128)
+
+
+def workload_shapes(base_seed: int, n: int):
+    """Shapes of instances 0..n-1 (the first draws of each instance's generator)."""
+    return [_instance(base_seed, k, False)[0] for k in range(n)]
+
+
+def make_workload(base_seed: int, n: int = N_INST, indices=None):
+    """Per-instance seeded triples: (shapes, As, bs, cs) of instances `indices` (default 0..n-1)."""
+    idx = range(n) if indices is None else indices
     shapes, As, bs = [], [], []
-    for k in range(n):
-        rng = np.random.default_rng(base_seed + k)
-        D = int(rng.integers(1, 5))
-        shape = tuple(int(x) for x in rng.integers(5, 41, D))
-        if D == 1:
-            Q = np.exp(1j * rng.uniform(0, 2 * np.pi, (1, 1)))
-        else:
-            Q = unitary_group.rvs(D, random_state=rng)
-        s = rng.uniform(0.0, 0.8, D)
-        A = (Q * s) @ Q.T
-        b = 0.3 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(2)
+    for k in idx:
+        shape, A, b = _instance(base_seed, int(k), True)
         shapes.append(shape)
-        As.append(A.astype(np.complex128))
-        bs.append(b.astype(np.complex128))
-    cs = np.ones(n, np.complex128)
+        As.append(A)
+        bs.append(b)
+    cs = np.ones(len(shapes), np.complex128)
     return shapes, As, bs, cs
+
+
+def workload_config(n_instances: int, amplitudes: int, world: int) -> dict:
+    """The workload both arms run (identical dict in the GB300 and the reference line)."""
+    return {"workload": f"ragged batch: {n_instances} triples, D~U{{1..4}}, cutoff~U{{5..40}}, Takagi A "
+                        "s~U(0,0.8), b sigma 0.3, c=1, fwd+VJP per step",
+            "instances": n_instances, "amplitudes": int(amplitudes),
+            "l2": "inputs larger than L2 (G, dLdG ~4.4 GB per 4096 triples)",
+            "parallelism": (f"instances sharded over {world} ranks (cost-balanced, no collective)" if world > 1
+                            else "one GPU")}
 
 
 def fp64_ops(shape):
@@ -153,7 +181,7 @@ def run_reference(args, rank, world):
     import oracle
 
     oracle.build()
-    shapes, As, bs, cs = make_workload(20260000, args.instances)
+    shapes, As, bs, cs = make_workload(BASE_SEED, args.instances * world)
     rh = oracle.RaggedHost(shapes)
     A = np.concatenate([a.ravel() for a in As])
     b = np.concatenate(bs)
@@ -186,9 +214,7 @@ def run_reference(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"ragged batch: {len(shapes)} triples, D~U{{1..4}}, cutoff~U{{5..40}}, Takagi A "
-                               "s~U(0,0.8), b sigma 0.3, c=1, fwd+VJP", "instances": len(shapes),
-                   "amplitudes": int(rh.total)},
+        "config": workload_config(len(shapes), int(rh.total), world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -215,9 +241,13 @@ def run_gb300(args, rank, local_rank, world):
     lib = _lib.load()
     stream = torch.cuda.current_stream(dev)
 
-    # --- workload (weak scaling: every rank its own 4096 triples)
-    shapes, As, bs, cs = make_workload(20260000 + rank * N_INST, args.instances)
-    rb = mm.RaggedBatch(shapes, device=dev)
+    # --- workload: one batch of 4096 x world triples, split over the ranks by cost (weak scaling:
+    #     about 4096 triples' work per GPU; no collective on the data path)
+    n_global = args.instances * world
+    shapes_all = workload_shapes(BASE_SEED, n_global)
+    total_all = int(sum(int(np.prod(s)) for s in shapes_all))
+    rb = mm.RaggedBatch.shard(shapes_all, rank, world, device=dev)
+    shapes, As, bs, cs = make_workload(BASE_SEED, indices=rb.global_index)
     A, b, c = rb.pack(As, bs, cs)
     gen = torch.Generator(device=dev)
     gen.manual_seed(7 + rank)
@@ -263,7 +293,7 @@ def run_gb300(args, rank, local_rank, world):
         t = torch.tensor([ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         ms = float(t.item())
-    value = total * world / (ms * 1e-3)
+    value = total_all / (ms * 1e-3)
     clocks = clk.summary()
 
     # --- device status after the timed region
@@ -317,17 +347,29 @@ def run_gb300(args, rank, local_rank, world):
     else:
         e2e_ms, h2d, d2h, plain_value, cpu, extras = run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads,
                                                                 shapes, As, bs, cs, time_eager, dfma_peak)
+    # self-certification: oracle error of every instance, batched over per-instance loop
+    err = extras.pop("max_rel_err_vs_oracle", None)
+    bop = value / world / plain_value if plain_value == plain_value else None
+    single = extras.get("single_instance_forward") or {}
+    gates = {"max_rel_err_vs_oracle": err, "err_tol": ERR_TOL,
+             "err_checked": ("every instance's G, dA, db, dc of the host-buffer step vs the C oracle"
+                             if err is not None else "not checked (--skip-cpu, or N > 1)"),
+             "batched_over_plain": bop, "batched_over_plain_min": MIN_BATCHED_OVER_PLAIN,
+             "single_instance_forward_ms": {k: v["ms"] for k, v in single.items()}}
+    failed = []
+    if err is not None and not err <= ERR_TOL:
+        failed.append(f"oracle error {err:.3e} > {ERR_TOL:g}")
+    if bop is not None and not bop >= MIN_BATCHED_OVER_PLAIN:
+        failed.append(f"batched/plain {bop:.2f} < {MIN_BATCHED_OVER_PLAIN:g}")
+    gates["pass"] = not failed
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": f"ragged batch: {len(shapes)} triples, D~U{{1..4}}, cutoff~U{{5..40}}, Takagi A "
-                                   "s~U(0,0.8), b sigma 0.3, c=1, fwd+VJP (one CUDA graph replay per step)",
-                       "instances": len(shapes), "amplitudes": total,
-                       "l2": "inputs larger than L2 (G, dLdG ~4.4 GB each)",
-                       "parallelism": f"replicas x{world} (instances independent)"},
-            "e2e": {"value": total * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "gates": gates,
+            "config": workload_config(n_global, total_all, world),
+            "e2e": {"value": total_all / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": launches_per_step * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -339,21 +381,25 @@ def run_gb300(args, rank, local_rank, world):
                          "binding_pipe": "fp64",
                          "note": "the recurrence and its VJP are FP64 arithmetic on a part with 1/64-rate FP64: "
                                  "the FP64 pipe (fp64.frac, of the measured DFMA peak) binds, not HBM"},
-            "kernels_ms": {"forward": t_fwd, "vjp": t_vjp},
-            "plain_loop": {"value": plain_value, "unit": UNIT, "sample": "256 instances, device_fwd + device_vjp per "
-                           "instance", "batched_over_plain": value / world / plain_value},
-            "max_rel_err_vs_oracle": None,
             "clocks": clocks,
+            "step": "one CUDA graph replay (ragged forward + VJP of this rank's instances)",
+            "kernels_ms": {"forward": t_fwd, "vjp": t_vjp},
+            "plain_loop": {"value": plain_value, "unit": UNIT,
+                           "sample": "256 instances drawn uniformly without replacement (numpy seed 11), "
+                                     "device_fwd + device_vjp per instance", "batched_over_plain": bop},
             "schedule": ({k: tuned[k] for k in ("team_min_amps", "team_cluster", "vjp_item_amps")}
                          if tuned else "plan defaults"),
         }
-        line.update(extras)
         if cpu is not None:
+            cpu["max_rel_err_vs_oracle"] = err
             line["cpu_baseline"] = cpu
+        line.update(extras)
         print(json.dumps(line), flush=True)
+        if failed:
+            print("bench gates failed: " + "; ".join(failed), file=sys.stderr, flush=True)
     if pg is not None:
         pg.destroy_process_group()
-    return 0
+    return 1 if failed else 0
 
 
 def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs, cs, time_eager, dfma_peak):
@@ -397,6 +443,10 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
         e2e_modes[name] = e0.elapsed_time(e1) / e2e_steps
     e2e_mode = min(e2e_modes, key=e2e_modes.get)
     e2e_ms = e2e_modes[e2e_mode]
+    if world > 1:  # the slowest rank's step, as for the device-timed value
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
     rb.ws.check_status("e2e")
 
     # --- plain per-instance GPU path on a sample of instances (scaled to amplitudes/s)
@@ -807,12 +857,18 @@ def run_plain_and_gradient(dev, time_eager, with_cpu=True):
                         torch.randn(shape, generator=gen, device=dev, dtype=torch.float64))
 
     def step():
+        # gradients set to None every step (as a training loop's zero_grad does): accumulating into
+        # .grad would make the first accumulating step launch torch's complex add kernel, whose
+        # module CUDA loads lazily on first use (~0.75 s from a cold page cache on a fresh box)
+        for x in (At, bt, ct):
+            x.grad = None
         G = mm.hermite_renormalized_autograd(At, bt, ct, shape)
         G.backward(gup)
 
     def wall_ms(fn, reps):
         # autograd runs the backward on its own thread: time with a host clock between synchronisations
-        fn()
+        for _ in range(3):
+            fn()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for _ in range(reps):
@@ -820,10 +876,35 @@ def run_plain_and_gradient(dev, time_eager, with_cpu=True):
         torch.cuda.synchronize(dev)
         return (time.perf_counter() - t0) / reps * 1e3
 
+    def per_rep(fn, reps):
+        """Per-rep host time (synchronised each rep) and device time by CUDA events on the stream
+        both the forward and autograd's backward run on (the current stream when the forward ran)."""
+        stream = torch.cuda.current_stream(dev)
+        host, devt = [], []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            host.append((time.perf_counter() - t0) * 1e3)
+            devt.append(e0.elapsed_time(e1))
+
+        def dist(a):
+            a = np.asarray(a)
+            return {"median": float(np.median(a)), "p10": float(np.percentile(a, 10)),
+                    "p90": float(np.percentile(a, 90)), "max": float(a.max()), "mean": float(a.mean())}
+
+        return {"reps": reps, "host_ms": dist(host), "device_ms": dist(devt)}
+
     with mm.settings(CHECK_DEVICE_STATUS=False):
-        t = wall_ms(step, reps=20)
+        t = wall_ms(step, reps=50)
+        reps = per_rep(step, 60)
     r = {"shape": list(shape), "amplitudes": 30 ** 4, "ms_fwd_bwd": t, "amplitudes_per_s": 30 ** 4 / (t * 1e-3),
-         "timing": "host clock between device synchronisations"}
+         "timing": "host clock over 50 back-to-back steps after 3 warm-up steps; per_rep: 60 synchronised steps",
+         "per_rep": reps}
     if with_cpu:
         import oracle
 
@@ -834,6 +915,22 @@ def run_plain_and_gradient(dev, time_eager, with_cpu=True):
         r["cpu_baseline"] = {"value": tc * 1e3, "unit": "ms", "cores": 1, "kind": "port",
                              "sample": "forward + VJP of the same triple, one pass"}
     res["autograd_4x30"] = r
+    # the same step with a checkpointed backward (residual: checkpoint slabs instead of G)
+    ck_rows = {}
+    for K in (5, 10):
+        def step_ck(K=K):
+            for x in (At, bt, ct):
+                x.grad = None
+            G = mm.hermite_renormalized_autograd(At, bt, ct, shape, checkpoint=K)
+            G.backward(gup)
+
+        with mm.settings(CHECK_DEVICE_STATUS=False):
+            t_ck = wall_ms(step_ck, reps=50)
+        resid = mm.checkpoint_elems(shape, K) * 16
+        ck_rows[f"K{K}"] = {"ms_fwd_bwd": t_ck, "residual_bytes": resid, "residual_frac_of_G": resid / (16 * 30 ** 4)}
+    res["autograd_4x30_checkpointed"] = {"shape": list(shape), "full_G_residual_bytes": 16 * 30 ** 4,
+                                         "segments": ck_rows,
+                                         "timing": "host clock over 50 back-to-back steps after 3 warm-up steps"}
     # 64-instance batched fidelity gradient step
     B = 64
     trip = [takagi(4, 0.8, 7300 + k) for k in range(B)]
@@ -853,7 +950,7 @@ def run_plain_and_gradient(dev, time_eager, with_cpu=True):
         loss.backward()
 
     with mm.settings(CHECK_DEVICE_STATUS=False):
-        t = wall_ms(fid_step, reps=5)
+        t = wall_ms(fid_step, reps=10)
     res["fidelity_step_64x4x30"] = {"instances": B, "shape": list(shape), "amplitudes": B * 30 ** 4,
                                     "ms_per_step": t, "amplitudes_per_s": B * 30 ** 4 / (t * 1e-3),
                                     "note": "forward, fidelity loss (torch reductions), backward; host clock between "

@@ -47,7 +47,8 @@ enum mm_status {
   MM_OK = 0,
   MM_ERR_INVALID_ARG = 1,   /* bad pointer, shape entry < 1, D < 1, ... */
   MM_ERR_UNSUPPORTED = 2,   /* D > mm_max_modes() */
-  MM_ERR_TOO_LARGE = 3,     /* a slab of the recurrence exceeds 2^31 - 1 amplitudes */
+  MM_ERR_TOO_LARGE = 3,     /* a slab of the recurrence exceeds 2^31 - 1 amplitudes, or (only from
+                               mm_hermite_vjp_noalloc) its scratch exceeds MM_NOALLOC_SCRATCH_BYTES */
   MM_ERR_CUDA = 4,          /* a CUDA runtime call failed */
   MM_ERR_WAIT_TIMEOUT = 5,  /* a bounded inter-CTA wait gave up (device status word) */
   MM_ERR_WORKSPACE = 6,     /* workspace missing, misaligned or too small */
@@ -128,23 +129,56 @@ MM_API int mm_hermite_vjp_batched(int64_t B, int D, const int64_t *shape, const 
                            mm_stream_t stream);
 
 /*
+ * Checkpointed VJP: vanilla_vjp_numba(G, c, dLdG) without G.  The JAX custom VJP keeps the
+ * whole tensor G as its residual (mrmustard/math/jax_vjps/hermite.py:80-81); here the forward
+ * keeps only checkpoint slabs along axis 0 and the backward recomputes the rest, segment by
+ * segment, before running the stencil of gradients.py:25-82 on it.
+ *  - Segments of K >= 2 slabs (slab m = every amplitude with k_0 = m, strides[0] of them);
+ *    the checkpoint buffer holds slab 0, then slabs jK - 2 and jK - 1 for j = 1 .. nseg - 1
+ *    (nseg = ceil(shape[0] / K)): mm_hermite_checkpoint_elems(D, shape, K) complex values,
+ *    about 2 / K of G.
+ *  - mm_hermite_checkpoint_save copies those slabs out of a forward's G (device to device).
+ *  - mm_hermite_vjp_checkpointed takes A, b, c (for the recomputation), the checkpoints and
+ *    the full cotangent; its workspace (mm_hermite_vjp_checkpointed_workspace_bytes) holds
+ *    a window of K + 2 slabs, never all of G.  Vanilla recurrence only.
+ * Results equal mm_hermite_vjp on the forward's G to rounding (the recomputed slabs follow
+ * the forward's terms; the per-fiber sums are split at segment boundaries).
+ * mm_hermite_checkpoint_elems returns -1 for a bad shape or K < 2.
+ */
+MM_API int64_t mm_hermite_checkpoint_elems(int D, const int64_t *shape, int K);
+MM_API int mm_hermite_checkpoint_save(int D, const int64_t *shape, int K, const mm_c128 *G, mm_c128 *ckpt,
+                                      mm_stream_t stream);
+MM_API size_t mm_hermite_vjp_checkpointed_workspace_bytes(int D, const int64_t *shape, int K);
+MM_API int mm_hermite_vjp_checkpointed(int D, const int64_t *shape, int K, const mm_c128 *A, const mm_c128 *b,
+                                       const mm_c128 *c, const mm_c128 *ckpt, const mm_c128 *dLdG, mm_c128 *dA,
+                                       mm_c128 *db, mm_c128 *dc, void *ws, size_t ws_bytes, mm_stream_t stream);
+
+/*
  * mm_hermite_vjp without a workspace argument: the same kernels and results,
  * for callers that cannot allocate device memory when they call (for example a
  * custom-call handler inside another framework's runtime, which owns all
  * device memory and the stream, so a cudaMalloc there would synchronise the
  * device or escape the framework's memory accounting).  No counterpart in the
  * reference.
- *  - Scratch is a 2 MiB array in the library's device memory, held by every
- *    GPU that loads the library until the process exits; shapes whose scratch
- *    (sqrt tables + per-work-item partial sums) does not fit return
- *    MM_ERR_TOO_LARGE.  Nothing is allocated by the call.
+ *  - Scratch is an array of MM_NOALLOC_SCRATCH_BYTES (2 MiB) in the library's
+ *    device memory, held by every GPU that loads the library until the process
+ *    exits; shapes whose scratch (512-byte header, three sqrt tables of
+ *    max(shape) + 1 doubles, 720 bytes of partial sums per work item) does not
+ *    fit return MM_ERR_TOO_LARGE, which mm_hermite_vjp with a workspace would
+ *    not.  Sufficient test before calling:
+ *    mm_hermite_workspace_bytes(D, shape, 1) <= MM_NOALLOC_SCRATCH_BYTES.
+ *    Nothing is allocated by the call.  Every argument is checked before the
+ *    array is touched, so a rejected call changes nothing on the device.
  *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress, with that device current); make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress, with that device current) and keeps it for the
+ *    life of the process; make that first call before any stream capture.
+ *    cudaDeviceReset ends the context that address belongs to: do not call
+ *    this entry point on a device after resetting it.
  *  - Every call uses the same array, so calls whose work overlaps on the GPU
  *    (other streams, other host threads) race: issue them in order on one
  *    stream.  The status word of the array is zeroed by each call.
  */
+#define MM_NOALLOC_SCRATCH_BYTES (2u << 20)
 MM_API int mm_hermite_vjp_noalloc(int D, const int64_t *shape, const mm_c128 *G, const mm_c128 *c,
                                   const mm_c128 *dLdG, mm_c128 *dA, mm_c128 *db, mm_c128 *dc, mm_stream_t stream);
 

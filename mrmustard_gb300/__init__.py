@@ -33,6 +33,9 @@ from .fock import apply_unitary, fock_gemm
 from .hermite import (
     device_fwd,
     device_vjp,
+    checkpoint_elems,
+    device_checkpoint_save,
+    device_vjp_checkpointed,
     hermite_renormalized,
     hermite_renormalized_batched,
     stable,
@@ -46,7 +49,7 @@ from .hermite import (
     vanilla_vjp,
     vanilla_vjp_numba,
 )
-from .ragged import RaggedBatch
+from .ragged import RaggedBatch, plan_offsets
 from .settings import settings
 
 __version__ = "0.1.0"
@@ -84,6 +87,10 @@ __all__ = [
     "fock_gemm",
     "device_fwd",
     "device_vjp",
+    "checkpoint_elems",
+    "device_checkpoint_save",
+    "device_vjp_checkpointed",
+    "plan_offsets",
     "hermite_renormalized",
     "hermite_renormalized_autograd",
     "hermite_renormalized_batched",

@@ -45,6 +45,10 @@ SIGNATURES = {
     "mm_hermite_vjp": (I32, [I32, P, P, P, P, P, P, P, P, SZ, P]),
     "mm_hermite_vjp_batched": (I32, [I64, I32, P, P, P, P, P, P, P, P, SZ, P]),
     "mm_hermite_vjp_noalloc": (I32, [I32, P, P, P, P, P, P, P, P]),
+    "mm_hermite_checkpoint_elems": (I64, [I32, P, I32]),
+    "mm_hermite_checkpoint_save": (I32, [I32, P, I32, P, P, P]),
+    "mm_hermite_vjp_checkpointed_workspace_bytes": (SZ, [I32, P, I32]),
+    "mm_hermite_vjp_checkpointed": (I32, [I32, P, I32, P, P, P, P, P, P, P, P, P, SZ, P]),
     "mm_ragged_plan_create": (I32, [I64, P, P, ctypes.POINTER(P)]),
     "mm_ragged_plan_destroy": (None, [P]),
     "mm_ragged_plan_workspace_bytes": (SZ, [P]),

@@ -1173,10 +1173,131 @@ int mm_ragged_vjp_copy_g(const mm_ragged_plan* plan, const mm_c128* G, const mm_
   return launch_vjp_reduce(src, plan->B, partials, (double2*)dA, (double2*)db, (double2*)dc, st);
 }
 
+// ------------------------------------------------------------ checkpointed VJP
+}  // extern "C"
+namespace {
+// Segments of kseg slabs along axis 0; checkpoint buffer = slab 0, then the two
+// slabs before each later segment (s - 2, s - 1 for s = j * kseg).
+struct CkptPlan {
+  UniformPlan P;
+  int kseg = 0;
+  int64_t nseg = 0;
+  size_t win = 0, total = 0;
+};
+
+int plan_ckpt(int D, const int64_t* shape, int kseg, int sms, CkptPlan& cp) {
+  if (kseg < 2) return MM_ERR_INVALID_ARG;
+  int rc = plan_uniform(1, D, shape, cp.P, sms, false);
+  if (rc) return rc;
+  const Geom& g = cp.P.g;
+  cp.kseg = kseg;
+  cp.nseg = (g.shape[0] + kseg - 1) / kseg;
+  cp.P.L = make_layout(g.maxC + 1, coef_entries(g), cp.nseg * cp.P.items_per_inst, 0, 0, 0);
+  cp.win = cp.P.L.total;
+  const int64_t slabs = std::min<int64_t>(kseg, g.shape[0]) + 2;
+  cp.total = align_up(cp.win + (size_t)slabs * (size_t)g.strides[0] * sizeof(double2));
+  return MM_OK;
+}
+
+int64_t ckpt_slabs(int64_t C0, int kseg) { return 1 + 2 * (((C0 + kseg - 1) / kseg) - 1); }
+
+template <int D>
+int launch_ckpt_segments(const CkptPlan& cp, const UniformSrc& src, char* w, const double2* ckpt, double2* dA,
+                         double2* db, double2* dc, cudaStream_t st) {
+  const Geom& g = cp.P.g;
+  const int64_t s0 = g.strides[0], C0 = g.shape[0];
+  double2* W = reinterpret_cast<double2*>(w + cp.win);
+  const Tables T = tables_of(w, cp.P.L);
+  double2* partials = reinterpret_cast<double2*>(w + cp.P.L.partials);
+  const int64_t items = cp.P.items_per_inst;
+  UniformSrc ws = src;
+  ws.G = W;
+  const unsigned nb = (unsigned)((s0 + 255) / 256);
+  for (int64_t j = 0; j < cp.nseg; ++j) {
+    const int s = (int)(j * cp.kseg), e = (int)std::min<int64_t>(s + cp.kseg, C0);
+    const int wbase = j == 0 ? 0 : s - 2;
+    const double2* from = j == 0 ? ckpt : ckpt + s0 + 2 * (j - 1) * s0;
+    MM_CUDA(cudaMemcpyAsync(W, from, (size_t)(j == 0 ? 1 : 2) * s0 * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    for (int m = j == 0 ? 1 : s; m < e; ++m) {
+      fwd_slab_kernel<D><<<nb, 256, 0, st>>>(g, src.b, src.coef, T.rs, W, m, wbase);
+      MM_LAUNCHED();
+    }
+    vjp_window_kernel<D><<<(unsigned)items, MM_BLOCK, 0, st>>>(ws, T, partials + j * items * MM_NV_MAX, s, e, wbase);
+    MM_LAUNCHED();
+  }
+  UniformSrc rs = src;
+  rs.items_per_inst = cp.nseg * items;
+  return launch_vjp_reduce(rs, 1, partials, dA, db, dc, st);
+}
+}  // namespace
+extern "C" {
+
+int64_t mm_hermite_checkpoint_elems(int D, const int64_t* shape, int kseg) {
+  Geom g;
+  if (kseg < 2 || make_geom(D, shape, g)) return -1;
+  return ckpt_slabs(g.shape[0], kseg) * g.strides[0];
+}
+
+int mm_hermite_checkpoint_save(int D, const int64_t* shape, int kseg, const mm_c128* G, mm_c128* ckpt,
+                               mm_stream_t stream) {
+  Geom g;
+  int rc = make_geom(D, shape, g);
+  if (rc) return rc;
+  if (kseg < 2 || !G || !ckpt) return MM_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t s0 = g.strides[0], nseg = (g.shape[0] + kseg - 1) / kseg;
+  const size_t slab = (size_t)s0 * sizeof(mm_c128);
+  MM_CUDA(cudaMemcpyAsync(ckpt, G, slab, cudaMemcpyDeviceToDevice, st));
+  for (int64_t j = 1; j < nseg; ++j)
+    MM_CUDA(cudaMemcpyAsync(ckpt + s0 + 2 * (j - 1) * s0, G + (j * kseg - 2) * s0, 2 * slab, cudaMemcpyDeviceToDevice,
+                            st));
+  return MM_OK;
+}
+
+size_t mm_hermite_vjp_checkpointed_workspace_bytes(int D, const int64_t* shape, int kseg) {
+  DevInfo di;
+  int sms = device_info(di) == MM_OK ? di.sms : 152;
+  CkptPlan cp;
+  if (plan_ckpt(D, shape, kseg, sms, cp)) return 0;
+  return cp.total;
+}
+
+int mm_hermite_vjp_checkpointed(int D, const int64_t* shape, int kseg, const mm_c128* A, const mm_c128* b,
+                                const mm_c128* c, const mm_c128* ckpt, const mm_c128* dLdG, mm_c128* dA, mm_c128* db,
+                                mm_c128* dc, void* ws, size_t ws_bytes, mm_stream_t stream) {
+  DevInfo di;
+  int rc = device_info(di);
+  if (rc) return rc;
+  CkptPlan cp;
+  if ((rc = plan_ckpt(D, shape, kseg, di.sms, cp))) return rc;
+  if (!A || !b || !c || !ckpt || !dLdG || !dA || !db || !dc) return MM_ERR_INVALID_ARG;
+  if ((rc = check_ws(ws, ws_bytes, cp.total))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = static_cast<char*>(ws);
+  UniformSrc src = uniform_src(cp.P, (const double2*)A, (const double2*)b, (const double2*)c, nullptr,
+                               (const double2*)dLdG, w);
+  if ((rc = reset_launch_state(w, st))) return rc;
+  if ((rc = launch_setup(src, 1, w, cp.P.L, 1, st))) return rc;
+  double2 *oA = (double2*)dA, *ob = (double2*)db, *oc = (double2*)dc;
+  const double2* ck = (const double2*)ckpt;
+  int r2 = MM_ERR_UNSUPPORTED;
+  switch (D) {
+    case 1: r2 = launch_ckpt_segments<1>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 2: r2 = launch_ckpt_segments<2>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 3: r2 = launch_ckpt_segments<3>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 4: r2 = launch_ckpt_segments<4>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 5: r2 = launch_ckpt_segments<5>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 6: r2 = launch_ckpt_segments<6>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 7: r2 = launch_ckpt_segments<7>(cp, src, w, ck, oA, ob, oc, st); break;
+    case 8: r2 = launch_ckpt_segments<8>(cp, src, w, ck, oA, ob, oc, st); break;
+  }
+  return r2;
+}
+
 // ------------------------------------------------------- VJP without a workspace
-// Scratch of mm_hermite_vjp_noalloc: 2 MiB of device memory in this library's
-// module, present on every GPU that loads the library until the process exits.
-#define MM_NOALLOC_SCRATCH_BYTES (2u << 20)
+// Scratch of mm_hermite_vjp_noalloc: MM_NOALLOC_SCRATCH_BYTES (2 MiB, include/mm_gb300.h)
+// of device memory in this library's module, present on every GPU that loads the
+// library until the process exits.
 static __device__ __align__(256) unsigned char g_vjp_scratch[MM_NOALLOC_SCRATCH_BYTES];
 
 // Device address of g_vjp_scratch for the current device, looked up once per
@@ -1205,6 +1326,9 @@ int mm_hermite_vjp_noalloc(int D, const int64_t* shape, const mm_c128* G, const 
   UniformPlan P;
   if ((rc = plan_uniform(1, D, shape, P, di.sms, false))) return rc;
   if (P.L.total > MM_NOALLOC_SCRATCH_BYTES) return MM_ERR_TOO_LARGE;
+  // every argument is checked before the shared array is touched: a rejected call has no
+  // effect on the device (it cannot disturb a call still running on another stream)
+  if (!G || !c || !dLdG || !dA || !db || !dc) return MM_ERR_INVALID_ARG;
   void* ws = nullptr;
   if ((rc = noalloc_scratch(&ws))) return rc;
   // the status word is the only scratch content read before it is written

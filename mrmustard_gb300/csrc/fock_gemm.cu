@@ -82,8 +82,6 @@ __global__ void __launch_bounds__(256) zgemm_fp64_kernel(const double2* __restri
 // ---------------------------------------------------------------- Ozaki split
 constexpr int OZ_BETA = 6;       // bits per slice
 constexpr int OZ_MAX_SLICES = 9;  // 54 bits
-constexpr int OZ_FLUSH = 4096;    // exact FP32 accumulation length for |s| <= 63
-constexpr int OZ_BM = 64, OZ_BN = 32, OZ_BK = 32, OZ_PAD = 8;
 constexpr int OZ_KALIGN = 64;     // Kp: K padded to a multiple of this (zeros)
 
 // x = (-1)^neg * mant * 2^ex with mant < 2^53; returns the exponent bound E(x)
@@ -186,142 +184,10 @@ __global__ void __launch_bounds__(256) split_x_kernel(const double2* __restrict_
   slice_value(v.y, Fc, S, Xs + plane + idx, 2 * plane);
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
 __device__ __forceinline__ double pow2(int e) {
   if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
   return ldexp(1.0, e);
 }
-
-// One CTA: a 64 x 32 tile of Y, 4 warps each 32 x 16 (2 x 2 mma tiles of 16 x 8).
-// Per slice-order group d, all pairs (p, q = d - p) accumulate into int64 sums;
-// the group is then added to Y in FP64 (the first group stores).
-__global__ void __launch_bounds__(128) ozaki_mma_kernel(const __nv_bfloat16* __restrict__ Us,
-                                                        const __nv_bfloat16* __restrict__ Xs,
-                                                        const int* __restrict__ E, const int* __restrict__ F,
-                                                        double2* __restrict__ Y, int M, int N, int Kp, int S) {
-  __shared__ __align__(16) __nv_bfloat16 As[2][OZ_BM][OZ_BK + OZ_PAD];  // [comp][row][k]
-  __shared__ __align__(16) __nv_bfloat16 Bs[2][OZ_BN][OZ_BK + OZ_PAD];  // [comp][col][k]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 16;
-  const int m0 = blockIdx.y * OZ_BM, n0 = blockIdx.x * OZ_BN;
-  const int64_t uplane = (int64_t)M * Kp, xplane = (int64_t)N * Kp;
-
-  for (int d = 2; d <= S + 1; ++d) {
-    long long Tre[16], Tim[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) Tre[i] = Tim[i] = 0;
-    const int plo = d - S > 1 ? d - S : 1, phi = d - 1 < S ? d - 1 : S;
-    for (int p = plo; p <= phi; ++p) {
-      const int q = d - p;
-      const __nv_bfloat16* Up = Us + (int64_t)(p - 1) * 2 * uplane;
-      const __nv_bfloat16* Xq = Xs + (int64_t)(q - 1) * 2 * xplane;
-      float rr[16], ii[16], ri[16], ir[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) rr[i] = ii[i] = ri[i] = ir[i] = 0.f;
-      for (int k0 = 0; k0 < Kp; k0 += OZ_BK) {
-        // A: 2 comps x 64 rows x 32 k = 512 x 16-byte chunks; B: 2 x 32 x 32 = 256 chunks
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const int ch = tid + r * 128;
-          const int comp = ch >> 8, row = (ch >> 2) & 63, kc = (ch & 3) * 8;
-          const int gm = m0 + row;
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (gm < M) v = __ldg(reinterpret_cast<const uint4*>(Up + comp * uplane + (int64_t)gm * Kp + k0 + kc));
-          *reinterpret_cast<uint4*>(&As[comp][row][kc]) = v;
-        }
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const int ch = tid + r * 128;
-          const int comp = ch >> 7, col = (ch >> 2) & 31, kc = (ch & 3) * 8;
-          const int gn = n0 + col;
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (gn < N) v = __ldg(reinterpret_cast<const uint4*>(Xq + comp * xplane + (int64_t)gn * Kp + k0 + kc));
-          *reinterpret_cast<uint4*>(&Bs[comp][col][kc]) = v;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < OZ_BK; kk += 16) {
-          uint32_t a[2][2][4], b[2][2][2];  // [comp][mtile][reg], [comp][ntile][reg]
-#pragma unroll
-          for (int c = 0; c < 2; ++c) {
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-              const int r0 = wm + mt * 16 + g;
-              a[c][mt][0] = *reinterpret_cast<const uint32_t*>(&As[c][r0][kk + t * 2]);
-              a[c][mt][1] = *reinterpret_cast<const uint32_t*>(&As[c][r0 + 8][kk + t * 2]);
-              a[c][mt][2] = *reinterpret_cast<const uint32_t*>(&As[c][r0][kk + 8 + t * 2]);
-              a[c][mt][3] = *reinterpret_cast<const uint32_t*>(&As[c][r0 + 8][kk + 8 + t * 2]);
-            }
-#pragma unroll
-            for (int nt = 0; nt < 2; ++nt) {
-              const int c0 = wn + nt * 8 + g;
-              b[c][nt][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][c0][kk + t * 2]);
-              b[c][nt][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][c0][kk + 8 + t * 2]);
-            }
-          }
-#pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-            for (int nt = 0; nt < 2; ++nt) {
-              float* prr = rr + (mt * 2 + nt) * 4;
-              float* pii = ii + (mt * 2 + nt) * 4;
-              float* pri = ri + (mt * 2 + nt) * 4;
-              float* pir = ir + (mt * 2 + nt) * 4;
-              mma_bf16(*reinterpret_cast<float(*)[4]>(prr), a[0][mt], b[0][nt]);
-              mma_bf16(*reinterpret_cast<float(*)[4]>(pii), a[1][mt], b[1][nt]);
-              mma_bf16(*reinterpret_cast<float(*)[4]>(pri), a[0][mt], b[1][nt]);
-              mma_bf16(*reinterpret_cast<float(*)[4]>(pir), a[1][mt], b[0][nt]);
-            }
-        }
-        __syncthreads();
-        const int kdone = k0 + OZ_BK;
-        if ((kdone % OZ_FLUSH) == 0 || kdone >= Kp) {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            Tre[i] += (long long)rr[i] - (long long)ii[i];
-            Tim[i] += (long long)ri[i] + (long long)ir[i];
-            rr[i] = ii[i] = ri[i] = ir[i] = 0.f;
-          }
-        }
-      }
-    }
-    // add group d in FP64
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int gm = m0 + wm + mt * 16 + g + (h >> 1) * 8;
-          const int gn = n0 + wn + nt * 8 + t * 2 + (h & 1);
-          if (gm < M && gn < N) {
-            const int i = (mt * 2 + nt) * 4 + h;
-            const int er = E[gm], fc = F[gn];
-            double2 y = cmk(0.0, 0.0);
-            if (er != INT32_MIN && fc != INT32_MIN) {
-              const double sc = pow2(er + fc - OZ_BETA * d);
-              y = cmk((double)Tre[i] * sc, (double)Tim[i] * sc);
-            }
-            double2* py = Y + (int64_t)gm * N + gn;
-            if (d == 2) {
-              *py = y;
-            } else {
-              const double2 o = *py;
-              *py = cmk(o.x + y.x, o.y + y.y);
-            }
-          }
-        }
-  }
-}
-
 
 // ---------------------------------------------------------------- tcgen05 path
 // Warp-specialised Blackwell kernel for the slice products.  One CTA owns a
@@ -763,15 +629,6 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int S) {
   L.total = off;
   return L;
 }
-// MM_OZAKI_LEGACY_MMA=1 selects the warp-level mma.sync kernel instead of tcgen05 (comparison only).
-bool mode_legacy_mma() {
-  static const bool v = [] {
-    const char* e = getenv("MM_OZAKI_LEGACY_MMA");
-    return e && e[0] == '1';
-  }();
-  return v;
-}
-
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -849,13 +706,6 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
       (const double2*)X, (int)K, (int)N, F);
   split_u_kernel<<<(unsigned)((M * Kp + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, Us);
   split_x_kernel<<<(unsigned)((N * Kp + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, Kp, slices, F, Xs);
-  if (mode_legacy_mma()) {
-    dim3 grid((unsigned)((N + OZ_BN - 1) / OZ_BN), (unsigned)((M + OZ_BM - 1) / OZ_BM));
-    if (grid.y > 65535) return MM_ERR_TOO_LARGE;
-    ozaki_mma_kernel<<<grid, 128, 0, st>>>(Us, Xs, E, F, (double2*)Y, (int)M, (int)N, Kp, slices);
-    mm::note_launches(5);
-    return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
-  }
   CUtensorMap tu, tx;
   if (!make_map(&tu, Us, (uint64_t)slices * 2 * M, (uint64_t)Kp, TC_BM) ||
       !make_map(&tx, Xs, (uint64_t)slices * 2 * N, (uint64_t)Kp, TC_NC))

@@ -1769,4 +1769,129 @@ __global__ void __launch_bounds__(128) vjp_reduce_kernel(Src src, const double2*
   }
 }
 
+// ============================================================== checkpointed VJP
+// Backward pass that never holds all of G (the forward keeps only checkpoint
+// slabs; reference: vanilla_vjp_numba, gradients.py:25-82, whose stencil
+// reads G only at u, u - 1_i, u - 1_i - 1_j, u - 2_i).  Slab m of level 0 (all
+// amplitudes with k_0 = m, a contiguous run of strides[0] amplitudes) depends
+// only on slabs m - 1 and m - 2, so segment [s, e) of slabs is recomputed into
+// a window buffer from the checkpointed slabs s - 2, s - 1 and the VJP stencil
+// then runs over the segment's slabs reading G from the window.
+//
+// Window: slot t holds slab wbase + t.  One launch per slab; one thread per
+// amplitude q of the slab; the arithmetic is fwd_chunk's at level 0.
+template <int D>
+__global__ void __launch_bounds__(256) fwd_slab_kernel(Geom g, const double2* __restrict__ b,
+                                                       const double2* __restrict__ coef,
+                                                       const double* __restrict__ rs, double2* __restrict__ W,
+                                                       int m, int wbase) {
+  const int64_t s0 = g.strides[0];
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= s0 || m < 1 || m - 1 < wbase) return;
+  const double2 b0 = __ldg(b);
+  const double2 cd = (m >= 2) ? __ldg(coef + g.prefC[0] + m) : cmk(0.0, 0.0);
+  const double rsm = rs[m];
+  const double2* Gp = W + (int64_t)(m - 1 - wbase) * s0;
+  int32_t k[D];
+  decompose<D>((uint32_t)q, 1, g, k);
+  double2 acc = cmul(b0, __ldcg(Gp + q));
+  if (m >= 2) acc = cfma(cd, __ldcg(Gp - s0 + q), acc);
+#pragma unroll
+  for (int j = 1; j < D; ++j)
+    if (k[j] > 0) acc = cfma(__ldg(coef + g.prefC[j] + k[j]), __ldcg(Gp + q - g.strides[j]), acc);
+  W[(int64_t)(m - wbase) * s0 + q] = cscale(rsm, acc);
+}
+
+// vjp_fibers over the slabs m in [m_lo, m_hi) only, G read from the window
+// (slab m at W + (m - wbase) * strides[0]); the cotangent is the full tensor.
+// Same terms and weights as vjp_fibers; per fiber the sum over m is split at the
+// segment boundaries, so results agree with the full-G VJP to rounding.
+template <int D>
+__device__ __forceinline__ void vjp_fibers_window(const InstView& v, const Tables& T, uint32_t q0, uint32_t q1,
+                                                  int m_lo, int m_hi, int wbase, double2 (&tot)[vjp_nv(D)]) {
+  constexpr int NV = vjp_nv(D);
+  const Geom& g = v.g;
+  const int64_t s0 = g.strides[0];
+  int64_t sj[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) sj[j] = g.strides[j];
+  const double2* __restrict__ G = v.G;  // the window
+  const double2* __restrict__ gb = v.dLdG;
+  const double* __restrict__ sq = T.sq;
+  const double* __restrict__ hh = T.hh;
+  for (uint32_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+    int32_t r[D];
+    decompose<D>(q, 1, g, r);
+    double2 a[NV];
+#pragma unroll
+    for (int s = 0; s < NV; ++s) a[s] = cmk(0.0, 0.0);
+    for (int m = m_lo; m < m_hi; ++m) {
+      const int64_t f = (int64_t)m * s0 + q;          // index in the full tensor (cotangent)
+      const int64_t w = (int64_t)(m - wbase) * s0 + q;  // index in the window
+      const double2 gu = __ldg(gb + f);
+      const double2 gf = __ldg(G + w);
+      a[0] = cfma(gf, gu, a[0]);
+      if (m >= 1) {
+        const double2 h0 = cscale(sq[m], gu);
+        a[1] = cfma(__ldg(G + w - s0), h0, a[1]);
+#pragma unroll
+        for (int j = 1; j < D; ++j)
+          if (r[j] >= 1) a[vjp_slot(D, 0, j)] = cfma(__ldg(G + w - s0 - sj[j]), h0, a[vjp_slot(D, 0, j)]);
+        if (m >= 2) {
+          const double2 h00 = cscale(hh[m], gu);
+          a[vjp_slot(D, 0, 0)] = cfma(__ldg(G + w - 2 * s0), h00, a[vjp_slot(D, 0, 0)]);
+        }
+      }
+#pragma unroll
+      for (int i = 1; i < D; ++i) {
+        if (r[i] >= 1) {
+          a[1 + i] = cfma(__ldg(G + w - sj[i]), gu, a[1 + i]);
+          if (r[i] >= 2) a[vjp_slot(D, i, i)] = cfma(__ldg(G + w - 2 * sj[i]), gu, a[vjp_slot(D, i, i)]);
+#pragma unroll
+          for (int j = i + 1; j < D; ++j)
+            if (r[j] >= 1) a[vjp_slot(D, i, j)] = cfma(__ldg(G + w - sj[i] - sj[j]), gu, a[vjp_slot(D, i, j)]);
+        }
+      }
+    }
+    tot[0] = cadd(tot[0], a[0]);
+    tot[1] = cadd(tot[1], a[1]);
+    tot[vjp_slot(D, 0, 0)] = cadd(tot[vjp_slot(D, 0, 0)], a[vjp_slot(D, 0, 0)]);
+#pragma unroll
+    for (int j = 1; j < D; ++j) tot[vjp_slot(D, 0, j)] = crfma(sq[r[j]], a[vjp_slot(D, 0, j)], tot[vjp_slot(D, 0, j)]);
+#pragma unroll
+    for (int i = 1; i < D; ++i) {
+      tot[1 + i] = crfma(sq[r[i]], a[1 + i], tot[1 + i]);
+      tot[vjp_slot(D, i, i)] = crfma(hh[r[i]], a[vjp_slot(D, i, i)], tot[vjp_slot(D, i, i)]);
+#pragma unroll
+      for (int j = i + 1; j < D; ++j)
+        tot[vjp_slot(D, i, j)] = crfma(sq[r[i]] * sq[r[j]], a[vjp_slot(D, i, j)], tot[vjp_slot(D, i, j)]);
+    }
+  }
+}
+
+// One CTA per work item of one segment (src: one instance, G = the window);
+// partial sums to partials[item * MM_NV_MAX + slot].
+template <int D>
+__global__ void __launch_bounds__(MM_BLOCK) vjp_window_kernel(UniformSrc src, Tables T, double2* __restrict__ partials,
+                                                              int m_lo, int m_hi, int wbase) {
+  MM_SHARED(InstView, sv);
+  MM_SHARED(uint32_t, sq0);
+  MM_SHARED(uint32_t, sq1);
+  const int64_t item = blockIdx.x;
+  if (threadIdx.x == 0) {
+    int64_t k;
+    uint32_t q0, q1;
+    src.item(item, k, q0, q1);
+    src.load(k, sv);
+    sq0 = q0;
+    sq1 = q1;
+  }
+  __syncthreads();
+  double2 tot[vjp_nv(D)];
+#pragma unroll
+  for (int s = 0; s < vjp_nv(D); ++s) tot[s] = cmk(0.0, 0.0);
+  vjp_fibers_window<D>(sv, T, sq0, sq1, m_lo, m_hi, wbase, tot);
+  block_reduce_write<vjp_nv(D)>(tot, partials + item * MM_NV_MAX);
+}
+
 }  // namespace mm

@@ -41,6 +41,9 @@ __all__ = [
     "hermite_renormalized_batched",
     "device_fwd",
     "device_vjp",
+    "checkpoint_elems",
+    "device_checkpoint_save",
+    "device_vjp_checkpointed",
 ]
 
 
@@ -192,6 +195,62 @@ def device_vjp(G: torch.Tensor, c: torch.Tensor, dLdG: torch.Tensor, batched: bo
                                 _stream())
     _lib.check(rc, "mm_hermite_vjp")
     _finish(ws, "hermite vjp")
+    return dA, db, dc
+
+
+def checkpoint_elems(shape, K: int) -> int:
+    """Complex values of the checkpoint buffer of one instance (mm_hermite_checkpoint_elems)."""
+    shape, sh = _shape_arr(shape)
+    n = int(_lib.load().mm_hermite_checkpoint_elems(len(shape), sh, int(K)))
+    if n < 0:
+        raise ValueError(f"checkpoint segments need K >= 2 and a valid shape (K={K}, shape={shape})")
+    return n
+
+
+def device_checkpoint_save(G: torch.Tensor, shape, K: int, batched: bool) -> torch.Tensor:
+    """Checkpoint slabs of a forward's G (slab 0, then the two slabs before every K-th slab
+    along axis 0): (checkpoint_elems,) or (B, checkpoint_elems) complex128 on G's device."""
+    lib = _lib.load()
+    G = raw(G)
+    shape, sh = _shape_arr(shape)
+    n = checkpoint_elems(shape, K)
+    B = G.shape[0] if batched else 1
+    ck = torch.empty(((B,) if batched else ()) + (n,), dtype=torch.complex128, device=G.device)
+    Gf, ckf = G.reshape(B, -1), ck.reshape(B, n)
+    for k in range(B):
+        _lib.check(lib.mm_hermite_checkpoint_save(len(shape), sh, int(K), _ptr(Gf[k]), _ptr(ckf[k]), _stream()),
+                   "mm_hermite_checkpoint_save")
+    return ck
+
+
+def device_vjp_checkpointed(A: torch.Tensor, b: torch.Tensor, c: torch.Tensor, ckpt: torch.Tensor,
+                            dLdG: torch.Tensor, shape, K: int, batched: bool):
+    """VJP from checkpoints (mm_hermite_vjp_checkpointed): G is recomputed K slabs at a time from
+    the checkpoint slabs and A, b; never held whole.  Returns (dA, db, dc) on the device."""
+    lib = _lib.load()
+    A, b, c, ckpt, dLdG = raw(A), raw(b), raw(c), raw(ckpt), raw(dLdG)
+    shape, sh = _shape_arr(shape)
+    D = len(shape)
+    B = A.shape[0] if batched else 1
+    dev = A.device
+    dA = torch.empty(((B,) if batched else ()) + (D, D), dtype=torch.complex128, device=dev)
+    db = torch.empty(((B,) if batched else ()) + (D,), dtype=torch.complex128, device=dev)
+    dc = torch.empty((B,) if batched else (), dtype=torch.complex128, device=dev)
+    if B == 0:
+        return dA, db, dc
+    nbytes = lib.mm_hermite_vjp_checkpointed_workspace_bytes(D, sh, int(K))
+    if nbytes == 0:
+        raise ValueError(f"checkpointed VJP: bad shape {shape} or K={K}")
+    ws = Workspace(nbytes, dev)
+    Af, bf, cf = A.reshape(B, D, D), b.reshape(B, D), c.reshape(B)
+    ckf, gf = ckpt.reshape(B, -1), dLdG.reshape(B, -1)
+    dAf, dbf, dcf = dA.reshape(B, D, D), db.reshape(B, D), dc.reshape(B)
+    for k in range(B):
+        _lib.check(lib.mm_hermite_vjp_checkpointed(D, sh, int(K), _ptr(Af[k]), _ptr(bf[k]), _ptr(cf[k:k + 1]),
+                                                   _ptr(ckf[k]), _ptr(gf[k]), _ptr(dAf[k]), _ptr(dbf[k]),
+                                                   _ptr(dcf[k:k + 1]), ws.ptr, ws.nbytes, _stream()),
+                   "mm_hermite_vjp_checkpointed")
+    _finish(ws, "checkpointed hermite vjp")
     return dA, db, dc
 
 

@@ -23,7 +23,27 @@ from . import _lib
 from .hermite import Workspace, _stream, raw, require_cuda
 from .settings import settings
 
-__all__ = ["RaggedBatch"]
+__all__ = ["RaggedBatch", "plan_offsets"]
+
+
+def plan_offsets(shapes):
+    """Host-side plan of a ragged set (no device needed): (g_off, a_off, b_off, total) of the flat
+    packing the library uses for these shapes, from mm_ragged_plan_offsets."""
+    lib = _lib.load()
+    shapes = [tuple(int(x) for x in s) for s in shapes]
+    B = len(shapes)
+    D = np.array([len(s) for s in shapes], np.int32)
+    flat = np.array([x for s in shapes for x in s] or [0], np.int64)
+    plan = ctypes.c_void_p()
+    _lib.check(lib.mm_ragged_plan_create(B, D.ctypes.data, flat.ctypes.data, ctypes.byref(plan)),
+               "mm_ragged_plan_create")
+    try:
+        offs = [np.zeros(B, np.int64) for _ in range(3)]
+        _lib.check(lib.mm_ragged_plan_offsets(plan, *(o.ctypes.data for o in offs)), "mm_ragged_plan_offsets")
+        total = int(lib.mm_ragged_plan_amplitudes(plan))
+    finally:
+        lib.mm_ragged_plan_destroy(plan)
+    return offs[0], offs[1], offs[2], total
 
 
 class RaggedBatch:
@@ -47,12 +67,31 @@ class RaggedBatch:
         _lib.check(lib.mm_ragged_plan_offsets(plan, self.g_off.ctypes.data, self.a_off.ctypes.data,
                                               self.b_off.ctypes.data), "mm_ragged_plan_offsets")
         self.sizes = np.array([int(np.prod(s)) for s in self.shapes], np.int64)
+        self.global_index = np.arange(self.B, dtype=np.int64)
         self.total = int(lib.mm_ragged_plan_amplitudes(plan))
         self.n_a = int((self.D.astype(np.int64) ** 2).sum())
         self.n_b = int(self.D.sum())
         self.tuning = {"team_min_amps": int(team_min_amps or 0), "vjp_item_amps": int(vjp_item_amps or 65536),
                        "team_cluster": 8}
         self._upload()
+
+    @classmethod
+    def shard(cls, shapes, rank: int, world: int, device=None, **tuning) -> "RaggedBatch":
+        """The share of rank `rank` (of `world`) of one ragged batch of `shapes`.
+
+        Instances are independent, so ranks split them with no collective: a greedy
+        longest-processing-time split of the per-instance cost (``shard.shard_instances``).
+        The returned batch holds this rank's instances in increasing global order;
+        ``global_index[k]`` is the position in `shapes` of its instance k."""
+        from .shard import instance_costs, shard_instances
+
+        shapes = [tuple(int(x) for x in s) for s in shapes]
+        if not 0 <= rank < max(world, 1):
+            raise ValueError(f"rank {rank} outside world size {world}")
+        local = shard_instances(instance_costs(shapes), world)[rank] if world > 1 else list(range(len(shapes)))
+        rb = cls([shapes[k] for k in local], device=device, **tuning)
+        rb.global_index = np.asarray(local, np.int64)
+        return rb
 
     def _upload(self):
         lib = _lib.load()

@@ -400,6 +400,35 @@ def test_ragged_graph_replay(cuda, oracle_lib):
         assert torch.equal(t, e)  # deterministic reductions: bitwise reproducible
 
 
+def test_ragged_shards_reproduce_unsharded_batch(cuda, oracle_lib):
+    """RaggedBatch.shard: the shares of 3 ranks (run one after the other on this GPU; no rank waits
+    on another) hold every instance once, and their G and gradients equal the unsharded batch's
+    instance by instance (the forward bit for bit; the VJP within tolerance of the oracle)."""
+    shapes, As, bs, cs = _ragged_case(90, 17, cmax=14)
+    full = mm.RaggedBatch(shapes)
+    A, b, c = full.pack(As, bs, cs)
+    g_full = torch.as_tensor(cn(full.total, 18), device=cuda)
+    G_full = full.forward(A, b, c)
+    Gs_full = full.unpack(G_full.cpu().numpy())
+    gs_full = full.unpack(g_full.cpu().numpy())
+    seen = []
+    for rank in range(3):
+        rb = mm.RaggedBatch.shard(shapes, rank, 3)
+        idx = list(rb.global_index)
+        seen += idx
+        Al, bl, cl = rb.pack([As[k] for k in idx], [bs[k] for k in idx], cs[idx])
+        gl = torch.as_tensor(np.concatenate([gs_full[k].ravel() for k in idx]), device=cuda)
+        Gl = rb.forward(Al, bl, cl)
+        dA, db, dc = rb.vjp(Gl, cl, gl)
+        dAs, dbs = rb.unpack_grads(dA.cpu().numpy(), db.cpu().numpy())
+        for j, (k, Gk) in enumerate(zip(idx, rb.unpack(Gl.cpu().numpy()))):
+            assert np.array_equal(Gk, Gs_full[k]), (rank, k)
+            rA, rbb, rc = oracle_lib.vjp(Gs_full[k], cs[k], gs_full[k])
+            assert rel(dAs[j], rA) < VJP_TOL and rel(dbs[j], rbb) < VJP_TOL, (rank, k)
+            assert abs(dc.cpu().numpy()[j] - rc) <= VJP_TOL * max(1.0, abs(rc))
+    assert sorted(seen) == list(range(len(shapes)))
+
+
 # ---------------------------------------------------------------- autograd
 def test_autograd_matches_finite_differences(cuda):
     A, b, _ = takagi(3, 0.7, 801)
