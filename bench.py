@@ -191,20 +191,20 @@ def run_reference(args, rank, world):
 
     # bounded sample: a fixed subset of instances (cost-weighted stride) so a step takes a few seconds
     t0 = time.perf_counter()
-    oracle.fwd_ragged(rh, A, b, cs, out=G)
-    oracle.vjp_ragged(rh, G, cs, g)
+    oracle.fwd_ragged(rh, A, b, cs, out=G, fast=True)
+    oracle.vjp_ragged(rh, G, cs, g, fast=True)
     full_s = time.perf_counter() - t0
     frac = min(1.0, 4.0 / full_s) if full_s > 0 else 1.0
     idx = rh.order[:: max(1, int(round(1 / frac)))] if frac < 1 else rh.order
     amps = int(rh.sizes[idx].sum())
     for _ in range(args.warmup):
-        oracle.fwd_ragged(rh, A, b, cs, out=G, indices=idx)
-        oracle.vjp_ragged(rh, G, cs, g, indices=idx)
+        oracle.fwd_ragged(rh, A, b, cs, out=G, indices=idx, fast=True)
+        oracle.vjp_ragged(rh, G, cs, g, indices=idx, fast=True)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.fwd_ragged(rh, A, b, cs, out=G, indices=idx)
-        oracle.vjp_ragged(rh, G, cs, g, indices=idx)
+        oracle.fwd_ragged(rh, A, b, cs, out=G, indices=idx, fast=True)
+        oracle.vjp_ragged(rh, G, cs, g, indices=idx, fast=True)
         times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
     value = amps / t
@@ -216,6 +216,7 @@ def run_reference(args, rank, world):
         "data": "synthetic", "impl": "reference",
         "config": workload_config(len(shapes), int(rh.total), world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                         "build": "gcc " + " ".join(oracle.FAST_FLAGS) + " -fopenmp (no -march flags)",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -476,15 +477,24 @@ def run_extras(args, rank, world, dev, rb, A, b, c, g, G, grads, shapes, As, bs,
         b_np = np.concatenate(bs)
         g_np = g_h.numpy()
         G_np = np.empty(total, np.complex128)
+        # timed: the speed build of the C port (-O3, FMA contraction, OpenMP over instances)
+        G_fast = np.empty(total, np.complex128)
+        t0 = time.perf_counter()
+        oracle.fwd_ragged(rh, A_np, b_np, cs, out=G_fast, fast=True)
+        oracle.vjp_ragged(rh, G_fast, cs, g_np, fast=True)
+        tc = time.perf_counter() - t0
+        del G_fast
+        # the checker build (-O2, no contraction: the parity oracle), also timed for reference
         t0 = time.perf_counter()
         oracle.fwd_ragged(rh, A_np, b_np, cs, out=G_np)
-        oracle.vjp_ragged(rh, G_np, cs, g_np)
-        tc = time.perf_counter() - t0
-        cpu = {"value": total / tc, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-               "sample": f"all {len(shapes)} instances ({total} amplitudes), one fwd+VJP pass, {tc:.2f} s"}
-        # the oracle as checker: every instance's G, dA, db, dc from the host-buffer step above
-        # against the oracle's, max over instances of max|x - ref| / max|ref|
         dA_o, db_o, dc_o = oracle.vjp_ragged(rh, G_np, cs, g_np)
+        tc_chk = time.perf_counter() - t0
+        cpu = {"value": total / tc, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+               "build": "gcc " + " ".join(oracle.FAST_FLAGS) + " -fopenmp (no -march flags)",
+               "sample": f"all {len(shapes)} instances ({total} amplitudes), one fwd+VJP pass, {tc:.2f} s",
+               "checker_build_value": total / tc_chk}
+        # the oracle as checker: every instance's G, dA, db, dc from the host-buffer step above
+        # against the checker build's, max over instances of max|x - ref| / max|ref|
         assert all(np.array_equal(x, y) for x, y in ((rb.g_off, rh.g_off), (rb.a_off, rh.a_off), (rb.b_off, rh.b_off)))
 
         def inst_err(x, ref, off):
@@ -838,12 +848,17 @@ def run_plain_and_gradient(dev, time_eager, with_cpu=True):
         import oracle
 
         G = mm.hermite_renormalized(A, b, 1.0 + 0j, shape)
-        t0 = time.perf_counter()
-        for _ in range(20):
-            ref = oracle.vanilla(shape, A, b, 1.0 + 0j)
-        tc = (time.perf_counter() - t0) / 20
-        r["cpu_baseline"] = {"value": tc * 1e6, "unit": "us per call", "cores": 1, "kind": "port",
-                             "sample": "the same call, 20 passes", "max_rel_err_vs_gpu": oracle.rel_err(G, ref)}
+        tcs = {}
+        for fast in (True, False):
+            oracle.vanilla(shape, A, b, 1.0 + 0j, fast=fast)
+            t0 = time.perf_counter()
+            for _ in range(50):
+                ref = oracle.vanilla(shape, A, b, 1.0 + 0j, fast=fast)
+            tcs[fast] = (time.perf_counter() - t0) / 50
+        r["cpu_baseline"] = {"value": tcs[True] * 1e6, "unit": "us per call", "cores": 1, "kind": "port",
+                             "build": "gcc " + " ".join(oracle.FAST_FLAGS), "checker_build_us": tcs[False] * 1e6,
+                             "sample": "the same call (numpy in, numpy out), 50 passes",
+                             "max_rel_err_vs_gpu": oracle.rel_err(G, ref)}
     res["plain_3x20"] = r
     # autograd 4 x 30
     A, b = takagi(4, 0.8, 7171)
@@ -908,12 +923,15 @@ def run_plain_and_gradient(dev, time_eager, with_cpu=True):
     if with_cpu:
         import oracle
 
+        gh = gup.cpu().numpy()
         t0 = time.perf_counter()
-        G = oracle.vanilla(shape, A, b, 1.0 + 0j)
-        oracle.vjp(G, 1.0 + 0j, gup.cpu().numpy())
-        tc = time.perf_counter() - t0
+        for _ in range(3):
+            G = oracle.vanilla(shape, A, b, 1.0 + 0j, fast=True)
+            oracle.vjp(G, 1.0 + 0j, gh, fast=True)
+        tc = (time.perf_counter() - t0) / 3
         r["cpu_baseline"] = {"value": tc * 1e3, "unit": "ms", "cores": 1, "kind": "port",
-                             "sample": "forward + VJP of the same triple, one pass"}
+                             "build": "gcc " + " ".join(oracle.FAST_FLAGS),
+                             "sample": "forward + VJP of the same triple, 3 passes"}
     res["autograd_4x30"] = r
     # the same step with a checkpointed backward (residual: checkpoint slabs instead of G)
     ck_rows = {}
@@ -983,14 +1001,33 @@ def run_single(dev, time_eager, dfma_peak=None):
         out = torch.empty((cut,) * D, dtype=torch.complex128, device=dev)
         with mm.settings(CHECK_DEVICE_STATUS=False):
             t1 = time_eager(lambda: mm.device_fwd(At, bt, ct, (cut,) * D, out=out), reps=10)
+            t_st = time_eager(lambda: mm.device_fwd(At, bt, ct, (cut,) * D, stable=True, out=out), reps=5)
         n1 = cut ** D
         ops = fp64_ops((cut,) * D)[0]
+        ops_st = fp64_ops_stable((cut,) * D)
+        hbm_peak = measured_peaks()[0]
         r = {"amplitudes": n1, "ms": t1, "amplitudes_per_s": n1 / (t1 * 1e-3),
-             "hbm_gbs": 16.0 * n1 / (t1 * 1e-3) / 1e9, "fp64_instructions": ops}
+             "hbm_gbs": 16.0 * n1 / (t1 * 1e-3) / 1e9, "fp64_instructions": ops,
+             "stable": {"ms": t_st, "amplitudes_per_s": n1 / (t_st * 1e-3), "fp64_instructions": ops_st,
+                        "hbm_frac": 16.0 * n1 / (t_st * 1e-3) / 1e9 / hbm_peak}}
         if dfma_peak:
             r["fp64_frac"] = ops / (t1 * 1e-3) / dfma_peak
+            r["stable"]["fp64_frac"] = ops_st / (t_st * 1e-3) / dfma_peak
         single[name] = r
     return single
+
+
+def fp64_ops_stable(shape):
+    """FP64 pipe instructions of the stable forward (stable_wave) for one shape: per amplitude and
+    per pivot i (k_i > 0) b_i G (4), one complex FMA (4) per other non-zero axis and for k_i >= 2,
+    the scaled add into the average (2); then the 1/#pivots scale (2)."""
+    idx = np.indices(shape).reshape(len(shape), -1)
+    nz = (idx > 0).sum(0)
+    ops = 2.0 * (nz > 0).sum()
+    for i in range(len(shape)):
+        piv = idx[i] > 0
+        ops += float((piv * (6 + 4 * (nz - 1) + 4 * (idx[i] >= 2))).sum())
+    return ops
 
 
 def fp64_probe(dev, time_eager):

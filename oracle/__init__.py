@@ -32,8 +32,14 @@ SRC = HERE / "hermite_oracle.c"
 SOURCES = (SRC, HERE / "autoshape_oracle.c", HERE / "binomial_oracle.c", HERE / "diagonal_oracle.c")
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
+# the same recurrence and VJP source built for speed, used only as a timed CPU baseline:
+# -O3 with contraction to FMA and unrolling (no -march flags: the box's baseline aarch64 ISA
+# already has FMA and NEON), never as the parity checker
+FAST_LIB_PATH = BUILD_DIR / "liboracle_fast.so"
+FAST_FLAGS = ["-O3", "-ffp-contract=fast", "-funroll-loops"]
 
 _lib = None
+_fast = None
 
 
 def build(force: bool = False) -> Path:
@@ -50,7 +56,44 @@ def build(force: bool = False) -> Path:
     except subprocess.CalledProcessError:
         subprocess.run(base + ["-o", str(tmp), "-lm"], check=True)
     os.replace(tmp, LIB_PATH)
+    build_fast(force)
     return LIB_PATH
+
+
+def build_fast(force: bool = False) -> Path:
+    """Compile ``hermite_oracle.c`` with FAST_FLAGS into ``oracle/_build/liboracle_fast.so``."""
+    BUILD_DIR.mkdir(exist_ok=True)
+    if FAST_LIB_PATH.exists() and not force and FAST_LIB_PATH.stat().st_mtime >= SRC.stat().st_mtime:
+        return FAST_LIB_PATH
+    base = ["gcc", *FAST_FLAGS, "-std=c11", "-fPIC", "-shared", str(SRC)]
+    tmp = BUILD_DIR / f"liboracle_fast.{os.getpid()}.so"
+    try:
+        subprocess.run(base + ["-fopenmp", "-o", str(tmp), "-lm"], check=True, capture_output=True)
+    except subprocess.CalledProcessError:
+        subprocess.run(base + ["-o", str(tmp), "-lm"], check=True)
+    os.replace(tmp, FAST_LIB_PATH)
+    return FAST_LIB_PATH
+
+
+def fast_lib():
+    """The speed build (timed baselines only)."""
+    global _fast
+    if _fast is None:
+        build_fast()
+        L = ctypes.CDLL(str(FAST_LIB_PATH))
+        P, I64, I32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+        for name, args in {
+            "oracle_vanilla": [I32, P, P, P, P, P],
+            "oracle_vjp": [I32, P, P, P, P, P, P, P],
+            "oracle_fwd_ragged": [I64, P, P, P, P, P, P, P, P, I32, P, P, P],
+            "oracle_vjp_ragged": [I64, P, P, P, P, P, P, P, P, P, P, P, P, P],
+        }.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L.oracle_num_threads.restype = ctypes.c_int
+        _fast = L
+    return _fast
 
 
 def lib():
@@ -117,13 +160,13 @@ def num_threads() -> int:
     return int(lib().oracle_num_threads())
 
 
-def vanilla(shape, A, b, c) -> np.ndarray:
-    """``vanilla_numba(shape, A, b, c)`` (core.py:25-124)."""
+def vanilla(shape, A, b, c, fast=False) -> np.ndarray:
+    """``vanilla_numba(shape, A, b, c)`` (core.py:25-124); ``fast``: the speed build."""
     shape = tuple(int(s) for s in shape)
     A, b = _cc(A), _cc(b)
     sh = np.array(shape, np.int64)
     G = np.empty(shape, np.complex128)
-    rc = lib().oracle_vanilla(len(shape), _ptr(sh), _ptr(A), _ptr(b), _c(c), _ptr(G))
+    rc = (fast_lib() if fast else lib()).oracle_vanilla(len(shape), _ptr(sh), _ptr(A), _ptr(b), _c(c), _ptr(G))
     if rc:
         raise ValueError(f"oracle_vanilla failed ({rc})")
     return G
@@ -141,15 +184,15 @@ def stable(shape, A, b, c) -> np.ndarray:
     return G
 
 
-def vjp(G, c, dLdG):
-    """``vanilla_vjp_numba(G, c, dLdG)`` (gradients.py:25-82) -> (dA, db, dc)."""
+def vjp(G, c, dLdG, fast=False):
+    """``vanilla_vjp_numba(G, c, dLdG)`` (gradients.py:25-82) -> (dA, db, dc); ``fast``: the speed build."""
     G, g = _cc(G), _cc(dLdG)
     D = G.ndim
     sh = np.array(G.shape, np.int64)
     dA = np.empty((D, D), np.complex128)
     db = np.empty(D, np.complex128)
     dc = np.empty(1, np.complex128)
-    rc = lib().oracle_vjp(D, _ptr(sh), _ptr(G), _c(c), _ptr(g), _ptr(dA), _ptr(db), _ptr(dc))
+    rc = (fast_lib() if fast else lib()).oracle_vjp(D, _ptr(sh), _ptr(G), _c(c), _ptr(g), _ptr(dA), _ptr(db), _ptr(dc))
     if rc:
         raise ValueError(f"oracle_vjp failed ({rc})")
     return dA, db, dc[0]
@@ -199,12 +242,13 @@ class RaggedHost:
         self.order = np.argsort(-self.sizes * (self.D + 1), kind="stable").astype(np.int64)
 
 
-def fwd_ragged(rh: RaggedHost, A, b, c, stable=False, out=None, indices=None):
-    """Per-instance loop of ``vanilla_numba`` over a packed ragged batch (OpenMP over instances)."""
+def fwd_ragged(rh: RaggedHost, A, b, c, stable=False, out=None, indices=None, fast=False):
+    """Per-instance loop of ``vanilla_numba`` over a packed ragged batch (OpenMP over instances).
+    ``fast``: run the speed build (timed baselines) instead of the checker build."""
     A, b, c = _cc(A), _cc(b), _cc(c)
     G = np.empty(rh.total, np.complex128) if out is None else out
     order = rh.order if indices is None else np.ascontiguousarray(indices, np.int64)
-    rc = lib().oracle_fwd_ragged(len(order), _ptr(rh.D), _ptr(rh.flat_shapes), _ptr(rh.shape_off), _ptr(A),
+    rc = (fast_lib() if fast else lib()).oracle_fwd_ragged(len(order), _ptr(rh.D), _ptr(rh.flat_shapes), _ptr(rh.shape_off), _ptr(A),
                                  _ptr(rh.a_off), _ptr(b), _ptr(rh.b_off), _ptr(c), int(bool(stable)), _ptr(G),
                                  _ptr(rh.g_off), _ptr(order))
     if rc:
@@ -212,14 +256,14 @@ def fwd_ragged(rh: RaggedHost, A, b, c, stable=False, out=None, indices=None):
     return G
 
 
-def vjp_ragged(rh: RaggedHost, G, c, dLdG, indices=None):
-    """Per-instance loop of ``vanilla_vjp_numba`` over a packed ragged batch."""
+def vjp_ragged(rh: RaggedHost, G, c, dLdG, indices=None, fast=False):
+    """Per-instance loop of ``vanilla_vjp_numba`` over a packed ragged batch (``fast``: speed build)."""
     G, c, g = _cc(G), _cc(c), _cc(dLdG)
     dA = np.zeros(int((rh.D.astype(np.int64) ** 2).sum()), np.complex128)
     db = np.zeros(int(rh.D.sum()), np.complex128)
     dc = np.zeros(rh.B, np.complex128)
     order = rh.order if indices is None else np.ascontiguousarray(indices, np.int64)
-    rc = lib().oracle_vjp_ragged(len(order), _ptr(rh.D), _ptr(rh.flat_shapes), _ptr(rh.shape_off), _ptr(G),
+    rc = (fast_lib() if fast else lib()).oracle_vjp_ragged(len(order), _ptr(rh.D), _ptr(rh.flat_shapes), _ptr(rh.shape_off), _ptr(G),
                                  _ptr(rh.g_off), _ptr(c), _ptr(g), _ptr(dA), _ptr(rh.a_off), _ptr(db),
                                  _ptr(rh.b_off), _ptr(dc), _ptr(order))
     if rc:
