@@ -1073,7 +1073,7 @@ def run_contraction(dev, time_eager):
     t_np = time.perf_counter() - t0
     flops = 8.0 * 2500 * 256 * 2500
     contraction = {"shape": "2500x2500 @ 2500x256 complex128", "flops": flops, "numpy_zgemm_ms": t_np * 1e3}
-    for mode in ("fp64", "ozaki"):
+    for mode in ("fp64", "dmma", "ozaki"):
         with mm.settings(CHECK_DEVICE_STATUS=False):
             tm = time_eager(lambda: mm.fock_gemm(U5, Xk, mode), reps=5)
         Y = mm.fock_gemm(U5, Xk, mode).cpu().numpy()

@@ -79,6 +79,113 @@ __global__ void __launch_bounds__(256) zgemm_fp64_kernel(const double2* __restri
     }
 }
 
+// ---------------------------------------------------------------- FP64 tensor-core path
+// The same product on the FP64 MMA instruction (mma.sync m8n8k4 .f64, the
+// tensor-core FP64 path; tcgen05 has no FP64 kind).  Complex operands are split
+// into real and imaginary planes in shared memory; per 8 x 8 output tile
+// Y_re += U_re X_re + (-U_im) X_im and Y_im += U_re X_im + U_im X_re, four
+// MMAs (256 FMAs each) per tile and k-step of 4.  CTA: 64 x 32 outputs, 4 warps
+// of 32 x 16 (4 x 2 tiles); the next K tile is fetched into registers while the
+// current one is multiplied.
+constexpr int DM_BM = 64, DM_BN = 32, DM_BK = 8, DM_PAD = 4;
+
+__device__ __forceinline__ void dmma_884(double& c0, double& c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+__device__ __forceinline__ double neg(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(128) zgemm_dmma_kernel(const double2* __restrict__ U, const double2* __restrict__ X,
+                                                         double2* __restrict__ Y, int M, int N, int K) {
+  __shared__ double Ar[DM_BK][DM_BM + DM_PAD], Ai[DM_BK][DM_BM + DM_PAD];  // [k][m]
+  __shared__ double Br[DM_BK][DM_BN + DM_PAD], Bi[DM_BK][DM_BN + DM_PAD];  // [k][n]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 16;
+  const int m0 = blockIdx.y * DM_BM, n0 = blockIdx.x * DM_BN;
+  double cr[4][2][2], ci[4][2][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) cr[i][j][0] = cr[i][j][1] = ci[i][j][0] = ci[i][j][1] = 0.0;
+  // global -> register staging: U tile 64 x 8 (4 per thread), X tile 8 x 32 (2 per thread)
+  double2 ru[4], rx[2];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * 128, row = idx >> 3, kk = idx & 7;
+      const int gm = m0 + row, gk = k0 + kk;
+      ru[r] = (gm < M && gk < K) ? __ldg(U + (int64_t)gm * K + gk) : cmk(0.0, 0.0);
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + r * 128, kk = idx >> 5, col = idx & 31;
+      const int gk = k0 + kk, gn = n0 + col;
+      rx[r] = (gk < K && gn < N) ? __ldg(X + (int64_t)gk * N + gn) : cmk(0.0, 0.0);
+    }
+  };
+  auto stash = [&]() {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * 128, row = idx >> 3, kk = idx & 7;
+      Ar[kk][row] = ru[r].x;
+      Ai[kk][row] = ru[r].y;
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + r * 128, kk = idx >> 5, col = idx & 31;
+      Br[kk][col] = rx[r].x;
+      Bi[kk][col] = rx[r].y;
+    }
+  };
+  fetch(0);
+  for (int k0 = 0; k0 < K; k0 += DM_BK) {
+    stash();
+    __syncthreads();
+    if (k0 + DM_BK < K) fetch(k0 + DM_BK);
+#pragma unroll
+    for (int ks = 0; ks < DM_BK; ks += 4) {
+      double ar[4], ai[4], bre[2], bim[2];
+#pragma unroll
+      for (int mt = 0; mt < 4; ++mt) {
+        ar[mt] = Ar[ks + t][wm + mt * 8 + g];
+        ai[mt] = Ai[ks + t][wm + mt * 8 + g];
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        bre[nt] = Br[ks + t][wn + nt * 8 + g];
+        bim[nt] = Bi[ks + t][wn + nt * 8 + g];
+      }
+#pragma unroll
+      for (int mt = 0; mt < 4; ++mt) {
+        const double an = neg(ai[mt]);
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+          dmma_884(cr[mt][nt][0], cr[mt][nt][1], ar[mt], bre[nt]);
+          dmma_884(cr[mt][nt][0], cr[mt][nt][1], an, bim[nt]);
+          dmma_884(ci[mt][nt][0], ci[mt][nt][1], ar[mt], bim[nt]);
+          dmma_884(ci[mt][nt][0], ci[mt][nt][1], ai[mt], bre[nt]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // accumulator (mt, nt, i): row wm + mt*8 + g, column wn + nt*8 + 2t + i
+#pragma unroll
+  for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int gm = m0 + wm + mt * 8 + g, gn = n0 + wn + nt * 8 + 2 * t + i;
+        if (gm < M && gn < N) Y[(int64_t)gm * N + gn] = cmk(cr[mt][nt][i], ci[mt][nt][i]);
+      }
+}
+
 // ---------------------------------------------------------------- Ozaki split
 constexpr int OZ_BETA = 6;       // bits per slice
 constexpr int OZ_MAX_SLICES = 9;  // 54 bits
@@ -669,7 +776,7 @@ extern "C" {
 
 MM_API size_t mm_fock_gemm_workspace_bytes(int mode, int64_t M, int64_t N, int64_t K, int slices) {
   if (M < 1 || N < 1 || K < 1) return 0;
-  if (mode == 0) return 256;
+  if (mode == 0 || mode == 2) return 256;
   if (mode != 1 || slices < 2 || slices > OZ_MAX_SLICES) return 0;
   return oz_layout(M, N, K, slices).total;
 }
@@ -688,6 +795,13 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
     dim3 grid((unsigned)((N + FG_BN - 1) / FG_BN), (unsigned)((M + FG_BM - 1) / FG_BM));
     if (grid.y > 65535) return MM_ERR_TOO_LARGE;
     zgemm_fp64_kernel<<<grid, 256, 0, st>>>((const double2*)U, (const double2*)X, (double2*)Y, (int)M, (int)N, (int)K);
+    mm::note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
+  }
+  if (mode == 2) {
+    dim3 grid((unsigned)((N + DM_BN - 1) / DM_BN), (unsigned)((M + DM_BM - 1) / DM_BM));
+    if (grid.y > 65535) return MM_ERR_TOO_LARGE;
+    zgemm_dmma_kernel<<<grid, 128, 0, st>>>((const double2*)U, (const double2*)X, (double2*)Y, (int)M, (int)N, (int)K);
     mm::note_launches(1);
     return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
   }

@@ -8,8 +8,9 @@ a gate-on-kets contraction to numpy ``tensordot`` -> BLAS zgemm.  With the refer
 unitary's Fock tensor is (out0, out1, in0, in1) and the contraction with kets (n, in0, in1) is
 one complex GEMM: U reshaped (c0*c1, c0'*c1') times the kets stacked as columns.
 
-``fock_gemm(U, X, mode)`` computes Y = U X with the native FP64 kernel (``"fp64"``) or the
-Ozaki-split BF16 tensor-core kernel (``"ozaki"``); ``apply_unitary`` is the gate-on-kets wrapper.
+``fock_gemm(U, X, mode)`` computes Y = U X with the native FP64 kernel (``"fp64"``: DFMA), the
+FP64 tensor-core kernel (``"dmma"``: mma.sync .f64) or the Ozaki-split BF16 tensor-core kernel
+(``"ozaki"``); ``apply_unitary`` is the gate-on-kets wrapper.
 """
 
 from __future__ import annotations
@@ -22,7 +23,7 @@ from .hermite import Workspace, _is_dev, _stream, raw, require_cuda
 
 __all__ = ["fock_gemm", "apply_unitary"]
 
-_MODES = {"fp64": 0, "ozaki": 1, "ozaki_bf16": 1}
+_MODES = {"fp64": 0, "ozaki": 1, "ozaki_bf16": 1, "dmma": 2, "fp64_dmma": 2}
 
 
 def fock_gemm(U, X, mode: str = "fp64", slices: int = 9, out=None):

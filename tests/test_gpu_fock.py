@@ -1,7 +1,7 @@
-"""GPU parity of the Fock contraction (FP64 and Ozaki-split BF16 paths) against the FP64 CPU
-oracle (numpy @ -> BLAS zgemm, the arithmetic ArrayAnsatz.contract reaches through einsum).
+"""GPU parity of the Fock contraction (FP64 DFMA, FP64 MMA and Ozaki-split BF16 paths) against the
+FP64 CPU oracle (numpy @ -> BLAS zgemm, the arithmetic ArrayAnsatz.contract reaches through einsum).
 
-Error metric: max|Y - Y_ref| / max|Y_ref|.  FP64 kernel: 1e-14.  Ozaki split with 9 slices
+Error metric: max|Y - Y_ref| / max|Y_ref|.  FP64 kernels (DFMA and MMA): 1e-14.  Ozaki split with 9 slices
 (54 bits per operand, pairs with slice order <= 10): 1e-13; fewer slices give coarser results
 (checked to shrink monotonically)."""
 
@@ -34,6 +34,7 @@ def test_gemm_random(cuda, oracle_lib, M, N, K):
     U, X = cn((M, K), M + K), cn((K, N), N)
     ref = oracle_lib.fock_gemm(U, X)
     assert rel(mm.fock_gemm(U, X, "fp64"), ref) < 1e-14
+    assert rel(mm.fock_gemm(U, X, "dmma"), ref) < 1e-14
     assert rel(mm.fock_gemm(U, X, "ozaki"), ref) < 1e-13
 
 
@@ -48,6 +49,7 @@ def test_gemm_wide_dynamic_range(cuda, oracle_lib):
     scale = np.abs(U).max(axis=1, keepdims=True) * np.abs(X).max(axis=0, keepdims=True) * U.shape[1]
     assert (np.abs(Y - ref) / scale).max() < 1e-15
     assert rel(mm.fock_gemm(U, X, "fp64"), ref) < 1e-14
+    assert rel(mm.fock_gemm(U, X, "dmma"), ref) < 1e-14
 
 
 def test_gemm_slices_converge(cuda, oracle_lib):
@@ -74,7 +76,7 @@ def test_cfg5_unitary_on_kets(cuda, oracle_lib):
     kt = torch.as_tensor(kets, device=cuda)
     U = Ut.cpu().numpy()
     ref = np.einsum("abcd,ncd->nab", U, kets)
-    for mode, tol in (("fp64", 1e-14), ("ozaki", 1e-13)):
+    for mode, tol in (("fp64", 1e-14), ("dmma", 1e-14), ("ozaki", 1e-13)):
         Y = mm.apply_unitary(Ut, kt, mode=mode)
         assert Y.shape == (256, 50, 50)
         assert rel(Y, ref) < tol, mode
