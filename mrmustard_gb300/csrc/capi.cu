@@ -267,6 +267,99 @@ FlowTuning flow_tuning() {
   return t;
 }
 
+// One small instance on one thread-block cluster (fwd_cluster_kernel, no setup
+// kernel): used for single vanilla instances of at least MM_CLUSTER_MIN_AMPS
+// amplitudes (default 1024) that fit its shared-memory tables (cluster_fits);
+// MM_CLUSTER_FWD=0 disables it, MM_CLUSTER_CTAS fixes the cluster size (default:
+// CTA 0 for slab 0 plus one worker CTA per 64 amplitudes of a level-0 chunk, at
+// most 16 CTAs).
+struct ClusterTuning {
+  int enabled = 1, ctas = 0;
+  int64_t min_amps = 1024;
+};
+ClusterTuning cluster_tuning() {
+  static ClusterTuning t = [] {
+    ClusterTuning r;
+    if (const char* e = getenv("MM_CLUSTER_FWD")) r.enabled = atoi(e) != 0;
+    if (const char* e = getenv("MM_CLUSTER_CTAS")) r.ctas = std::min(16, std::max(1, atoi(e)));
+    if (const char* e = getenv("MM_CLUSTER_MIN_AMPS")) r.min_amps = std::max<int64_t>(1, atoll(e));
+    return r;
+  }();
+  return t;
+}
+
+bool cluster_route(const UniformPlan& P, int stable) {
+  const ClusterTuning t = cluster_tuning();
+  return P.B == 1 && !stable && t.enabled && P.g.n >= t.min_amps && cluster_fits(P.g);
+}
+
+template <int D, int A>
+int launch_fwd_cluster_A(const UniformSrc& src, int cl, cudaStream_t st) {
+  auto kern = fwd_cluster_kernel<D, A>;
+  // attributes once per kernel; whether a cluster of `cl` fits, once per (kernel, cl)
+  static std::once_flag attr_once;
+  static std::atomic<int> fits[17];
+  std::call_once(attr_once, [&] {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cluster_fwd_smem_bytes());
+    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaGetLastError();
+  });
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = {};
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)cl);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = cluster_fwd_smem_bytes();
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int f = fits[cl].load();
+  if (f == 0) {
+    int ncl = 0;
+    f = (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) == cudaSuccess && ncl >= 1) ? 1 : -1;
+    cudaGetLastError();
+    fits[cl].store(f);
+  }
+  if (f < 0) return MM_ERR_UNSUPPORTED;
+  MM_CUDA(cudaLaunchKernelEx(&cfg, kern, src));
+  g_launches.fetch_add(1);
+  return MM_OK;
+}
+
+template <int D>
+int launch_fwd_cluster_D(const UniformPlan& P, const UniformSrc& src, cudaStream_t st) {
+  const ClusterTuning t = cluster_tuning();
+  const uint32_t s0 = (uint32_t)P.g.strides[0];
+  int cl = t.ctas ? t.ctas : (s0 <= 64u ? 1 : (int)std::min<uint32_t>(16u, 1u + (s0 + 63u) / 64u));
+  int rc = MM_ERR_UNSUPPORTED;
+  for (; cl >= 1 && rc == MM_ERR_UNSUPPORTED; cl = cl > 8 ? 8 : 0) {
+    const uint32_t nwork = cl > 1 ? (uint32_t)cl - 1u : 1u;
+    const uint32_t pc = (s0 + nwork - 1u) / nwork;
+    if (pc > kClusterRangeMax) break;
+    if (pc <= 128) rc = launch_fwd_cluster_A<D, 1>(src, cl, st);
+    else if (pc <= 256) rc = launch_fwd_cluster_A<D, 2>(src, cl, st);
+    else rc = launch_fwd_cluster_A<D, 4>(src, cl, st);
+  }
+  return rc;
+}
+
+int launch_fwd_cluster(const UniformPlan& P, const UniformSrc& src, cudaStream_t st) {
+  switch (P.g.D) {
+    case 1: return launch_fwd_cluster_D<1>(P, src, st);
+    case 2: return launch_fwd_cluster_D<2>(P, src, st);
+    case 3: return launch_fwd_cluster_D<3>(P, src, st);
+    case 4: return launch_fwd_cluster_D<4>(P, src, st);
+    case 5: return launch_fwd_cluster_D<5>(P, src, st);
+    case 6: return launch_fwd_cluster_D<6>(P, src, st);
+    case 7: return launch_fwd_cluster_D<7>(P, src, st);
+    case 8: return launch_fwd_cluster_D<8>(P, src, st);
+  }
+  return MM_ERR_UNSUPPORTED;
+}
+
 template <int D>
 int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, int stable, const DevInfo& di,
                          cudaStream_t st) {
@@ -498,6 +591,7 @@ struct HostStage {
   char* dev = nullptr;
   size_t dev_bytes = 0;
   bool ws_fresh = false;
+  size_t ws_at = 0;  // offset of the workspace in `dev` at the last call
 };
 HostStage g_stage[64];
 
@@ -520,9 +614,11 @@ int stage_reserve(HostStage& s, size_t pin_need, size_t dev_need) {
   return MM_OK;
 }
 
-// Runs `compute` on device copies of `ins` (host buffers, concatenated) and copies `outs` back;
-// the workspace sits at the start of the device buffer and its status word comes back with the
-// outputs in the same synchronisation.
+// Runs `compute` on `ins` (host buffers, concatenated into the pinned staging area) and copies
+// `outs` back.  Device buffer: outputs, then the workspace (its status word right after the
+// outputs, so one copy brings both back), then device copies of the inputs.  With `zero_copy_in`
+// the kernels read the inputs from the pinned staging area itself (mapped into the device's
+// address space), which saves the upload for small inputs read once.
 struct HostSeg {
   const void* host;
   size_t bytes;
@@ -533,7 +629,7 @@ struct HostOut {
 };
 template <class F>
 int run_host_staged(size_t ws_bytes, const HostSeg* ins, int n_in, const HostOut* outs, int n_out, cudaStream_t st,
-                    F compute) {
+                    bool zero_copy_in, F compute) {
   int dev = 0;
   MM_CUDA(cudaGetDevice(&dev));
   HostStage& s = g_stage[dev & 63];
@@ -541,35 +637,37 @@ int run_host_staged(size_t ws_bytes, const HostSeg* ins, int n_in, const HostOut
   size_t in_bytes = 0, out_bytes = 0;
   for (int i = 0; i < n_in; ++i) in_bytes += align_up(ins[i].bytes);
   for (int i = 0; i < n_out; ++i) out_bytes += align_up(outs[i].bytes);
-  const size_t d_in = align_up(ws_bytes), d_out = d_in + in_bytes;
-  const size_t p_status = in_bytes, p_out = p_status + kAlign;
-  int rc = stage_reserve(s, p_out + out_bytes, d_out + out_bytes);
+  const size_t d_ws = out_bytes, d_in = d_ws + align_up(ws_bytes);
+  const size_t p_out = in_bytes;  // pinned: inputs, then outputs and the status word
+  int rc = stage_reserve(s, p_out + out_bytes + kAlign, d_in + (zero_copy_in ? 0 : in_bytes));
   if (rc) return rc;
-  if (s.ws_fresh) {
-    MM_CUDA(cudaMemsetAsync(s.dev, 0, sizeof(WsHeader), st));
+  char* ws = s.dev + d_ws;
+  if (s.ws_fresh || s.ws_at != d_ws) {  // the workspace moved (or is new): zero its header
+    MM_CUDA(cudaMemsetAsync(ws, 0, sizeof(WsHeader), st));
     s.ws_fresh = false;
+    s.ws_at = d_ws;
   }
   std::vector<char*> din(n_in), dout(n_out);
   size_t o = 0;
   for (int i = 0; i < n_in; ++i) {
     memcpy(s.pin + o, ins[i].host, ins[i].bytes);
-    din[i] = s.dev + d_in + o;
+    din[i] = zero_copy_in ? s.pin + o : s.dev + d_in + o;
     o += align_up(ins[i].bytes);
   }
-  if (in_bytes) MM_CUDA(cudaMemcpyAsync(s.dev + d_in, s.pin, in_bytes, cudaMemcpyHostToDevice, st));
+  if (in_bytes && !zero_copy_in) MM_CUDA(cudaMemcpyAsync(s.dev + d_in, s.pin, in_bytes, cudaMemcpyHostToDevice, st));
   o = 0;
   for (int i = 0; i < n_out; ++i) {
-    dout[i] = s.dev + d_out + o;
+    dout[i] = s.dev + o;
     o += align_up(outs[i].bytes);
   }
-  if ((rc = compute(s.dev, din.data(), dout.data()))) return rc;
-  if (out_bytes) MM_CUDA(cudaMemcpyAsync(s.pin + p_out, s.dev + d_out, out_bytes, cudaMemcpyDeviceToHost, st));
-  MM_CUDA(cudaMemcpyAsync(s.pin + p_status, s.dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  if ((rc = compute(ws, din.data(), dout.data()))) return rc;
+  // outputs and the status word (first bytes of the workspace, right after them) in one copy
+  MM_CUDA(cudaMemcpyAsync(s.pin + p_out, s.dev, out_bytes + sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   MM_CUDA(cudaStreamSynchronize(st));
   int32_t status = 0;
-  memcpy(&status, s.pin + p_status, sizeof(status));
+  memcpy(&status, s.pin + p_out + out_bytes, sizeof(status));
   if (status != 0) {
-    MM_CUDA(cudaMemsetAsync(s.dev, 0, sizeof(int32_t), st));
+    MM_CUDA(cudaMemsetAsync(ws, 0, sizeof(int32_t), st));
     MM_CUDA(cudaStreamSynchronize(st));
     return status;
   }
@@ -578,6 +676,37 @@ int run_host_staged(size_t ws_bytes, const HostSeg* ins, int n_in, const HostOut
     memcpy(outs[i].host, s.pin + p_out + o, outs[i].bytes);
     o += align_up(outs[i].bytes);
   }
+  return MM_OK;
+}
+}  // namespace
+
+// Host-buffer forward of one instance on the one-cluster kernel: the kernel reads A, b, c from
+// the pinned staging area and writes G straight into it (the GPU addresses pinned host memory
+// directly; the kernel never reads G back), so the call is one launch, one synchronisation and
+// one host copy.  The kernel has no waits that can give up, so there is no status word to read.
+namespace {
+int fwd_host_cluster(const UniformPlan& P, const mm_c128* A, const mm_c128* b, const mm_c128* c, mm_c128* G,
+                     cudaStream_t st) {
+  int dev = 0;
+  MM_CUDA(cudaGetDevice(&dev));
+  HostStage& s = g_stage[dev & 63];
+  std::lock_guard<std::mutex> lk(s.mu);
+  const int D = P.g.D;
+  const size_t a_bytes = align_up((size_t)D * D * sizeof(mm_c128)), b_bytes = align_up((size_t)D * sizeof(mm_c128));
+  const size_t in_bytes = a_bytes + b_bytes + align_up(sizeof(mm_c128));
+  const size_t out_bytes = (size_t)P.g.n * sizeof(mm_c128);
+  int rc = stage_reserve(s, in_bytes + out_bytes, 0);
+  if (rc) return rc;
+  memcpy(s.pin, A, (size_t)D * D * sizeof(mm_c128));
+  memcpy(s.pin + a_bytes, b, (size_t)D * sizeof(mm_c128));
+  memcpy(s.pin + a_bytes + b_bytes, c, sizeof(mm_c128));
+  UniformSrc src = uniform_src(P, reinterpret_cast<const double2*>(s.pin), reinterpret_cast<const double2*>(s.pin + a_bytes),
+                               reinterpret_cast<const double2*>(s.pin + a_bytes + b_bytes),
+                               reinterpret_cast<double2*>(s.pin + in_bytes), nullptr, s.pin);
+  src.coef = nullptr;  // no workspace: the cluster kernel builds its own coefficients
+  if ((rc = launch_fwd_cluster(P, src, st))) return rc;
+  MM_CUDA(cudaStreamSynchronize(st));
+  memcpy(G, s.pin + in_bytes, out_bytes);
   return MM_OK;
 }
 }  // namespace
@@ -881,6 +1010,10 @@ int mm_hermite_fwd_batched(int64_t B, int D, const int64_t* shape, const mm_c128
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(ws);
   UniformSrc src = uniform_src(P, (const double2*)A, (const double2*)b, (const double2*)c, (double2*)G, nullptr, w);
+  if (cluster_route(P, stable)) {  // one launch, no setup kernel and no workspace state
+    rc = launch_fwd_cluster(P, src, st);
+    if (rc != MM_ERR_UNSUPPORTED) return rc;  // no cluster fits: the paths below
+  }
   if ((rc = reset_launch_state(w, st))) return rc;
   if ((rc = launch_setup(src, B, w, P.L, 1, st))) return rc;
   return launch_fwd_uniform(P, src, w, stable, di, st);
@@ -899,10 +1032,14 @@ int mm_hermite_fwd_host(int D, const int64_t* shape, const mm_c128* A, const mm_
   UniformPlan P;
   if ((rc = plan_uniform(1, D, shape, P, di.sms))) return rc;
   if (!A || !b || !c || !G) return MM_ERR_INVALID_ARG;
+  if (cluster_route(P, stable)) {
+    rc = fwd_host_cluster(P, A, b, c, G, (cudaStream_t)stream);
+    if (rc != MM_ERR_UNSUPPORTED) return rc;  // no cluster fits: the staged path below
+  }
   const size_t wsb = mm_hermite_workspace_bytes(D, shape, 1);
   const HostSeg ins[3] = {{A, (size_t)D * D * sizeof(mm_c128)}, {b, (size_t)D * sizeof(mm_c128)}, {c, sizeof(mm_c128)}};
   const HostOut outs[1] = {{G, (size_t)P.g.n * sizeof(mm_c128)}};
-  return run_host_staged(wsb, ins, 3, outs, 1, (cudaStream_t)stream, [&](char* ws, char** din, char** dout) {
+  return run_host_staged(wsb, ins, 3, outs, 1, (cudaStream_t)stream, true, [&](char* ws, char** din, char** dout) {
     return mm_hermite_fwd(D, shape, (const mm_c128*)din[0], (const mm_c128*)din[1], (const mm_c128*)din[2], stable,
                           (mm_c128*)dout[0], ws, wsb, stream);
   });
@@ -921,7 +1058,7 @@ int mm_hermite_vjp_host(int D, const int64_t* shape, const mm_c128* G, const mm_
   const HostSeg ins[3] = {{G, nb}, {dLdG, nb}, {c, sizeof(mm_c128)}};
   const HostOut outs[3] = {{dA, (size_t)D * D * sizeof(mm_c128)}, {db, (size_t)D * sizeof(mm_c128)},
                            {dc, sizeof(mm_c128)}};
-  return run_host_staged(wsb, ins, 3, outs, 3, (cudaStream_t)stream, [&](char* ws, char** din, char** dout) {
+  return run_host_staged(wsb, ins, 3, outs, 3, (cudaStream_t)stream, false, [&](char* ws, char** din, char** dout) {
     return mm_hermite_vjp(D, shape, (const mm_c128*)din[0], (const mm_c128*)din[2], (const mm_c128*)din[1],
                           (mm_c128*)dout[0], (mm_c128*)dout[1], (mm_c128*)dout[2], ws, wsb, stream);
   });

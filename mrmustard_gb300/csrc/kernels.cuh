@@ -872,24 +872,27 @@ void bar_sync_n(uint32_t id, uint32_t n);
 // `lanes` threads (lane pairs, see part_fma), synchronised by a named
 // barrier over those threads only.  With one amplitude per lane pair its
 // indices and coefficients are loaded once; the per-chunk coefficients
-// (A_ii sqrt(m), 1/sqrt(m)) are fetched one chunk ahead.
+// (A_ii sqrt(m), 1/sqrt(m)) are fetched one chunk ahead.  `crow` is level i's
+// row of the coefficient block and `coff` the column it starts at (entry
+// prefC[j] + k is crow[prefC[j] + k - coff]), so a caller may stage only the
+// columns j >= 1 of a row in shared memory; `bi` is b_i.
 template <int D>
-__device__ void small_level(const InstView& v, const double* __restrict__ rs, int i, double2* Gs, uint32_t lanes) {
+__device__ void small_level(const InstView& v, const double* __restrict__ rs, int i, double2* Gs, uint32_t lanes,
+                            const double2* crow, int32_t coff, double2 bi) {
   const Geom& g = v.g;
   const uint32_t si = (uint32_t)g.strides[i];
   const int Ci = (int)g.shape[i];
   const bool im = (threadIdx.x & 1u) != 0;
   const uint32_t pairs = lanes >> 1, a0 = threadIdx.x >> 1;
-  const double2 bi = __ldg(v.b + i);
-  const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
-  const int32_t pci = g.prefC[i];
+  const int32_t pci = g.prefC[i] - coff;
   double* Gd = reinterpret_cast<double*>(Gs);
   const bool one = si <= pairs;
   int32_t k1[D];
   double2 w1[D];
   decompose<D>(a0 < si ? a0 : 0u, i + 1, g, k1);
 #pragma unroll
-  for (int j = 0; j < D; ++j) w1[j] = (one && j > i && k1[j] > 0) ? crow[g.prefC[j] + k1[j]] : cmk(0.0, 0.0);
+  for (int j = 0; j < D; ++j)
+    w1[j] = (one && j > i && k1[j] > 0) ? crow[g.prefC[j] - coff + k1[j]] : cmk(0.0, 0.0);
   double rs_c = rs[1];
   double2 cd_c = cmk(0.0, 0.0);
   for (int m = 1; m < Ci; ++m) {
@@ -919,7 +922,8 @@ __device__ void small_level(const InstView& v, const double* __restrict__ rs, in
         if (m >= 2) acc = part_fma(cd, Gs[p - si], im, acc);
 #pragma unroll
         for (int j = 1; j < D; ++j)
-          if (j > i && k[j] > 0) acc = part_fma(crow[g.prefC[j] + k[j]], Gs[p - (uint32_t)g.strides[j]], im, acc);
+          if (j > i && k[j] > 0)
+            acc = part_fma(crow[g.prefC[j] - coff + k[j]], Gs[p - (uint32_t)g.strides[j]], im, acc);
         Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
       }
     }
@@ -1066,7 +1070,8 @@ __global__ void __launch_bounds__(256) fwd_flow_kernel(UniformSrc src, const dou
       __syncthreads();
       for (int i = D - 1; i >= L; --i) {
         const uint32_t lanes = min((2u * (uint32_t)g.strides[i] + 31u) / 32u * 32u, blockDim.x);
-        if (threadIdx.x < lanes) small_level<D>(sv, rs, i, Gs, lanes);
+        if (threadIdx.x < lanes)
+          small_level<D>(sv, rs, i, Gs, lanes, sv.coef + (int64_t)i * g.sumC, 0, __ldg(sv.b + i));
         __syncthreads();
       }
       for (uint32_t f = threadIdx.x; f < fp.small_amps; f += blockDim.x) stG(sv, f, Gs[f], 7);
@@ -1133,6 +1138,240 @@ __global__ void __launch_bounds__(256) fwd_flow_kernel(UniformSrc src, const dou
       // the CTA barrier orders every thread's stores before thread 0's release
       if (threadIdx.x == 0 && (publish_each || m == Ci - 1)) st_release_u32(prog + fp.flag0[i] + v, (uint32_t)m);
     }
+  }
+}
+
+// ------------------------------------------------ one small instance on one cluster
+// Instances whose slab 0 (the strides[0] amplitudes with k_0 = 0) fits the face
+// region, in ONE launch with no setup kernel: every CTA builds the coefficients
+// and 1/sqrt(m) values it needs in its own shared memory with the expressions of
+// setup_kernel (A_ii sqrt(m - 1), A_ij sqrt(k), 1 / sqrt(m)), so the values are
+// the same.  CTA 0 computes levels 1 .. D-1 in its shared memory (small_level,
+// lane pairs), then every chunk m >= 1 of level 0 is split over the cluster's
+// CTAs in contiguous ranges [lo, hi), one hardware cluster barrier per chunk.  A
+// lane pair keeps the last two values of its amplitudes in registers and a CTA
+// its range of the previous chunk in shared memory (S).  The neighbours
+// q - strides[j] below `lo` (at most `hmax`, the largest stride of an axis
+// j >= 1, away) are PUSHED by the CTAs that own them, right after they compute
+// them, into the halo buffer H of every CTA that will read them (remote
+// shared-memory stores), so a chunk reads only its own shared memory and the
+// push latency is hidden behind the barrier.  Slab 0 is pushed the same way by
+// CTA 0 before chunk 1.  The only waits are hardware cluster barriers that every
+// CTA reaches the same number of times.
+constexpr uint32_t kClusterRangeMax = 512;   // amplitudes of one CTA's level-0 range (A <= 4 at 256 threads)
+constexpr uint32_t kClusterHaloMax = 1280;   // hmax <= strides[0] / 2 <= kFlowSmemAmps / 2
+constexpr uint32_t kClusterCoefMax = 2560;   // coefficient columns j >= 1 of levels 1 .. D-1
+constexpr uint32_t kClusterC0Max = 1024;     // extent of axis 0 (per-chunk tables of level 0)
+constexpr uint32_t kClusterRsMax = kFlowSmemAmps + 1;
+
+__host__ __device__ constexpr size_t cluster_fwd_smem_bytes() {
+  return (size_t)(kFlowSmemAmps + 2 * kClusterRangeMax + 2 * kClusterHaloMax + kClusterCoefMax + kClusterC0Max +
+                  MM_MAXD * MM_MAXD + MM_MAXD + 8) * sizeof(double2) +
+         (size_t)(kClusterRsMax + 1 + kClusterC0Max) * sizeof(double);
+}
+
+// Largest stride of an axis j >= 1 whose extent is at least 2 (the farthest
+// neighbour of level 0); 0 if there is none.
+__host__ __device__ inline uint32_t cluster_halo(const Geom& g) {
+  uint32_t h = 0;
+  for (int j = 1; j < g.D; ++j)
+    if (g.shape[j] >= 2 && (uint32_t)g.strides[j] > h) h = (uint32_t)g.strides[j];
+  return h;
+}
+
+// Coefficient columns j >= 1 (levels 1 .. D-1 read only those).
+__host__ __device__ inline uint32_t cluster_coef_cols(const Geom& g) { return (uint32_t)(g.sumC - g.shape[0]); }
+
+// Largest extent of an axis j >= 1.
+__host__ __device__ inline uint32_t cluster_face_cmax(const Geom& g) {
+  uint32_t c = 1;
+  for (int j = 1; j < g.D; ++j) c = max(c, (uint32_t)g.shape[j]);
+  return c;
+}
+
+// Whether an instance fits fwd_cluster_kernel's shared-memory tables.
+__host__ __device__ inline bool cluster_fits(const Geom& g) {
+  return g.strides[0] <= (int64_t)kFlowSmemAmps && g.shape[0] <= (int64_t)kClusterC0Max &&
+         (uint64_t)(g.D - 1) * cluster_coef_cols(g) <= kClusterCoefMax && cluster_face_cmax(g) < kClusterRsMax;
+}
+
+__device__ __forceinline__ uint32_t cluster_addr(const void* local, uint32_t peer) {
+#if defined(__CUDA_ARCH__)
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(local), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(peer));
+  return r;
+#else
+  (void)peer;
+  return (uint32_t)(uintptr_t)local;
+#endif
+}
+__device__ __forceinline__ void cluster_st(const double* local, uint32_t peer, double x) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(cluster_addr(local, peer)), "d"(x) : "memory");
+#else
+  (void)peer;
+  *const_cast<double*>(local) = x;
+#endif
+}
+__device__ __forceinline__ void cluster_st2(const double2* local, uint32_t peer, double2 x) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};" ::"r"(cluster_addr(local, peer)), "d"(x.x), "d"(x.y)
+               : "memory");
+#else
+  (void)peer;
+  *const_cast<double2*>(local) = x;
+#endif
+}
+
+// setup_kernel's coefficient of row i, column c (axis j = the one holding c).
+__device__ __forceinline__ double2 cluster_coef(const Geom& g, const double2* As, int i, int32_t c) {
+  int j = 0;
+  while (j + 1 < g.D && g.prefC[j + 1] <= c) ++j;
+  const int32_t kk = c - g.prefC[j];
+  const double2 a = As[i * g.D + j];
+  const double s = (j == i) ? (kk >= 1 ? sqrt((double)(kk - 1)) : 0.0) : sqrt((double)kk);
+  return cmk(a.x * s, a.y * s);
+}
+
+template <int D, int A>
+__global__ void __launch_bounds__(256) fwd_cluster_kernel(UniformSrc src) {
+  extern __shared__ __align__(16) unsigned char cluster_smem[];
+  double2* face = reinterpret_cast<double2*>(cluster_smem);
+  double2* S = face + kFlowSmemAmps;        // [2][kClusterRangeMax]: own range of chunks m - 1, m
+  double2* H = S + 2 * kClusterRangeMax;    // [2][kClusterHaloMax]: H[.][t] = amplitude lo - 1 - t
+  double2* cst = H + 2 * kClusterHaloMax;   // coefficient columns j >= 1 of levels 1 .. D-1 (CTA 0)
+  double2* cd0 = cst + kClusterCoefMax;     // A_00 sqrt(m - 1), m < C0
+  double2* As = cd0 + kClusterC0Max;        // A (D x D)
+  double2* bs = As + MM_MAXD * MM_MAXD;     // b, then c
+  double* rst = reinterpret_cast<double*>(bs + MM_MAXD + 8);  // 1 / sqrt(m), m <= max C_i (i >= 1)
+  double* rs0 = rst + kClusterRsMax + 1;                       // 1 / sqrt(m), m < C0
+  MM_SHARED(InstView, sv);
+  const uint32_t rank = cluster_rank(), nranks = cluster_size();
+  // CTA 0 computes slab 0; level 0 is split over the other CTAs ("workers"; CTA 0 too if it is alone),
+  // which build their tables and per-amplitude coefficients while CTA 0 works on slab 0
+  const uint32_t base = nranks > 1 ? 1u : 0u, nwork = nranks - base;
+  const bool worker = rank >= base;
+  const uint32_t wr = worker ? rank - base : 0u;
+  if (threadIdx.x == 0) src.load(0, sv);
+  __syncthreads();
+  const Geom& g = sv.g;
+  const uint32_t s0 = (uint32_t)g.strides[0];
+  const uint32_t per = (s0 + nwork - 1) / nwork;
+  const uint32_t lo = worker ? min(s0, per * wr) : 0u, hi = worker ? min(s0, lo + per) : 0u;
+  const uint32_t hmax = cluster_halo(g);
+  const int C0 = (int)g.shape[0];
+  for (uint32_t e = threadIdx.x; e < (uint32_t)(D * D); e += blockDim.x) As[e] = sv.A[e];
+  if (threadIdx.x < (uint32_t)D) bs[threadIdx.x] = sv.b[threadIdx.x];
+  if (threadIdx.x == (uint32_t)D) bs[D] = sv.c;
+  __syncthreads();
+  if (worker) {  // level-0 tables
+    for (uint32_t m = threadIdx.x; m < (uint32_t)C0; m += blockDim.x) {
+      const double sm = sqrt((double)m);
+      rs0[m] = m > 0 ? 1.0 / sm : 0.0;
+      const double s = m >= 1 ? sqrt((double)(m - 1)) : 0.0;
+      cd0[m] = cmk(As[0].x * s, As[0].y * s);
+    }
+  }
+  const bool im = (threadIdx.x & 1u) != 0;
+  const uint32_t pairs = blockDim.x >> 1, a0 = threadIdx.x >> 1;
+  int32_t k[A][D];
+  double2 w[A][D];    // A_0j sqrt(k_j) of each amplitude (j >= 1; zero where k_j = 0): constant along m
+  uint32_t ncons[A];  // workers after this one whose halo holds the amplitude
+#pragma unroll
+  for (int u = 0; u < A; ++u) {
+    const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+    decompose<D>(q < hi ? q : 0u, 1, g, k[u]);
+    uint32_t nc = 0;
+    while (q < hi && wr + 1 + nc < nwork && (wr + 1 + nc) * per <= q + hmax) ++nc;
+    ncons[u] = nc;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      w[u][j] = cmk(0.0, 0.0);
+      if (j >= 1 && q < hi && k[u][j] > 0) {
+        const double sk = sqrt((double)k[u][j]);
+        w[u][j] = cmk(As[j].x * sk, As[j].y * sk);
+      }
+    }
+  }
+  if (rank == 0) {
+    const uint32_t R = cluster_coef_cols(g), fc = cluster_face_cmax(g);
+    for (uint32_t m = threadIdx.x; m <= fc; m += blockDim.x) rst[m] = m > 0 ? 1.0 / sqrt((double)m) : 0.0;
+    for (uint32_t e = threadIdx.x; e < (uint32_t)(D - 1) * R; e += blockDim.x) {
+      const uint32_t i = 1 + e / R, col = e - (i - 1) * R;
+      cst[e] = cluster_coef(g, As, (int)i, g.prefC[1] + (int32_t)col);
+    }
+    if (threadIdx.x == 0) face[0] = bs[D];
+    __syncthreads();
+    for (int i = D - 1; i >= 1; --i) {
+      const uint32_t lanes = min((2u * (uint32_t)g.strides[i] + 31u) / 32u * 32u, blockDim.x);
+      if (threadIdx.x < lanes) small_level<D>(sv, rst, i, face, lanes, cst + (int64_t)(i - 1) * R, g.prefC[1], bs[i]);
+      __syncthreads();
+    }
+    // slab 0: to G, and pushed to every CTA as its "previous chunk" (S[0]) and halo (H[0])
+    for (uint32_t q = threadIdx.x; q < s0; q += blockDim.x) {
+      const double2 v = face[q];
+      stG(sv, q, v, 7);
+      if (C0 >= 2) {
+        const uint32_t r = q / per;  // worker owning q
+        cluster_st2(S + (q - r * per), r + base, v);
+        for (uint32_t r2 = r + 1; r2 < nwork && r2 * per <= q + hmax; ++r2)
+          cluster_st2(H + (r2 * per - 1 - q), r2 + base, v);
+      }
+    }
+  }
+  cluster_sync();
+  if (C0 < 2) return;  // the same in every CTA: no barrier is skipped by some only
+  const double2 b0 = bs[0];
+  double* Gd = reinterpret_cast<double*>(sv.G);
+  double* Sd = reinterpret_cast<double*>(S);
+  double* Hd = reinterpret_cast<double*>(H);
+  double gp[A], gpp[A];
+#pragma unroll
+  for (int u = 0; u < A; ++u) {
+    const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+    gpp[u] = 0.0;
+    gp[u] = q < hi ? Sd[2 * (q - lo) + (im ? 1 : 0)] : 0.0;  // slab 0 (pushed by CTA 0)
+  }
+  for (int m = 1; m < C0; ++m) {
+    const double2 cd = cd0[m];
+    const double rsm = rs0[m];
+    const uint32_t pb = ((m - 1) & 1u), nb = (m & 1u);
+    const double2* Sp = S + pb * kClusterRangeMax;
+    const double2* Hp = H + pb * kClusterHaloMax;
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+      const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+      const double op = __shfl_xor_sync(0xffffffffu, gp[u], 1), opp = __shfl_xor_sync(0xffffffffu, gpp[u], 1);
+      if (q < hi) {
+        double2 x[D];
+#pragma unroll
+        for (int j = 1; j < D; ++j) {
+          x[j] = cmk(0.0, 0.0);
+          if (k[u][j] > 0) {
+            const uint32_t qn = q - (uint32_t)g.strides[j];
+            x[j] = qn >= lo ? Sp[qn - lo] : Hp[lo - 1 - qn];
+          }
+        }
+        const double2 Gp = im ? cmk(op, gp[u]) : cmk(gp[u], op);
+        const double2 Gpp = im ? cmk(opp, gpp[u]) : cmk(gpp[u], opp);
+        double acc = part_fma(b0, Gp, im, 0.0);
+        if (m >= 2) acc = part_fma(cd, Gpp, im, acc);
+#pragma unroll
+        for (int j = 1; j < D; ++j)
+          if (k[u][j] > 0) acc = part_fma(w[u][j], x[j], im, acc);
+        const double val = rsm * acc;
+        const uint32_t pi = im ? 1u : 0u;
+        Gd[2 * ((int64_t)m * s0 + q) + pi] = val;
+        Sd[2 * (nb * kClusterRangeMax + (q - lo)) + pi] = val;
+        for (uint32_t c = 0; c < ncons[u]; ++c) {
+          const uint32_t r2 = wr + 1 + c;  // worker index
+          cluster_st(Hd + 2 * (nb * kClusterHaloMax + (r2 * per - 1 - q)) + pi, r2 + base, val);
+        }
+        gpp[u] = gp[u];
+        gp[u] = val;
+      }
+    }
+    cluster_sync();
   }
 }
 

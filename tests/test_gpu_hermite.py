@@ -178,8 +178,10 @@ def test_cfg2_large_single(cuda, oracle_lib, case):
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < tol
 
 
-# A single instance of at least 4096 amplitudes runs the dataflow forward (per-range progress
-# words, shared-memory small levels, lane-pair chains).  Shapes chosen for the corners of its plan:
+# A single instance of at least 4096 amplitudes whose slab 0 exceeds the 2560-amplitude face region
+# runs the dataflow forward (per-range progress words, shared-memory small levels, lane-pair chains);
+# those with a smaller slab 0 run the one-cluster kernel (tested below; the forced-schedule test runs
+# some of them on the dataflow kernel as well).  Shapes chosen for the corners of its plan:
 # a 1-D chain; 2-D; no shared-memory region (an axis longer than 2560); axes of length 1; D = 7, 8;
 # a whole tensor's face in shared memory; a level-1 chunk split over more than half the SMs (no
 # exclusive SMs); the smallest instances on the grid (4096 .. 8000 amplitudes, the 3-mode cutoff-20
@@ -193,6 +195,62 @@ def test_single_instance_dataflow_shapes(cuda, oracle_lib, shape):
     Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
                        torch.tensor(c, dtype=torch.complex128, device=cuda), shape)
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
+
+
+# A single instance of at least 1024 amplitudes whose slab 0 (strides[0] amplitudes) fits the
+# 2560-amplitude face region runs on one thread-block cluster (slab 0 on CTA 0, level-0 chunks split
+# over up to 16 CTAs, distributed shared memory): corners of its plan -- one chunk of level 0
+# (shape[0] = 1, 2), the largest slab 0 (2560: 16 CTAs, two amplitudes per lane pair), D = 1, 5, 6, 8,
+# a 1-CTA cluster, odd extents.
+CLUSTER_SHAPES = [(20, 20, 20), (8, 2560), (1, 40, 40), (2, 30, 30), (3, 4, 5, 6, 7), (1024,), (32, 32),
+                  (17, 13, 11), (4, 4, 4, 4, 4, 4), (3, 3, 3, 3, 3, 3, 3, 3), (10, 10, 10, 10), (40, 400)]
+
+
+@pytest.mark.parametrize("shape", CLUSTER_SHAPES)
+def test_single_instance_cluster_shapes(cuda, oracle_lib, shape):
+    A, b, _ = takagi(len(shape), 0.8, 1900 + sum(shape))
+    c = 0.7 - 0.2j
+    Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
+                       torch.tensor(c, dtype=torch.complex128, device=cuda), shape)
+    assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
+
+
+_FORCED = """
+import sys, numpy as np, torch
+sys.path.insert(0, {root!r})
+import mrmustard_gb300 as mm
+from test_gpu_hermite import takagi
+out = {{}}
+for shape in {shapes!r}:
+    A, b, c = takagi(len(shape), 0.8, 1900 + sum(shape))
+    G = mm.device_fwd(torch.as_tensor(A, device='cuda'), torch.as_tensor(b, device='cuda'),
+                      torch.tensor(0.7 - 0.2j, dtype=torch.complex128, device='cuda'), shape)
+    out['x'.join(map(str, shape))] = G.cpu().numpy()
+np.savez({path!r}, **out)
+"""
+
+
+@pytest.mark.parametrize("env", [{"MM_CLUSTER_FWD": "0"}, {"MM_CLUSTER_CTAS": "1"}, {"MM_CLUSTER_CTAS": "3"},
+                                 {"MM_CLUSTER_CTAS": "16"}])
+def test_single_instance_forced_schedules(cuda, oracle_lib, tmp_path, env):
+    """The same instances with the cluster kernel off (grid-wide dataflow kernel instead) and with
+    fixed cluster sizes (schedule knobs are read once per process, so each runs in a child)."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    shapes = [(20, 20, 20), (8, 2560), (2, 30, 30), (1024,), (40, 400)]
+    root = str(Path(__file__).resolve().parent.parent)
+    path = str(tmp_path / "forced.npz")
+    code = _FORCED.format(root=root, shapes=shapes, path=path)
+    envv = dict(os.environ, **env)
+    envv["PYTHONPATH"] = str(Path(__file__).resolve().parent) + os.pathsep + envv.get("PYTHONPATH", "")
+    subprocess.run([sys.executable, "-c", code], check=True, env=envv, timeout=600)
+    z = np.load(path)
+    for shape in shapes:
+        A, b, _ = takagi(len(shape), 0.8, 1900 + sum(shape))
+        assert rel(z["x".join(map(str, shape))], oracle_lib.vanilla(shape, A, b, 0.7 - 0.2j)) < FWD_TOL, (env, shape)
 
 
 @pytest.mark.parametrize("shape", [(24,) * 4, (20, 20, 20), (16, 16, 16), (4096,), (8, 8, 8, 8)])
