@@ -291,6 +291,21 @@ __global__ void __launch_bounds__(256) split_x_kernel(const double2* __restrict_
   slice_value(v.y, Fc, S, Xs + plane + idx, 2 * plane);
 }
 
+// t * 2^s for an integer |t| < 2^53 as a double, built with integer operations only (exact: a
+// power-of-two scale of an exactly representable integer), so the FP64 pipe -- 1/64 rate on
+// this part -- is not spent on conversions and scalings.  Falls back to FP64 arithmetic when the
+// result would leave the normal range.
+__device__ __forceinline__ double pow2(int e);
+__device__ __forceinline__ double scaled_i2d(long long t, int s) {
+  if (t == 0) return 0.0;
+  const unsigned long long a = t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
+  const int e = 63 - __clzll((long long)a);  // a = 1.f * 2^e
+  const int ex = e + s + 1023;
+  if (e > 52 || ex <= 0 || ex >= 2047) return (double)t * pow2(s);
+  const unsigned long long mant = (a << (52 - e)) & ((1ull << 52) - 1);
+  return __longlong_as_double((long long)(((t < 0 ? 1ull : 0ull) << 63) | ((unsigned long long)ex << 52) | mant));
+}
+
 __device__ __forceinline__ double pow2(int e) {
   if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
   return ldexp(1.0, e);
@@ -678,24 +693,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               tim = 0;
             }
           }
+          // every load of the group is issued before its stores, so the read-modify-writes of a row
+          // overlap instead of forming one chain of memory latencies
+          double2 y[8], o[8];
+          double2* yrow = Y + (int64_t)gm * N + n0 + c8 * 8;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int gn = n0 + c8 * 8 + j;
+            y[j] = cmk(0.0, 0.0);
+            o[j] = cmk(0.0, 0.0);
             if (gm < M && gn < N) {
               const int fc = F[gn];
-              double2 y = cmk(0.0, 0.0);
               if (er != INT32_MIN && fc != INT32_MIN) {
-                const double sc = pow2(er + fc - OZ_BETA * u.d);
-                y = cmk((double)vre[j] * sc, (double)vim[j] * sc);
+                const int sh = er + fc - OZ_BETA * u.d;
+                y[j] = cmk(scaled_i2d(vre[j], sh), scaled_i2d(vim[j], sh));
               }
-              double2* py = Y + (int64_t)gm * N + gn;
-              if (u.d == 2) {
-                *py = y;
-              } else {
-                const double2 o = *py;
-                *py = cmk(o.x + y.x, o.y + y.y);
-              }
+              if (u.d != 2) o[j] = yrow[j];
             }
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int gn = n0 + c8 * 8 + j;
+            if (gm < M && gn < N) yrow[j] = u.d == 2 ? y[j] : cmk(o[j].x + y[j].x, o[j].y + y[j].y);
           }
         }
         if constexpr (TMEM_T) tc_wait_st();

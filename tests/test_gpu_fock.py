@@ -80,3 +80,4 @@ def test_cfg5_unitary_on_kets(cuda, oracle_lib):
         Y = mm.apply_unitary(Ut, kt, mode=mode)
         assert Y.shape == (256, 50, 50)
         assert rel(Y, ref) < tol, mode
+
