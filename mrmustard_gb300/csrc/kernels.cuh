@@ -375,13 +375,42 @@ __device__ void fwd_instance_cta(const InstView& v, const double* rs) {
 static __constant__ double c_inv_n[MM_MAXD + 1] = {0.0,       1.0,       1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0,
                                             1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0, 1.0 / 8.0};
 
+// One amplitude k (flat index f) of the stable recurrence: the average over the
+// pivots i with k_i > 0 of (b_i G[k-1_i] + sum_j A_ij sqrt(k_j) G[k-1_i-1_j]
+// (k_j > 0, j != i) + A_ii sqrt(k_i - 1) G[k-2_i]) / sqrt(k_i) (core.py:182-211).
+template <int D, bool CG>
+__device__ __forceinline__ void stable_point(const InstView& v, const double* __restrict__ rs, const int32_t (&k)[D],
+                                             int64_t f, const int64_t (&sj)[D], const int32_t (&pj)[D]) {
+  const Geom& g = v.g;
+  double2* G = v.G;
+  double2 vals = cmk(0.0, 0.0);
+  int npiv = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    if (k[i] > 0) {
+      ++npiv;
+      const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
+      const int64_t pv = f - sj[i];
+      double2 acc = cmul(__ldg(v.b + i), ldG<CG>(G + pv));
+#pragma unroll
+      for (int j = 0; j < i; ++j)
+        if (k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + pv - sj[j]), acc);
+      if (k[i] >= 2) acc = cfma(crow[pj[i] + k[i]], ldG<CG>(G + pv - sj[i]), acc);
+#pragma unroll
+      for (int j = i + 1; j < D; ++j)
+        if (k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + pv - sj[j]), acc);
+      vals = crfma(rs[k[i]], acc, vals);
+    }
+  }
+  stG(v, f, cscale(c_inv_n[npiv], vals), 6);
+}
+
 // Wavefront |k| = w; prefixes p over axes 0..D-2 in [p_begin, p_end) by p_step.
 template <int D, bool CG>
 __device__ __forceinline__ void stable_wave(const InstView& v, const double* __restrict__ rs, int w, uint32_t p_begin,
                                             uint32_t p_end, uint32_t p_step, uint32_t t) {
   const Geom& g = v.g;
   const int32_t CL = (int32_t)g.shape[D - 1];
-  double2* G = v.G;
   int64_t sj[D];
   int32_t pj[D];
 #pragma unroll
@@ -403,27 +432,7 @@ __device__ __forceinline__ void stable_wave(const InstView& v, const double* __r
     const int32_t kl = w - sum;
     if (kl < 0 || kl >= CL) continue;
     k[D - 1] = kl;
-    const int64_t f = (int64_t)p * CL + kl;
-    double2 vals = cmk(0.0, 0.0);
-    int npiv = 0;
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-      if (k[i] > 0) {
-        ++npiv;
-        const double2* __restrict__ crow = v.coef + (int64_t)i * g.sumC;
-        const int64_t pv = f - sj[i];
-        double2 acc = cmul(__ldg(v.b + i), ldG<CG>(G + pv));
-#pragma unroll
-        for (int j = 0; j < i; ++j)
-          if (k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + pv - sj[j]), acc);
-        if (k[i] >= 2) acc = cfma(crow[pj[i] + k[i]], ldG<CG>(G + pv - sj[i]), acc);
-#pragma unroll
-        for (int j = i + 1; j < D; ++j)
-          if (k[j] > 0) acc = cfma(crow[pj[j] + k[j]], ldG<CG>(G + pv - sj[j]), acc);
-        vals = crfma(rs[k[i]], acc, vals);
-      }
-    }
-    stG(v, f, cscale(c_inv_n[npiv], vals), 6);
+    stable_point<D, CG>(v, rs, k, (int64_t)p * CL + kl, sj, pj);
   }
 }
 
