@@ -174,6 +174,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_tflops():
+    """Dense BF16 burst throughput of this part (cuBLAS, measured), else the earlier GB300 figure."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
 # ------------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -1079,6 +1089,15 @@ def run_contraction(dev, time_eager):
         Y = mm.fock_gemm(U5, Xk, mode).cpu().numpy()
         err = float(np.abs(Y - ref5).max() / np.abs(ref5).max())
         contraction[mode] = {"ms": tm, "tflops": flops / (tm * 1e-3) / 1e12, "max_rel_err_vs_fp64_cpu": err}
+    # the Ozaki split issues one real BF16 GEMM quadruple (U_re/U_im x X_re/X_im) per kept slice pair:
+    # 7 slices, pairs with p + q <= 8 -> 28 pairs
+    pairs = 7 * 8 // 2
+    peak, kind = measured_bf16_tflops()
+    issued = pairs * flops
+    contraction["ozaki"].update({"slice_pairs": pairs, "issued_bf16_flop": issued,
+                                 "issued_bf16_tflops_whole_call": issued / (contraction["ozaki"]["ms"] * 1e-3) / 1e12,
+                                 "bf16_peak_tflops": peak, "bf16_peak_kind": f"{kind} (burst)"})
+    contraction["ozaki"]["frac_of_bf16_peak_whole_call"] = contraction["ozaki"]["issued_bf16_tflops_whole_call"] / peak
     return contraction
 
 

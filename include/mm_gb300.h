@@ -261,10 +261,10 @@ MM_API int mm_ragged_vjp_copy_g(const mm_ragged_plan *plan, const mm_c128 *G, co
  * mrmustard/math/backend_manager.py:526-548).
  * mode MM_GEMM_FP64: native FP64 (DFMA).  mode MM_GEMM_FP64_DMMA: native FP64 on the
  * FP64 matrix-multiply instruction (mma.sync .f64).  mode MM_GEMM_OZAKI_BF16: FP64 values
- * split into `slices` (2..9) signed 6-bit slices per row of U / column of X,
- * slice products on the BF16 tensor cores with exact FP32 accumulation,
- * recombined through 64-bit integer sums and one FP64 scaling per slice order;
- * `slices` = 9 keeps 54 bits per operand.  ws: mm_fock_gemm_workspace_bytes
+ * split into `slices` (2..7) balanced 8-bit digits (each in [-128, 128]) per row
+ * of U / column of X, digit products on the BF16 tensor cores with exact FP32
+ * accumulation, recombined through integer sums and one FP64 scaling per slice
+ * order; `slices` = 7 keeps 55 bits per operand.  ws: mm_fock_gemm_workspace_bytes
  * (256 bytes for the two FP64 modes).
  */
 enum mm_gemm_mode { MM_GEMM_FP64 = 0, MM_GEMM_OZAKI_BF16 = 1, MM_GEMM_FP64_DMMA = 2 };

@@ -7,17 +7,19 @@
 //  * MM_GEMM_FP64: complex DFMA GEMM (4 FP64 FMA per complex multiply-add).
 //  * MM_GEMM_OZAKI_BF16: Ozaki-style split.  Each real and imaginary part of U
 //    (per row) and of X (per column) is scaled by a power of two 2^E so that
-//    |x| < 2^E, truncated to a 54-bit integer a = floor(|x| 2^(54-E)) and cut
-//    into S signed 6-bit slices s_p (a = sum_p s_p 2^(54-6p)), each an integer
-//    in [-63, 63] and therefore exact in BF16.  Slice products accumulate on the
-//    tensor cores in FP32, exactly (|s_p s_q| <= 3969 < 2^12, so 4096 terms stay
-//    below 2^24), and are flushed into 64-bit integer sums every 4096 terms.
+//    |x| < 2^E, truncated to a 55-bit integer a = floor(|x| 2^(55-E)) and
+//    written in S balanced base-256 digits s_p (a = sum_p s_p 2^(8(S-1-p)),
+//    every digit in [-128, 128]), each an integer exact in BF16.  Digit products
+//    accumulate on the tensor cores in FP32, exactly (|s_p s_q| <= 2^14, so 1024
+//    terms stay within 2^24), and are flushed into integer sums every 1024 terms.
 //    All pairs (p, q) with the same p + q = d share a scale, so they add up in
-//    the same integer sum; each group d = 2 .. S+1 is then scaled once by
-//    2^(E_row + F_col - 6d) and added in FP64.  Pairs with p + q > S + 1 are
-//    dropped (the Ozaki truncation); the slicing itself truncates below
-//    2^(E-54).  The only FP64 work is one conversion and one FMA per element
-//    and group, which matters on a part whose FP64 rate is 1/1000 of BF16.
+//    the same integer sum; group d = 2 .. S+1 carries the scale
+//    2^(E_row + F_col + 8(2S - d) - 110), so all groups of an element add up
+//    exactly in one 128-bit integer, rounded once to double.  Pairs with
+//    p + q > S + 1 are dropped (the Ozaki truncation: 28 of the 49 pairs kept at
+//    S = 7); the slicing itself truncates below 2^(E-55).  No step uses FP64
+//    arithmetic, which matters on a part whose FP64 rate is 1/1000 of BF16.
+#include <algorithm>
 #include <cstdint>
 #include <cstdlib>
 #include <mutex>
@@ -27,6 +29,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "i128_round.cuh"
 
 namespace {
 
@@ -187,8 +190,9 @@ __global__ void __launch_bounds__(128) zgemm_dmma_kernel(const double2* __restri
 }
 
 // ---------------------------------------------------------------- Ozaki split
-constexpr int OZ_BETA = 6;       // bits per slice
-constexpr int OZ_MAX_SLICES = 9;  // 54 bits
+constexpr int OZ_BETA = 8;        // bits per slice (balanced digits in [-128, 128])
+constexpr int OZ_MAX_SLICES = 7;  // digits of the 55-bit integer a
+constexpr int OZ_TOP = 55;        // a = floor(|x| 2^(OZ_TOP - E)) < 2^OZ_TOP
 constexpr int OZ_KALIGN = 64;     // Kp: K padded to a multiple of this (zeros)
 
 // x = (-1)^neg * mant * 2^ex with mant < 2^53; returns the exponent bound E(x)
@@ -200,24 +204,6 @@ __device__ __forceinline__ int exp_bound(double x) {
   if (e == 0 && frac == 0) return INT32_MIN;
   const int ex = e ? e - 1075 : -1074;
   return ex + 53;
-}
-
-// Row exponents of U (M x K): E[r] = max over the row's re and im of exp_bound.
-// Also sets every column exponent F[c] to INT32_MIN for col_exp_kernel's atomicMax.
-__global__ void __launch_bounds__(256) row_exp_kernel(const double2* __restrict__ U, int M, int K, int* __restrict__ E,
-                                                      int N, int* __restrict__ F) {
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int c = gtid; c < N; c += gridDim.x * blockDim.x) F[c] = INT32_MIN;
-  const int warp = gtid >> 5, lane = threadIdx.x & 31;
-  if (warp >= M) return;
-  int m = INT32_MIN;
-  for (int k = lane; k < K; k += 32) {
-    const double2 v = __ldg(U + (int64_t)warp * K + k);
-    m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (lane == 0) E[warp] = m;
 }
 
 // Column exponents of X (K x N): F[c] = max over the column.  CTA (x, y) covers
@@ -243,8 +229,13 @@ __global__ void __launch_bounds__(256) col_exp_kernel(const double2* __restrict_
   }
 }
 
-// Slices of one value against exponent bound E: out[p] for p < S.
-__device__ __forceinline__ void slice_value(double x, int E, int S, __nv_bfloat16* out, int64_t pstride) {
+// Digits of one value against exponent bound E: dig[p] for p < OZ_MAX_SLICES, the balanced
+// base-256 digits of a = floor(|x| 2^(OZ_TOP - E)) (digit 0 most significant), negated for x < 0.
+// Digits are taken from the least significant end; a digit of 128 or more becomes digit - 256
+// with a carry into the next one, so every digit lies in [-128, 127] and the top one
+// (a >> 48 < 128, plus a carry) in [0, 128].  Keeping only the S most significant digits
+// (S < OZ_MAX_SLICES) leaves a within half a unit of the last kept digit.
+__device__ __forceinline__ void value_digits(double x, int E, int (&dig)[OZ_MAX_SLICES]) {
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const int e = (int)((bits >> 52) & 0x7ff);
   const uint64_t frac = bits & ((1ull << 52) - 1);
@@ -253,104 +244,164 @@ __device__ __forceinline__ void slice_value(double x, int E, int S, __nv_bfloat1
   if (E != INT32_MIN && (e != 0 || frac != 0)) {
     const uint64_t mant = e ? (frac | (1ull << 52)) : frac;
     const int ex = e ? e - 1075 : -1074;
-    const int shift = ex + 54 - E;  // <= 1 because |x| < 2^E
+    const int shift = ex + OZ_TOP - E;  // <= 2 because |x| < 2^E
     if (shift >= 0) a = mant << shift;
     else if (shift > -64) a = mant >> (-shift);
   }
-  for (int p = 0; p < S; ++p) {
-    const int v = (int)((a >> (54 - OZ_BETA * (p + 1))) & ((1u << OZ_BETA) - 1));
-    out[p * pstride] = __float2bfloat16_rn((float)(neg ? -v : v));
+#pragma unroll
+  for (int p = OZ_MAX_SLICES - 1; p >= 1; --p) {
+    int v = (int)(a & 0xff);
+    a >>= 8;
+    if (v >= 128) {
+      v -= 256;
+      a += 1;
+    }
+    dig[p] = neg ? -v : v;
+  }
+  dig[0] = neg ? -(int)a : (int)a;
+}
+
+// Digits p < S of four consecutive values (of one plane row) as four BF16 (exact: |digit| <= 128)
+// packed into one 8-byte store per plane.
+__device__ __forceinline__ void store_digits4(const int (&d)[4][OZ_MAX_SLICES], int S, __nv_bfloat16* out,
+                                              int64_t pstride) {
+#pragma unroll
+  for (int p = 0; p < OZ_MAX_SLICES; ++p) {
+    if (p >= S) break;
+    uint2 w;
+    w.x = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)d[0][p])) |
+          ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)d[1][p])) << 16);
+    w.y = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)d[2][p])) |
+          ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)d[3][p])) << 16);
+    *reinterpret_cast<uint2*>(out + p * pstride) = w;
   }
 }
 
-// U (M x K) -> Us[p][comp][M][Kp] (comp 0 = re, 1 = im); zero padding for k >= K.
+// One CTA per row r of U (M x K): E[r] = max over the row's re and im of exp_bound, then the
+// row's slices Us[p][comp][r][0 .. Kp) (comp 0 = re, 1 = im; zeros for k >= K), four K values per
+// thread (the second pass reads the row from cache).  The CTAs also set every column exponent
+// F[c] to INT32_MIN for col_exp_kernel's atomicMax, which runs after this kernel.
 __global__ void __launch_bounds__(256) split_u_kernel(const double2* __restrict__ U, int M, int K, int Kp, int S,
-                                                      const int* __restrict__ E, __nv_bfloat16* __restrict__ Us) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (int64_t)M * Kp) return;
-  const int r = (int)(idx / Kp), k = (int)(idx - (int64_t)r * Kp);
+                                                      int* __restrict__ E, int N, int* __restrict__ F,
+                                                      __nv_bfloat16* __restrict__ Us) {
+  __shared__ int wmax[8];
+  const int r = blockIdx.x;
+  for (int c = r * 256 + (int)threadIdx.x; c < N; c += gridDim.x * 256) F[c] = INT32_MIN;
+  const double2* row = U + (int64_t)r * K;
+  int m = INT32_MIN;
+  for (int k = threadIdx.x; k < K; k += 256) {
+    const double2 v = __ldg(row + k);
+    m = max(m, max(exp_bound(v.x), exp_bound(v.y)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+  __syncthreads();
+  int Er = wmax[0];
+#pragma unroll
+  for (int w = 1; w < 8; ++w) Er = max(Er, wmax[w]);
+  if (threadIdx.x == 0) E[r] = Er;
   const int64_t plane = (int64_t)M * Kp;  // one (p, comp) plane
-  double2 v = cmk(0.0, 0.0);
-  if (k < K) v = __ldg(U + (int64_t)r * K + k);
-  const int Er = E[r];
-  slice_value(v.x, Er, S, Us + idx, 2 * plane);
-  slice_value(v.y, Er, S, Us + plane + idx, 2 * plane);
+  for (int k0 = 4 * (int)threadIdx.x; k0 < Kp; k0 += 1024) {
+    int dr[4][OZ_MAX_SLICES], di[4][OZ_MAX_SLICES];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double2 v = k0 + j < K ? __ldg(row + k0 + j) : cmk(0.0, 0.0);
+      value_digits(v.x, Er, dr[j]);
+      value_digits(v.y, Er, di[j]);
+    }
+    __nv_bfloat16* o = Us + (int64_t)r * Kp + k0;
+    store_digits4(dr, S, o, 2 * plane);
+    store_digits4(di, S, o + plane, 2 * plane);
+  }
 }
 
-// X (K x N) -> Xs[q][comp][N][Kp] (transposed: each column's K values contiguous).
+// X (K x N) -> Xs[q][comp][N][Kp] (transposed: each column's K values contiguous).  CTA (x, y):
+// 32 columns x 64 K values through shared memory, read along the rows of X, written along K
+// (four values per thread, one 8-byte store per plane).
 __global__ void __launch_bounds__(256) split_x_kernel(const double2* __restrict__ X, int K, int N, int Kp, int S,
                                                       const int* __restrict__ F, __nv_bfloat16* __restrict__ Xs) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (int64_t)N * Kp) return;
-  const int c = (int)(idx / Kp), k = (int)(idx - (int64_t)c * Kp);
+  __shared__ double2 tile[64][33];
+  const int lane = threadIdx.x & 31;
+  const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 64;
+  for (int rr = threadIdx.x >> 5; rr < 64; rr += 8) {
+    const int k = k0 + rr, c = c0 + lane;
+    tile[rr][lane] = (k < K && c < N) ? __ldg(X + (int64_t)k * N + c) : cmk(0.0, 0.0);
+  }
+  __syncthreads();
   const int64_t plane = (int64_t)N * Kp;
-  double2 v = cmk(0.0, 0.0);
-  if (k < K) v = __ldg(X + (int64_t)k * N + c);
-  const int Fc = F[c];
-  slice_value(v.x, Fc, S, Xs + idx, 2 * plane);
-  slice_value(v.y, Fc, S, Xs + plane + idx, 2 * plane);
-}
-
-// t * 2^s for an integer |t| < 2^53 as a double, built with integer operations only (exact: a
-// power-of-two scale of an exactly representable integer), so the FP64 pipe -- 1/64 rate on
-// this part -- is not spent on conversions and scalings.  Falls back to FP64 arithmetic when the
-// result would leave the normal range.
-__device__ __forceinline__ double pow2(int e);
-__device__ __forceinline__ double scaled_i2d(long long t, int s) {
-  if (t == 0) return 0.0;
-  const unsigned long long a = t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
-  const int e = 63 - __clzll((long long)a);  // a = 1.f * 2^e
-  const int ex = e + s + 1023;
-  if (e > 52 || ex <= 0 || ex >= 2047) return (double)t * pow2(s);
-  const unsigned long long mant = (a << (52 - e)) & ((1ull << 52) - 1);
-  return __longlong_as_double((long long)(((t < 0 ? 1ull : 0ull) << 63) | ((unsigned long long)ex << 52) | mant));
-}
-
-__device__ __forceinline__ double pow2(int e) {
-  if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
-  return ldexp(1.0, e);
+  for (int it = threadIdx.x; it < 32 * 16; it += 256) {
+    const int cl = it >> 4, kg = it & 15;  // 16 consecutive threads write one column's 64 K values
+    const int c = c0 + cl;
+    if (c >= N) continue;
+    const int Fc = F[c];
+    int dr[4][OZ_MAX_SLICES], di[4][OZ_MAX_SLICES];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double2 v = tile[kg * 4 + j][cl];
+      value_digits(v.x, Fc, dr[j]);
+      value_digits(v.y, Fc, di[j]);
+    }
+    __nv_bfloat16* o = Xs + (int64_t)c * Kp + k0 + kg * 4;
+    store_digits4(dr, S, o, 2 * plane);
+    store_digits4(di, S, o + plane, 2 * plane);
+  }
 }
 
 // ---------------------------------------------------------------- tcgen05 path
-// Warp-specialised Blackwell kernel for the slice products.  One CTA owns a
-// 128-row x 40-complex-column tile of Y (a 2500 x 256 product is 20 x 7 = 140
-// tiles: one wave on 152 SMs).  For every slice pair (p, q) and every chunk of
-// at most 4096 K values (one "unit"), the tensor cores compute two M = 128,
-// N = 80 products into TMEM:
-//     acc_r = U_re,p [X_re,q | X_im,q]   (columns 0..39: rr, 40..79: ri)
-//     acc_i = U_im,p [X_re,q | X_im,q]   (columns 0..39: ir, 40..79: ii)
-// The kernel is bound by the latency of its TMA ring (bytes in flight per SM),
-// not by L2 bandwidth: sharing the U tiles of a row of CTAs through cluster
-// multicast was measured and gained nothing, so every CTA loads its own.
-// with FP32 accumulation that is exact for 6-bit slices.  Roles:
-//   warp 0, lane 0: TMA producer (3-stage ring of [U_re | U_im | X_re ; X_im] K-blocks of 64),
+// Warp-specialised Blackwell kernel for the slice products.  Y is cut into tiles of
+// 128 rows x 128 complex columns.  The work of a tile is one unit per slice pair (p, q),
+// component (re or im of U) and chunk of at most TC_UNIT_K K values; in a unit the tensor
+// cores compute one M = 128, N = 256 product into TMEM:
+//     comp re: acc = U_re,p [X_re,q | X_im,q]   (columns 0..127: rr, 128..255: ri)
+//     comp im: acc = U_im,p [X_re,q | X_im,q]   (columns 0..127: ir, 128..255: ii)
+// with FP32 accumulation that is exact for digits of at most 128 in magnitude.  The units
+// of all tiles form one sequence (OzSeq: tile by tile; within a tile by slice order
+// d = p + q ascending, the pairs of an order alternating direction so that consecutive
+// units reuse U slices still in L2; then by component and K chunk), cut into contiguous runs
+// of equal numbers of K blocks, one per SM, so every SM works for the same time whatever the
+// number of tiles (a 2500 x 256 product has 40).  A CTA adds each finished unit, converted to
+// integers, to per-thread integer sums of its current tile and order (re += rr - ii,
+// im += ri + ir); when the tile or the order changes it adds them to that order's sums in
+// global memory with integer atomics (exact and order-independent: the result does not
+// depend on the schedule), and oz_recombine_kernel then forms each element from all orders.
+// The slice products are bound by the tensor cores' operand reads from shared memory (each
+// MMA reads its A and B tiles; measured on this part: M = N = 128 MMAs without any TMA
+// traffic reach ~60 % of the BF16 peak), so the MMAs use the widest N: 96 instead of 128
+// bytes read per MMA cycle.  Roles:
+//   warp 0, lane 0: TMA producer (4-stage ring of [U_comp | X_re ; X_im] K-blocks of 64),
 //   warp 1, lane 0: MMA issuer (tcgen05.mma, tcgen05.commit into mbarriers),
-//   warps 2..5:      epilogue (tcgen05.ld of a finished unit, exact integer sums per slice order,
-//                    one FP64 scaling per order into Y).
+//   warps 2..17:     epilogue, four warps per 32-lane TMEM quadrant (tcgen05.ld reaches only
+//                    the quadrant warp % 4), 32 of the 128 columns each.
 // Accumulators are double-buffered (TMEM columns 0 and 256) so the epilogue of one
 // unit overlaps the MMAs of the next.  Every mbarrier wait is bounded; on a
 // timeout the CTA records MM_ERR_WAIT_TIMEOUT, lets its in-flight copies land,
 // frees its TMEM and returns.
-constexpr int TC_BM = 128;                                // Y rows per CTA (MMA M)
-constexpr int TC_NC = 40;                                 // Y complex columns per CTA (MMA N = 80)
+constexpr int TC_BM = 128;                                // Y rows per tile (MMA M)
+constexpr int TC_NC = 128;                                // Y complex columns per tile (MMA N = 256)
 constexpr int TC_BK = 64;                                 // K per stage: one 128-byte swizzled row of BF16
-constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;             // 16 KB per U component
-constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 10 KB ([X_re; X_im] rows)
-constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + TC_B_BYTES;  // 42 KB (a multiple of 1 KB: swizzle atoms stay aligned)
-// Slice-order sums [comp][col][row]: int32 while 9 pairs x Kp x 2 x 63^2 < 2^31,
-// held in TMEM columns TC_T_COL.. (free between the two accumulator buffers), so
-// five stages fit in shared memory; int64 beyond, in shared memory (three stages).
-constexpr int TC_KP_INT32_MAX = 30000;
-// tbytes: bytes per shared-memory order sum (0: sums in TMEM)
-constexpr int tc_smem_bytes(int tbytes, int stages) {
-  return 1024 + stages * TC_STAGE_BYTES + 2 * TC_NC * TC_BM * tbytes + 256;
-}
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;             // 16 KB (one U component)
+constexpr int TC_B_BYTES = 2 * TC_NC * TC_BK * 2;         // 32 KB ([X_re; X_im] rows)
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;   // 48 KB (a multiple of 1 KB: swizzle atoms stay aligned)
+constexpr int TC_STAGES = 4;
+// K values per unit: 1024 products of at most 2^14 in magnitude keep every FP32 partial sum an
+// integer of at most 2^24 (exact).
+constexpr int TC_UNIT_K = 1024;
+constexpr int TC_UNIT_KB = TC_UNIT_K / TC_BK;
+static_assert(TC_UNIT_K * 128 * 128 <= (1 << 24), "exact FP32 unit sums");
+// Slice-order sums [tile][order][comp][col][row]: int32 while S pairs x 2 products x Kp x 2^14
+// < 2^31 (Kp <= 9362 at S = 7), int64 beyond.
+constexpr int TC_KP_INT32_MAX = 9344;
+static_assert((long long)OZ_MAX_SLICES * 2 * TC_KP_INT32_MAX * 128 * 128 < (1ll << 31), "int32 order sums");
+constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * TC_STAGE_BYTES + 256;
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_ACC_STRIDE = 256;                        // TMEM columns between the two accumulator buffers
-constexpr int TC_T_COL = 4 * TC_NC;                       // int32 order sums: [re cols | im cols] after buffer 0
-static_assert(TC_NC % 8 == 0 && 6 * TC_NC <= TC_ACC_STRIDE, "accumulator and order-sum layout");
+static_assert(2 * TC_NC <= TC_ACC_STRIDE, "accumulator layout");
 static_assert(TC_STAGE_BYTES % 1024 == 0 && (TC_B_BYTES / 2) % 1024 == 0, "swizzle atoms");
-constexpr int TC_THREADS = 192;
+constexpr int TC_EPI_WARPS = 16;
+constexpr int TC_EPI_COLS = TC_NC / 4;                    // complex columns per epilogue warp
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;
+constexpr int TC_TILE_SUMS = 2 * TC_NC * TC_BM;           // order-sum elements per tile and order
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 2 * TC_NC, M = 128.
 constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)((2 * TC_NC) >> 3) << 17) |
                               ((uint32_t)(128 >> 4) << 24);
@@ -420,73 +471,85 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t (&r)[8]) {
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                : "r"(taddr));
 }
-__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t (&r)[8]) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
-               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
-               : "memory");
-}
-__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Units of a CTA, in order: slice order d = 2 .. S+1; within an order the
-// pairs p in [max(1, d-S), min(S, d-1)], ascending for even d and descending
-// for odd d (consecutive units then reuse the U slices still in L2); K chunks
-// of at most 4096.  Every role walks the same sequence.
-struct UnitIter {
-  int S, nkb, chunk_kb;
-  int d, p, c;  // current unit
-  __device__ int plo() const { return d - S > 1 ? d - S : 1; }
-  __device__ int phi() const { return d - 1 < S ? d - 1 : S; }
-  __device__ bool desc() const { return (d & 1) != 0; }
-  __device__ void start(int S_, int nkb_, int chunk_kb_) {
-    S = S_;
-    nkb = nkb_;
-    chunk_kb = chunk_kb_;
-    d = 2;
-    p = 1;
-    c = 0;
+__device__ __forceinline__ void red_add(int* p, int v) {
+  if (v) atomicAdd(p, v);
+}
+__device__ __forceinline__ void red_add(long long* p, long long v) {
+  if (v) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+}
+
+// The unit sequence, shared by every role of every CTA and by the host's sizing.  The CTAs
+// form `lanes` lanes (lanes = the number of column tiles, or 1): lane l = b % lanes of CTA b
+// works on column tile l of every row tile, so the CTAs of one row of lanes read the same U
+// slices at the same time (once from DRAM, then from L2).  A lane's sequence runs over groups
+// g (row tiles; tiles when lanes = 1; tile t = g * lanes + l), pairs, components and K chunks:
+// unit i has pair index pj = i / (2 nch) (group pj / npairs), component (i / nch) % 2 and
+// chunk c = i % nch of the pair's nkb K blocks (all chunks but the last have TC_UNIT_KB
+// blocks).  Within a group the pairs run by order d = 2 .. S+1 (d - 1 pairs each), p ascending
+// for even d and descending for odd d.  Row r = b / lanes of CTAs takes the units whose first
+// K block lies in [r W, (r + 1) W), W = total_kb / nrows: contiguous runs of equal work.
+struct OzSeq {
+  int S, nkb, nch, npairs, n_ct, lanes, nrows;
+  long long nunits, total_kb;  // per lane
+  struct Unit {
+    long long t;
+    int d, p, comp, kb0, kb1;
+  };
+  __device__ long long prefix(long long i) const {
+    const long long sj = i / nch;  // (pair, component) index
+    return sj * nkb + (i - sj * nch) * TC_UNIT_KB;
   }
-  __device__ bool valid() const { return d <= S + 1; }
-  __device__ int q() const { return d - p; }
-  __device__ int kb_begin() const { return c * chunk_kb; }
-  __device__ int kb_end() const { return min(nkb, (c + 1) * chunk_kb); }
-  __device__ bool last_of_order() const { return p == (desc() ? plo() : phi()) && kb_end() >= nkb; }
-  __device__ void next() {
-    if (kb_end() < nkb) {
-      ++c;
-      return;
+  __device__ int row_of(long long i) const { return (int)(prefix(i) * nrows / total_kb); }
+  // smallest unit index i with row_of(i) >= r (nunits for r = nrows)
+  __device__ long long first_unit(int r) const {
+    long long lo = 0, hi = nunits;
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      if (row_of(mid) >= r) hi = mid;
+      else lo = mid + 1;
     }
-    c = 0;
-    if (desc() ? p > plo() : p < phi()) {
-      p += desc() ? -1 : 1;
-      return;
+    return lo;
+  }
+  __device__ Unit unit(long long i, int lane) const {
+    Unit u;
+    const long long sj = i / nch;
+    const int c = (int)(i - sj * nch);
+    const long long pj = sj >> 1;
+    u.comp = (int)(sj & 1);
+    const long long g = pj / npairs;
+    u.t = g * lanes + lane;
+    int j = (int)(pj - g * npairs);
+    int d = 2;
+    while (j >= d - 1) {
+      j -= d - 1;
+      ++d;
     }
-    ++d;
-    p = desc() ? phi() : plo();
+    u.d = d;
+    u.p = (d & 1) ? d - 1 - j : 1 + j;
+    u.kb0 = c * TC_UNIT_KB;
+    u.kb1 = min(nkb, u.kb0 + TC_UNIT_KB);
+    return u;
   }
 };
 
-// TT: type of the slice-order sums; TMEM_T: they live in TMEM (int32 only).
-template <typename TT, int TC_STAGES, bool TMEM_T>
+// TT: type of the slice-order sums in global memory (int or long long).
+template <typename TT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ CUtensorMap tmap_x,
-                    const int* __restrict__ E, const int* __restrict__ F, double2* __restrict__ Y, int M, int N,
-                    int Kp, int S, mm::WsHeader* h, uint64_t budget_ns) {
+                    TT* __restrict__ sums, OzSeq seq, int M, int N, mm::WsHeader* h, uint64_t budget_ns) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* stages = smem;
-  static_assert(!TMEM_T || sizeof(TT) == 4, "TMEM sums are 32-bit");
-  constexpr int t_bytes = TMEM_T ? 0 : 2 * TC_NC * TC_BM * (int)sizeof(TT);
-  TT* T = reinterpret_cast<TT*>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][TC_NC][TC_BM] (shared-memory sums)
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES + t_bytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE_BYTES);
   // bars: full[STAGES], empty[STAGES], accf[2], acce[2], drain
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_NC;
-  const int nkb = Kp / TC_BK;
-  const int chunk_kb = 4096 / TC_BK;
+  const int lane_id = (int)blockIdx.x % seq.lanes, crow = (int)blockIdx.x / seq.lanes;
+  const long long i_lo = seq.first_unit(crow), i_hi = seq.first_unit(crow + 1);
   auto full = [&](int s) { return smem_u32(bars + s); };
   auto empty = [&](int s) { return smem_u32(bars + TC_STAGES + s); };
   auto accf = [&](int b) { return smem_u32(bars + 2 * TC_STAGES + b); };
@@ -500,7 +563,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(accf(b), 1);
-      mbar_init(acce(b), 128);
+      mbar_init(acce(b), 32 * TC_EPI_WARPS);
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -524,12 +587,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t armed_parity[TC_STAGES];
     bool armed[TC_STAGES];
     for (int s = 0; s < TC_STAGES; ++s) armed[s] = false;
-    UnitIter u;
-    u.start(S, nkb, chunk_kb);
     bool ok = true;
-    for (; ok && u.valid(); u.next()) {
-      const int yu = (u.p - 1) * 2 * M + m0, yx = (u.q() - 1) * 2 * N + n0;
-      for (int kb = u.kb_begin(); kb < u.kb_end(); ++kb) {
+    for (long long i = i_lo; ok && i < i_hi; ++i) {
+      const OzSeq::Unit u = seq.unit(i, lane_id);
+      const int m0 = (int)(u.t / seq.n_ct) * TC_BM, n0 = (int)(u.t % seq.n_ct) * TC_NC;
+      const int yu = ((u.p - 1) * 2 + u.comp) * M + m0, yx = (u.d - u.p - 1) * 2 * N + n0;
+      for (int kb = u.kb0; kb < u.kb1; ++kb) {
         if (!mbar_wait(empty(stage), phase ^ 1, abort_flag, h, budget_ns)) {
           ok = false;
           break;
@@ -540,9 +603,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         armed_parity[stage] = phase;
         const int x = kb * TC_BK;
         tma_load_2d(smem_u32(st), &tmap_u, x, yu, full(stage));
-        tma_load_2d(smem_u32(st + TC_A_BYTES), &tmap_u, x, yu + M, full(stage));
-        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), &tmap_x, x, yx, full(stage));
-        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + TC_B_BYTES / 2), &tmap_x, x, yx + N, full(stage));
+        tma_load_2d(smem_u32(st + TC_A_BYTES), &tmap_x, x, yx, full(stage));
+        tma_load_2d(smem_u32(st + TC_A_BYTES + TC_B_BYTES / 2), &tmap_x, x, yx + N, full(stage));
         if (++stage == TC_STAGES) {
           stage = 0;
           phase ^= 1;
@@ -563,14 +625,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t phase = 0;
     int abuf = 0;
     uint32_t aphase = 0;
-    UnitIter u;
-    u.start(S, nkb, chunk_kb);
     bool ok = true;
-    for (; ok && u.valid(); u.next()) {
+    for (long long i = i_lo; ok && i < i_hi; ++i) {
+      const OzSeq::Unit u = seq.unit(i, lane_id);
       if (!mbar_wait(acce(abuf), aphase ^ 1, abort_flag, h, budget_ns)) break;
       tc_fence_after();
-      const uint32_t d_r = tmem + (uint32_t)(abuf * TC_ACC_STRIDE), d_i = d_r + 2 * TC_NC;
-      for (int kb = u.kb_begin(); kb < u.kb_end(); ++kb) {
+      const uint32_t dacc = tmem + (uint32_t)(abuf * TC_ACC_STRIDE);
+      for (int kb = u.kb0; kb < u.kb1; ++kb) {
         if (!mbar_wait(full(stage), phase, abort_flag, h, budget_ns)) {
           ok = false;
           break;
@@ -580,10 +641,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int k16 = 0; k16 < TC_BK / 16; ++k16) {
           const uint32_t koff = (uint32_t)k16 * 32;
-          const uint32_t acc = (kb > u.kb_begin() || k16 > 0) ? 1u : 0u;
-          const uint64_t bdesc = sw128_desc(st + 2 * TC_A_BYTES + koff);
-          tc_mma(d_r, sw128_desc(st + koff), bdesc, acc);
-          tc_mma(d_i, sw128_desc(st + TC_A_BYTES + koff), bdesc, acc);
+          const uint32_t acc = (kb > u.kb0 || k16 > 0) ? 1u : 0u;
+          tc_mma(dacc, sw128_desc(st + koff), sw128_desc(st + TC_A_BYTES + koff), acc);
         }
         tc_commit(empty(stage));  // frees the stage once these MMAs have read it
         if (++stage == TC_STAGES) {
@@ -607,117 +666,55 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ------------------------------------------------------------ epilogue
     const int lane_base = 32 * (warp & 3);
     const int row = lane_base + lane;
-    const int gm = m0 + row;
+    const int c0 = TC_EPI_COLS * ((warp - 2) >> 2);  // this warp's first complex column of the tile
     const uint32_t trow = tmem + ((uint32_t)lane_base << 16);  // this warp's 32 TMEM lanes
-    const uint32_t zeros[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-    if constexpr (TMEM_T) {
+    TT sre[TC_EPI_COLS], sim[TC_EPI_COLS];
 #pragma unroll
-      for (int c8 = 0; c8 < 2 * TC_NC / 8; ++c8) tc_st8(trow + TC_T_COL + c8 * 8, zeros);
-      tc_wait_st();
-    } else {
-      for (int c = 0; c < TC_NC; ++c) T[(0 * TC_NC + c) * TC_BM + row] = T[(1 * TC_NC + c) * TC_BM + row] = 0;
-    }
+    for (int j = 0; j < TC_EPI_COLS; ++j) sre[j] = sim[j] = 0;
     int abuf = 0;
     uint32_t aphase = 0;
-    UnitIter u;
-    u.start(S, nkb, chunk_kb);
-    for (; u.valid(); u.next()) {
+    for (long long i = i_lo; i < i_hi; ++i) {
+      const OzSeq::Unit u = seq.unit(i, lane_id);
       // one lane waits, the warp follows it, so the warp-wide tcgen05.ld stays convergent
       int okw = lane == 0 ? (int)mbar_wait(accf(abuf), aphase, abort_flag, h, budget_ns) : 0;
       okw = __shfl_sync(0xffffffffu, okw, 0);
       if (!okw) break;
       tc_fence_after();
-      const uint32_t base = trow + (uint32_t)(abuf * TC_ACC_STRIDE);
+      const uint32_t base = trow + (uint32_t)(abuf * TC_ACC_STRIDE) + (uint32_t)c0;
+      // comp re: columns [rr | ri] -> re += rr, im += ri;  comp im: [ir | ii] -> re -= ii, im += ir
+      const bool cre = u.comp == 0;
 #pragma unroll
-      for (int c8 = 0; c8 < TC_NC / 8; ++c8) {
-        uint32_t rr[8], ri[8], ir[8], ii[8], tr[8], ti[8];
-        tc_ld8(base + c8 * 8, rr);
-        tc_ld8(base + TC_NC + c8 * 8, ri);
-        tc_ld8(base + 2 * TC_NC + c8 * 8, ir);
-        tc_ld8(base + 3 * TC_NC + c8 * 8, ii);
-        if constexpr (TMEM_T) {
-          tc_ld8(trow + TC_T_COL + c8 * 8, tr);
-          tc_ld8(trow + TC_T_COL + TC_NC + c8 * 8, ti);
-        }
+      for (int c8 = 0; c8 < TC_EPI_COLS / 8; ++c8) {
+        uint32_t a0[8], a1[8];
+        tc_ld8(base + c8 * 8, a0);
+        tc_ld8(base + TC_NC + c8 * 8, a1);
         tc_wait_ld();
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const int c = c8 * 8 + j;
-          const TT re = (TT)__float2int_rn(__uint_as_float(rr[j])) - (TT)__float2int_rn(__uint_as_float(ii[j]));
-          const TT im = (TT)__float2int_rn(__uint_as_float(ri[j])) + (TT)__float2int_rn(__uint_as_float(ir[j]));
-          if constexpr (TMEM_T) {
-            tr[j] = (uint32_t)((int)tr[j] + (int)re);
-            ti[j] = (uint32_t)((int)ti[j] + (int)im);
-          } else {
-            T[(0 * TC_NC + c) * TC_BM + row] += re;
-            T[(1 * TC_NC + c) * TC_BM + row] += im;
-          }
-        }
-        if constexpr (TMEM_T) {
-          tc_st8(trow + TC_T_COL + c8 * 8, tr);
-          tc_st8(trow + TC_T_COL + TC_NC + c8 * 8, ti);
+          const TT x0 = (TT)__float2int_rn(__uint_as_float(a0[j])), x1 = (TT)__float2int_rn(__uint_as_float(a1[j]));
+          sre[c8 * 8 + j] += cre ? x0 : -x1;
+          sim[c8 * 8 + j] += cre ? x1 : x0;
         }
       }
-      if constexpr (TMEM_T) tc_wait_st();
       tc_fence_before();
       mbar_arrive(acce(abuf));
       if (++abuf == 2) {
         abuf = 0;
         aphase ^= 1;
       }
-      if (u.last_of_order()) {  // add this slice order's sums to Y in FP64, then clear them
-        const int er = gm < M ? E[gm] : INT32_MIN;
+      bool flush = i + 1 >= i_hi;
+      if (!flush) {
+        const OzSeq::Unit v = seq.unit(i + 1, lane_id);
+        flush = v.t != u.t || v.d != u.d;
+      }
+      if (flush) {  // this tile's and order's share of the sums: [tile][d - 2][comp][col][row]
+        TT* s = sums + (u.t * seq.S + (u.d - 2)) * (long long)TC_TILE_SUMS + (long long)c0 * TC_BM + row;
 #pragma unroll
-        for (int c8 = 0; c8 < TC_NC / 8; ++c8) {
-          long long vre[8], vim[8];
-          if constexpr (TMEM_T) {
-            uint32_t tr[8], ti[8];
-            tc_ld8(trow + TC_T_COL + c8 * 8, tr);
-            tc_ld8(trow + TC_T_COL + TC_NC + c8 * 8, ti);
-            tc_wait_ld();
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              vre[j] = (int)tr[j];
-              vim[j] = (int)ti[j];
-            }
-            tc_st8(trow + TC_T_COL + c8 * 8, zeros);
-            tc_st8(trow + TC_T_COL + TC_NC + c8 * 8, zeros);
-          } else {
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              TT& tre = T[(0 * TC_NC + c8 * 8 + j) * TC_BM + row];
-              TT& tim = T[(1 * TC_NC + c8 * 8 + j) * TC_BM + row];
-              vre[j] = (long long)tre;
-              vim[j] = (long long)tim;
-              tre = 0;
-              tim = 0;
-            }
-          }
-          // every load of the group is issued before its stores, so the read-modify-writes of a row
-          // overlap instead of forming one chain of memory latencies
-          double2 y[8], o[8];
-          double2* yrow = Y + (int64_t)gm * N + n0 + c8 * 8;
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int gn = n0 + c8 * 8 + j;
-            y[j] = cmk(0.0, 0.0);
-            o[j] = cmk(0.0, 0.0);
-            if (gm < M && gn < N) {
-              const int fc = F[gn];
-              if (er != INT32_MIN && fc != INT32_MIN) {
-                const int sh = er + fc - OZ_BETA * u.d;
-                y[j] = cmk(scaled_i2d(vre[j], sh), scaled_i2d(vim[j], sh));
-              }
-              if (u.d != 2) o[j] = yrow[j];
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int gn = n0 + c8 * 8 + j;
-            if (gm < M && gn < N) yrow[j] = u.d == 2 ? y[j] : cmk(o[j].x + y[j].x, o[j].y + y[j].y);
-          }
+        for (int j = 0; j < TC_EPI_COLS; ++j) {
+          red_add(s + j * TC_BM, sre[j]);
+          red_add(s + TC_NC * TC_BM + j * TC_BM, sim[j]);
+          sre[j] = sim[j] = 0;
         }
-        if constexpr (TMEM_T) tc_wait_st();
       }
     }
   }
@@ -729,20 +726,77 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
 }
 
+// Y[m][n] = sum over orders d = 2 .. S+1 of the order's integer sums scaled by
+// 2^(E_m + F_n + 8(2 OZ_MAX_SLICES - d) - 2 OZ_TOP), formed exactly in 128-bit integers and
+// rounded once to double (no FP64 arithmetic: 1/64 rate on this part).  CTA:
+// 128 rows x 8 columns of one tile; the sums are read along rows (their layout), the results
+// staged in shared memory and written along the rows of Y.
+constexpr int RC_COLS = 8;
+template <typename TT>
+__global__ void __launch_bounds__(256) oz_recombine_kernel(const TT* __restrict__ sums, const int* __restrict__ E,
+                                                           const int* __restrict__ F, double2* __restrict__ Y, int M,
+                                                           int N, int S, int n_ct) {
+  __shared__ double2 ys[RC_COLS][TC_BM + 1];
+  const long long t = blockIdx.x / (TC_NC / RC_COLS);
+  const int cb = (int)(blockIdx.x % (TC_NC / RC_COLS)) * RC_COLS;
+  const int m0 = (int)(t / n_ct) * TC_BM, n0 = (int)(t % n_ct) * TC_NC + cb;
+  const int rl = threadIdx.x & (TC_BM - 1), cg = threadIdx.x >> 7;  // two column groups of 4
+  const int m = m0 + rl;
+  const int er = m < M ? E[m] : INT32_MIN;
+#pragma unroll
+  for (int j = 0; j < RC_COLS / 2; ++j) {
+    const int cl = cb + cg * (RC_COLS / 2) + j, n = n0 + cg * (RC_COLS / 2) + j;
+    const int fc = n < N ? F[n] : INT32_MIN;
+    double2 y = cmk(0.0, 0.0);
+    if (er != INT32_MIN && fc != INT32_MIN) {
+      // exact sum of all orders as one 128-bit integer in units of the last order's scale
+      // (|sum| < 2^50 per order times at most 2^48), then one rounding to double
+      const TT* s = sums + t * S * (long long)TC_TILE_SUMS + (long long)cl * TC_BM + rl;
+      long long vre[OZ_MAX_SLICES], vim[OZ_MAX_SLICES];
+#pragma unroll
+      for (int o = 0; o < OZ_MAX_SLICES; ++o) {  // every load issued before the first use
+        vre[o] = o < S ? (long long)s[(long long)o * TC_TILE_SUMS] : 0;
+        vim[o] = o < S ? (long long)s[(long long)o * TC_TILE_SUMS + TC_NC * TC_BM] : 0;
+      }
+      unsigned __int128 are = 0, aim = 0;
+#pragma unroll
+      for (int o = 0; o < OZ_MAX_SLICES; ++o) {  // order d = o + 2
+        if (o < S) {
+          const int w = OZ_BETA * (S - 1 - o);
+          are += (unsigned __int128)(__int128)vre[o] << w;
+          aim += (unsigned __int128)(__int128)vim[o] << w;
+        }
+      }
+      const int sh = er + fc + OZ_BETA * (2 * OZ_MAX_SLICES - (S + 1)) - 2 * OZ_TOP;
+      y = cmk(mm::i128_scaled_to_double((__int128)are, sh), mm::i128_scaled_to_double((__int128)aim, sh));
+    }
+    ys[cg * (RC_COLS / 2) + j][rl] = y;
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < TC_BM * RC_COLS; it += 256) {
+    const int r = it / RC_COLS, c = it % RC_COLS;
+    if (m0 + r < M && n0 + c < N) Y[(int64_t)(m0 + r) * N + n0 + c] = ys[c][r];
+  }
+}
+
 }  // namespace
 
 namespace {
 int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
 struct OzLayout {
-  int64_t Kp = 0;
-  size_t us = 0, xs = 0, e = 0, f = 0, total = 0;
+  int64_t Kp = 0, n_rt = 0, n_ct = 0;
+  bool sums64 = false;  // slice-order sums in int64 (Kp beyond the int32 bound)
+  size_t us = 0, xs = 0, e = 0, f = 0, sums = 0, sums_bytes = 0, total = 0;
 };
 
-// Workspace: 512-byte status header, U slices, X slices, row / column exponents.
+// Workspace: 512-byte status header, U slices, X slices, row / column exponents, slice-order sums.
 OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int S) {
   OzLayout L;
   L.Kp = round_up(K, OZ_KALIGN);
+  L.n_rt = (M + TC_BM - 1) / TC_BM;
+  L.n_ct = (N + TC_NC - 1) / TC_NC;
+  L.sums64 = L.Kp > TC_KP_INT32_MAX;
   size_t off = sizeof(mm::WsHeader);
   L.us = off;
   off = round_up(off + (size_t)S * 2 * M * L.Kp * sizeof(__nv_bfloat16), 256);
@@ -752,8 +806,29 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int S) {
   off = round_up(off + (size_t)M * sizeof(int), 256);
   L.f = off;
   off = round_up(off + (size_t)N * sizeof(int), 256);
+  L.sums = off;
+  L.sums_bytes = (size_t)(L.n_rt * L.n_ct) * S * TC_TILE_SUMS * (L.sums64 ? sizeof(long long) : sizeof(int));
+  off = round_up(off + L.sums_bytes, 256);
   L.total = off;
   return L;
+}
+
+int sm_count() {
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 1;
+  }
+  if (cache[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+      cudaGetLastError();
+      n = 1;
+    }
+    cache[dev] = n;
+  }
+  return cache[dev];
 }
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -834,32 +909,51 @@ MM_API int mm_fock_gemm(int mode, int64_t M, int64_t N, int64_t K, const mm_c128
   int* E = reinterpret_cast<int*>(w + L.e);
   int* F = reinterpret_cast<int*>(w + L.f);
   const int Kp = (int)L.Kp;
-  row_exp_kernel<<<(unsigned)((M * 32 + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, E, (int)N, F);
+  split_u_kernel<<<(unsigned)M, 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, (int)N, F, Us);
   col_exp_kernel<<<dim3((unsigned)((N + 31) / 32), (unsigned)((K + COL_EXP_ROWS - 1) / COL_EXP_ROWS)), 256, 0, st>>>(
       (const double2*)X, (int)K, (int)N, F);
-  split_u_kernel<<<(unsigned)((M * Kp + 255) / 256), 256, 0, st>>>((const double2*)U, (int)M, (int)K, Kp, slices, E, Us);
-  split_x_kernel<<<(unsigned)((N * Kp + 255) / 256), 256, 0, st>>>((const double2*)X, (int)K, (int)N, Kp, slices, F, Xs);
+  split_x_kernel<<<dim3((unsigned)((N + 31) / 32), (unsigned)(Kp / 64)), 256, 0, st>>>((const double2*)X, (int)K,
+                                                                                     (int)N, Kp, slices, F, Xs);
   CUtensorMap tu, tx;
   if (!make_map(&tu, Us, (uint64_t)slices * 2 * M, (uint64_t)Kp, TC_BM) ||
       !make_map(&tx, Xs, (uint64_t)slices * 2 * N, (uint64_t)Kp, TC_NC))
     return MM_ERR_UNSUPPORTED;
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(ozaki_tc_kernel<int, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         tc_smem_bytes(0, 5));
-    cudaFuncSetAttribute(ozaki_tc_kernel<long long, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         tc_smem_bytes(8, 3));
+    cudaFuncSetAttribute(ozaki_tc_kernel<int>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
+    cudaFuncSetAttribute(ozaki_tc_kernel<long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
   });
-  dim3 grid((unsigned)((N + TC_NC - 1) / TC_NC), (unsigned)((M + TC_BM - 1) / TC_BM));
-  if (grid.y > 65535) return MM_ERR_TOO_LARGE;
+  OzSeq seq;
+  seq.S = slices;
+  seq.nkb = (int)(Kp / TC_BK);
+  seq.nch = (seq.nkb + TC_UNIT_KB - 1) / TC_UNIT_KB;
+  seq.npairs = slices * (slices + 1) / 2;
+  seq.n_ct = (int)L.n_ct;
+  const long long ntiles = L.n_rt * L.n_ct;
+  // one lane per column tile when the SMs divide into rows of lanes with little left over
+  const int sms = sm_count();
+  seq.lanes = (L.n_ct <= sms && (sms % L.n_ct) * 16 <= sms) ? (int)L.n_ct : 1;
+  const long long groups = ntiles / seq.lanes;
+  seq.nunits = groups * seq.npairs * 2 * seq.nch;
+  seq.total_kb = groups * seq.npairs * 2 * seq.nkb;
+  seq.nrows = (int)std::min<long long>(sms / seq.lanes, seq.nunits);
+  const int ncta = seq.nrows * seq.lanes;
   mm::WsHeader* h = reinterpret_cast<mm::WsHeader*>(w);
-  if (Kp <= TC_KP_INT32_MAX)
-    ozaki_tc_kernel<int, 5, true><<<grid, TC_THREADS, tc_smem_bytes(0, 5), st>>>(
-        tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices, h, tc_budget_ns());
-  else
-    ozaki_tc_kernel<long long, 3, false><<<grid, TC_THREADS, tc_smem_bytes(8, 3), st>>>(
-        tu, tx, E, F, (double2*)Y, (int)M, (int)N, Kp, slices, h, tc_budget_ns());
-  mm::note_launches(5);  // exponents, slices, products
+  if (cudaMemsetAsync(w + L.sums, 0, L.sums_bytes, st) != cudaSuccess) return MM_ERR_CUDA;
+  const unsigned rgrid = (unsigned)(ntiles * (TC_NC / RC_COLS));
+  if (L.sums64) {
+    long long* sums = reinterpret_cast<long long*>(w + L.sums);
+    ozaki_tc_kernel<long long><<<ncta, TC_THREADS, TC_SMEM_BYTES, st>>>(tu, tx, sums, seq, (int)M, (int)N, h,
+                                                                           tc_budget_ns());
+    oz_recombine_kernel<long long><<<rgrid, 256, 0, st>>>(sums, E, F, (double2*)Y, (int)M, (int)N, slices,
+                                                          (int)L.n_ct);
+  } else {
+    int* sums = reinterpret_cast<int*>(w + L.sums);
+    ozaki_tc_kernel<int><<<ncta, TC_THREADS, TC_SMEM_BYTES, st>>>(tu, tx, sums, seq, (int)M, (int)N, h,
+                                                                     tc_budget_ns());
+    oz_recombine_kernel<int><<<rgrid, 256, 0, st>>>(sums, E, F, (double2*)Y, (int)M, (int)N, slices, (int)L.n_ct);
+  }
+  mm::note_launches(5);  // row exponents and U slices, column exponents, X slices, products, recombination
   return cudaGetLastError() == cudaSuccess ? MM_OK : MM_ERR_CUDA;
 }
 

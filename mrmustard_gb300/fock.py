@@ -26,7 +26,7 @@ __all__ = ["fock_gemm", "apply_unitary"]
 _MODES = {"fp64": 0, "ozaki": 1, "ozaki_bf16": 1, "dmma": 2, "fp64_dmma": 2}
 
 
-def fock_gemm(U, X, mode: str = "fp64", slices: int = 9, out=None):
+def fock_gemm(U, X, mode: str = "fp64", slices: int = 7, out=None):
     """Y = U @ X for complex128 matrices (numpy in -> numpy out, CUDA tensors stay on device)."""
     lib = _lib.load()
     if mode not in _MODES:
@@ -56,7 +56,7 @@ def fock_gemm(U, X, mode: str = "fp64", slices: int = 9, out=None):
     return Y if dev_mode else Y.cpu().numpy()
 
 
-def apply_unitary(U, kets, mode: str = "fp64", slices: int = 9):
+def apply_unitary(U, kets, mode: str = "fp64", slices: int = 7):
     """Apply an n-mode gate Fock tensor U (out..., in...) to kets (batch, in...) -> (batch, out...)."""
     Ut = U if isinstance(U, torch.Tensor) else np.asarray(U)
     nin = kets.ndim - 1

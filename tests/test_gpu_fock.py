@@ -1,9 +1,9 @@
 """GPU parity of the Fock contraction (FP64 DFMA, FP64 MMA and Ozaki-split BF16 paths) against the
 FP64 CPU oracle (numpy @ -> BLAS zgemm, the arithmetic ArrayAnsatz.contract reaches through einsum).
 
-Error metric: max|Y - Y_ref| / max|Y_ref|.  FP64 kernels (DFMA and MMA): 1e-14.  Ozaki split with 9 slices
-(54 bits per operand, pairs with slice order <= 10): 1e-13; fewer slices give coarser results
-(checked to shrink monotonically)."""
+Error metric: max|Y - Y_ref| / max|Y_ref|.  FP64 kernels (DFMA and MMA): 1e-14.  Ozaki split with 7 slices
+(balanced 8-bit digits, 55 bits per operand, pairs with slice order <= 8): 1e-13; fewer slices give coarser
+results (checked to shrink monotonically)."""
 
 from __future__ import annotations
 
@@ -26,15 +26,19 @@ def cn(shape, seed):
     return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
 
 
-# (40, 300, 64): N spans several 40-column tiles with a ragged last one; K = 30100 takes the int64
-# slice-order sums (K padded beyond 30000), every other case the int32 ones.
+# (40, 300, 64): N spans several 40-column tiles with a ragged last one; K = 9345 and 30100 take the
+# int64 slice-order sums (K padded beyond 9344), K = 9344 the int32 ones at their bound, as every other
+# case; K = 1025 and 4200 end in a partial 1024-value unit.
 @pytest.mark.parametrize("M,N,K", [(1, 1, 1), (37, 5, 300), (300, 64, 200), (129, 33, 4200), (40, 300, 64),
-                                   (24, 12, 30100)])
+                                   (70, 41, 1025), (20, 9, 9344), (20, 9, 9345), (24, 12, 30100)])
 def test_gemm_random(cuda, oracle_lib, M, N, K):
     U, X = cn((M, K), M + K), cn((K, N), N)
     ref = oracle_lib.fock_gemm(U, X)
-    assert rel(mm.fock_gemm(U, X, "fp64"), ref) < 1e-14
-    assert rel(mm.fock_gemm(U, X, "dmma"), ref) < 1e-14
+    # FP64 sums of K random products (the kernels' and BLAS's, in different orders) drift apart like
+    # sqrt(K) unit roundoffs: 1e-14 up to K ~ 500, 2^-52 sqrt(K) beyond
+    tol64 = max(1e-14, 2.0 ** -52 * np.sqrt(K))
+    assert rel(mm.fock_gemm(U, X, "fp64"), ref) < tol64
+    assert rel(mm.fock_gemm(U, X, "dmma"), ref) < tol64
     assert rel(mm.fock_gemm(U, X, "ozaki"), ref) < 1e-13
 
 
@@ -55,7 +59,7 @@ def test_gemm_wide_dynamic_range(cuda, oracle_lib):
 def test_gemm_slices_converge(cuda, oracle_lib):
     U, X = cn((64, 512), 8), cn((512, 32), 9)
     ref = oracle_lib.fock_gemm(U, X)
-    errs = [rel(mm.fock_gemm(U, X, "ozaki", slices=s), ref) for s in (2, 4, 6, 9)]
+    errs = [rel(mm.fock_gemm(U, X, "ozaki", slices=s), ref) for s in (2, 3, 5, 7)]
     assert errs[0] > errs[1] > errs[2] >= errs[3]
     assert errs[3] < 1e-13
 
