@@ -215,6 +215,23 @@ def test_single_instance_cluster_shapes(cuda, oracle_lib, shape):
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
 
 
+# A single large instance whose slab 0 (k_0 = 0) fits the one-cluster kernel runs in two phases:
+# slab 0 as the triple (A[1:, 1:], b[1:], c) on one cluster, then level 0 alone over every SM.
+# Corners: the benchmark's 4 x 40 and 4 x 30 states, a cutoff-50 slab (2500 amplitudes, 16 CTAs), a
+# slab of one level-0 chunk (extent 1 on axis 1), D = 3, 6, a slab of 2560 amplitudes.
+SLAB0_SHAPES = [(6, 40, 40, 40), (30, 30, 30, 30), (3, 50, 50, 50), (5, 3, 1000), (2, 2, 2560),
+                (4, 8, 8, 8, 8, 6), (40, 1, 40, 40)]
+
+
+@pytest.mark.parametrize("shape", SLAB0_SHAPES)
+def test_single_instance_slab0_shapes(cuda, oracle_lib, shape):
+    A, b, _ = takagi(len(shape), 0.8, 700 + sum(shape))
+    c = 0.9 + 0.3j
+    Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
+                       torch.tensor(c, dtype=torch.complex128, device=cuda), shape)
+    assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
+
+
 _FORCED = """
 import sys, numpy as np, torch
 sys.path.insert(0, {root!r})
@@ -231,16 +248,17 @@ np.savez({path!r}, **out)
 
 
 @pytest.mark.parametrize("env", [{"MM_CLUSTER_FWD": "0"}, {"MM_CLUSTER_CTAS": "1"}, {"MM_CLUSTER_CTAS": "3"},
-                                 {"MM_CLUSTER_CTAS": "16"}])
+                                 {"MM_CLUSTER_CTAS": "16"}, {"MM_FLOW_SLAB0": "0"}])
 def test_single_instance_forced_schedules(cuda, oracle_lib, tmp_path, env):
-    """The same instances with the cluster kernel off (grid-wide dataflow kernel instead) and with
-    fixed cluster sizes (schedule knobs are read once per process, so each runs in a child)."""
+    """The same instances with the cluster kernel off (grid-wide dataflow kernel instead), with
+    fixed cluster sizes and with the two-phase large-instance forward off (schedule knobs are read
+    once per process, so each runs in a child)."""
     import os
     import subprocess
     import sys
     from pathlib import Path
 
-    shapes = [(20, 20, 20), (8, 2560), (2, 30, 30), (1024,), (40, 400)]
+    shapes = [(20, 20, 20), (8, 2560), (2, 30, 30), (1024,), (40, 400), (6, 40, 40, 40), (5, 3, 1000)]
     root = str(Path(__file__).resolve().parent.parent)
     path = str(tmp_path / "forced.npz")
     code = _FORCED.format(root=root, shapes=shapes, path=path)
