@@ -253,9 +253,11 @@ int launch_setup(const Src& src, int64_t n_inst, char* ws, const Layout& L, int 
 // and MM_FLOW_EXCLUSIVE in the environment override the defaults.
 // slab0: compute slab 0 (every amplitude with k_0 = 0, levels 1 .. D-1) first, as its own
 // instance (A[1:, 1:], b[1:], c) on one thread-block cluster (fwd_cluster_kernel), then level 0
-// alone on every SM (MM_FLOW_SLAB0=0: the one-launch dataflow over all levels).
+// alone on every SM (MM_FLOW_SLAB0=0: the one-launch dataflow over all levels).  poll: level 0
+// then polls its halo amplitudes in G (pre-filled with kPendingBits) instead of waiting on
+// progress words (MM_FLOW_POLL=0: progress words).
 struct FlowTuning {
-  int block = kFlowBlock, per_sm = kFlowPerSm, exclusive = 1, slab0 = 1;
+  int block = kFlowBlock, per_sm = kFlowPerSm, exclusive = 1, slab0 = 1, poll = 1;
   uint32_t min_amps = kFlowMinAmps;
 };
 
@@ -267,6 +269,7 @@ FlowTuning flow_tuning() {
     if (const char* e = getenv("MM_FLOW_MIN_AMPS")) r.min_amps = (uint32_t)std::max(2, atoi(e));
     if (const char* e = getenv("MM_FLOW_EXCLUSIVE")) r.exclusive = atoi(e) != 0;
     if (const char* e = getenv("MM_FLOW_SLAB0")) r.slab0 = atoi(e) != 0;
+    if (const char* e = getenv("MM_FLOW_POLL")) r.poll = atoi(e) != 0;
     return r;
   }();
   return t;
@@ -372,14 +375,48 @@ int launch_fwd_cluster(const UniformPlan& P, const UniformSrc& src, cudaStream_t
 // G[0, ...]; the sub-matrix is copied to the tail of the progress-word region.  Returns
 // MM_ERR_UNSUPPORTED (nothing launched) when slab 0 does not fit that kernel.
 template <int D>
+bool slab0_fits(const UniformPlan& P) {
+  Geom gs;
+  return D >= 2 && make_geom(D - 1, P.g.shape + 1, gs) == MM_OK && cluster_fits(gs) && gs.strides[0] >= 64;
+}
+
+// The pending fill of level 0 (G[strides[0] ..], see kPendingBits) runs on a side stream while the
+// slab-0 cluster kernel occupies a few SMs: fork after the work already queued on `st`, join
+// before level 0.  One side stream and event pair per device, used under a lock so that
+// concurrent calls cannot interleave their fork / join.
+int fill_pending_overlapped(double2* p, size_t bytes, cudaStream_t st, std::unique_lock<std::mutex>& lk,
+                            cudaEvent_t& join) {
+  struct Side {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+  };
+  static std::mutex mu;
+  static Side side[64];
+  int dev = 0;
+  MM_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return MM_ERR_UNSUPPORTED;
+  lk = std::unique_lock<std::mutex>(mu);
+  Side& sd = side[dev];
+  if (!sd.s) {
+    MM_CUDA(cudaStreamCreateWithFlags(&sd.s, cudaStreamNonBlocking));
+    MM_CUDA(cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming));
+    MM_CUDA(cudaEventCreateWithFlags(&sd.join, cudaEventDisableTiming));
+  }
+  MM_CUDA(cudaEventRecord(sd.fork, st));
+  MM_CUDA(cudaStreamWaitEvent(sd.s, sd.fork, 0));
+  MM_CUDA(cudaMemsetAsync(p, 0xff, bytes, sd.s));
+  MM_CUDA(cudaEventRecord(sd.join, sd.s));
+  join = sd.join;
+  return MM_OK;
+}
+
+template <int D>
 int slab0_cluster(const UniformPlan& P, const UniformSrc& src, char* ws, cudaStream_t st) {
   if constexpr (D < 2) {
     return MM_ERR_UNSUPPORTED;
   } else {
     UniformPlan Ps;
-    if (make_geom(D - 1, P.g.shape + 1, Ps.g) != MM_OK || !cluster_fits(Ps.g) || Ps.g.strides[0] < 64) {
-      return MM_ERR_UNSUPPORTED;
-    }
+    if (!slab0_fits<D>(P) || make_geom(D - 1, P.g.shape + 1, Ps.g) != MM_OK) return MM_ERR_UNSUPPORTED;
     Ps.B = 1;
     char* sub = ws + P.L.flags + ((size_t)(P.L.n_flags - kFlowSubWords) * sizeof(uint32_t) + 15) / 16 * 16;
     double2* As = reinterpret_cast<double2*>(sub);
@@ -419,8 +456,20 @@ int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, 
     MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_flow_kernel<D>, t.block, 0));
     if (occ >= 1) {
       const int per_sm = std::min(occ, t.per_sm);
-      // slab 0 first on one cluster (see FlowTuning), then level 0 alone
+      // slab 0 first on one cluster (see FlowTuning), then level 0 alone; with polling, level 0's
+      // pending fill overlaps the slab-0 kernel (joined below, whichever path runs)
+      std::unique_lock<std::mutex> side_lock;
+      cudaEvent_t fill_join = nullptr;
+      const int64_t s0 = P.g.strides[0];
+      if (t.slab0 && t.poll && slab0_fits<D>(P)) {
+        int rc = fill_pending_overlapped(src.G + s0, (size_t)(P.g.n - s0) * sizeof(double2), st, side_lock, fill_join);
+        if (rc) return rc;
+      }
       const bool slab0 = t.slab0 && slab0_cluster<D>(P, src, ws, st) == MM_OK;
+      if (fill_join) {
+        MM_CUDA(cudaStreamWaitEvent(st, fill_join, 0));
+        side_lock.unlock();
+      }
       FlowPlan fp;
       const int64_t n_flags =
           flow_plan(P.g, di.sms, per_sm, t.min_amps, slab0 ? 0 : t.exclusive, wait_budget_ns(), fp);
@@ -430,6 +479,7 @@ int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, 
       if (slab0) {
         // no CTA takes a level >= 1; their progress words (and word 0, G[0]) read as complete
         fp.face = 0;
+        if (fill_join) fp.poll_halo = 1;  // level 0's amplitudes read as pending until written
         MM_CUDA(cudaMemsetAsync(prog, 0xff, (size_t)fp.flag0[0] * sizeof(uint32_t), st));
         MM_CUDA(cudaMemsetAsync(prog + fp.flag0[0], 0, (size_t)(n_flags - fp.flag0[0] + kFlowMaxSmid) * sizeof(uint32_t),
                                 st));

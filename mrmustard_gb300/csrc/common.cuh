@@ -175,13 +175,27 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
 __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const void* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 #else  // host compilation of the device code (CPU emulation of the kernels' indexing)
 __device__ __forceinline__ uint64_t globaltimer_ns() { return 0; }
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
 __device__ __forceinline__ int32_t ld_relaxed_i32(const int32_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
 __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) { __atomic_store_n(p, v, __ATOMIC_RELEASE); }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const void* p) {
+  return __atomic_load_n(reinterpret_cast<const unsigned long long*>(p), __ATOMIC_RELAXED);
+}
 #endif
+
+// An amplitude that its producer has not written yet, in a region filled with this bit pattern
+// (all ones: a NaN that FP64 arithmetic never produces -- its NaN results are the canonical one).
+// A consumer that polls the amplitude itself needs no progress word and no release fence: every
+// aligned 8-byte store becomes visible whole.
+constexpr unsigned long long kPendingBits = 0xffffffffffffffffull;
 
 // Progress signal for waits: a CTA that works alone while the others wait at a
 // barrier bumps the heartbeat, which restarts their timeout.

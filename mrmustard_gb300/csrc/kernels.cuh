@@ -684,6 +684,7 @@ struct FlowPlan {
   uint32_t exclusive;   // see above
   uint32_t small_lvl;   // levels >= small_lvl live in shared memory (D: none)
   uint32_t small_amps;  // strides[small_lvl - 1]: amplitudes of that region
+  uint32_t poll_halo;   // level 0 alone, its chunks >= 1 pre-filled with kPendingBits: halo values polled
   uint64_t budget_ns;
 };
 
@@ -868,6 +869,30 @@ __device__ __forceinline__ double part_fma(double2 x, double2 y, bool im, double
   return fma(x.x, im ? y.y : y.x, fma(flip_sign_if(x.y, !im), im ? y.x : y.y, acc));
 }
 
+// One halo amplitude of the previous chunk, polled until its producer has written both parts
+// (see kPendingBits); bounded: after budget_ns, or when another CTA has given up, records the
+// failure (MM_ERR_WAIT_TIMEOUT on a timeout) and returns what it read.
+__device__ __forceinline__ double2 halo_poll(const double2* p, WsHeader* h, uint64_t budget_ns, int* s_fail) {
+  unsigned long long x = ld_relaxed_u64(p), y = ld_relaxed_u64(reinterpret_cast<const double*>(p) + 1);
+  if (x == kPendingBits || y == kPendingBits) {
+    const uint64_t t0 = globaltimer_ns();
+    while (x == kPendingBits || y == kPendingBits) {
+      if (ld_relaxed_i32(&h->abort) != 0) {
+        *s_fail = 1;
+        break;
+      }
+      if (globaltimer_ns() - t0 > budget_ns) {
+        set_status(h, MM_ERR_WAIT_TIMEOUT);
+        *s_fail = 1;
+        break;
+      }
+      x = ld_relaxed_u64(p);
+      y = ld_relaxed_u64(reinterpret_cast<const double*>(p) + 1);
+    }
+  }
+  return cmk(__longlong_as_double((long long)x), __longlong_as_double((long long)y));
+}
+
 // Barrier over the first n threads of the CTA (n a multiple of 32), id != 0.
 #if defined(__CUDA_ARCH__)
 __device__ __forceinline__ void bar_sync_n(uint32_t id, uint32_t n) {
@@ -1009,6 +1034,9 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
     if (threadIdx.x == 0) st_release_u32(my, 1u);
   }
   const uint32_t w_lo = fp.flag0[i] + (lo >= snext ? lo - snext : 0u) / per, w_hi = fp.flag0[i] + vr;
+  // level 0 alone with its chunks pre-filled (FlowPlan::poll_halo): no progress words, the halo
+  // values themselves are polled
+  const bool poll = i == 0 && fp.poll_halo != 0;
   for (int m = 2; m < Ci; ++m) {
     const double2 cd = crow[g.prefC[i] + m];
     const double rsm = rs[m];
@@ -1031,7 +1059,7 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
         }
       }
     }
-    if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, kFlowNone, (uint32_t)(m - 1), fp.budget_ns, s_fail))
+    if (!poll && w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, kFlowNone, (uint32_t)(m - 1), fp.budget_ns, s_fail))
       return false;
     const int64_t prev = (int64_t)(m - 1) * si;
 #pragma unroll
@@ -1042,7 +1070,9 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
         for (int j = 1; j < D; ++j) {
           const uint32_t sj = (uint32_t)g.strides[j];
           if (j > i && k[u][j] > 0 && q - sj < lo)
-            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + prev + (q - sj)), im, acc[u]);
+            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]],
+                              poll ? halo_poll(G + prev + (q - sj), h, fp.budget_ns, s_fail) : __ldcg(G + prev + (q - sj)),
+                              im, acc[u]);
         }
         const double val = rsm * acc[u];
         Gd[2 * ((int64_t)m * si + q) + im] = val;
@@ -1052,7 +1082,11 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) st_release_u32(my, (uint32_t)m);
+    if (poll) {
+      if (*s_fail) return false;
+    } else if (threadIdx.x == 0) {
+      st_release_u32(my, (uint32_t)m);
+    }
   }
   return true;
 }
