@@ -25,7 +25,6 @@ constexpr int kFlowBlock = 256;            // dataflow forward: threads per CTA
 constexpr int kFlowPerSm = 2;              // dataflow forward: CTAs per SM (capped by occupancy)
 constexpr int kFlowMaxPerSm = 8;           // bound used to size the progress words
 constexpr uint32_t kFlowMinAmps = 128;     // dataflow forward: fewest amplitudes of a chunk per CTA
-constexpr int64_t kFlowSubWords = 256;     // tail of the progress-word region: the slab-0 triple's A (<= 784 bytes)
 constexpr int64_t kVjpItemAmps = 65536;    // default amplitudes per VJP work item
 constexpr int kTeamCluster = 8;            // CTAs per cluster for the large instances of a ragged batch
 constexpr size_t kAlign = 256;
@@ -196,7 +195,7 @@ int plan_uniform(int64_t B, int D, const int64_t* shape, UniformPlan& P, int sms
   // progress words of the dataflow forward (one large instance)
   const int64_t n_flags =
       (fwd && B == 1 && P.g.n >= grid_min_amps())
-          ? 1 + (int64_t)MM_MAXD * kFlowMaxPerSm * std::max(sms, 1) + (int64_t)kFlowMaxSmid + kFlowSubWords
+          ? 1 + (int64_t)MM_MAXD * kFlowMaxPerSm * std::max(sms, 1) + (int64_t)kFlowMaxSmid
           : 0;
   P.L = make_layout(P.g.maxC + 1, B * coef_entries(P.g), B * P.items_per_inst, 0, 0, n_flags);
   return MM_OK;
@@ -251,13 +250,11 @@ int launch_setup(const Src& src, int64_t n_inst, char* ws, const Layout& L, int 
 
 // Tuning of the dataflow forward; MM_FLOW_BLOCK, MM_FLOW_PER_SM, MM_FLOW_MIN_AMPS
 // and MM_FLOW_EXCLUSIVE in the environment override the defaults.
-// slab0: compute slab 0 (every amplitude with k_0 = 0, levels 1 .. D-1) first, as its own
-// instance (A[1:, 1:], b[1:], c) on one thread-block cluster (fwd_cluster_kernel), then level 0
-// alone on every SM (MM_FLOW_SLAB0=0: the one-launch dataflow over all levels).  poll: level 0
-// then polls its halo amplitudes in G (pre-filled with kPendingBits) instead of waiting on
-// progress words (MM_FLOW_POLL=0: progress words).
+// poll: G is filled with kPendingBits first and every range polls the amplitudes of other CTAs
+// that it reads, instead of waiting on their progress words (when every level below the
+// shared-memory face runs on lane-pair ranges; MM_FLOW_POLL=0: progress words).
 struct FlowTuning {
-  int block = kFlowBlock, per_sm = kFlowPerSm, exclusive = 1, slab0 = 1, poll = 1;
+  int block = kFlowBlock, per_sm = kFlowPerSm, exclusive = 1, poll = 1;
   uint32_t min_amps = kFlowMinAmps;
 };
 
@@ -268,7 +265,6 @@ FlowTuning flow_tuning() {
     if (const char* e = getenv("MM_FLOW_PER_SM")) r.per_sm = std::min(kFlowMaxPerSm, std::max(1, atoi(e)));
     if (const char* e = getenv("MM_FLOW_MIN_AMPS")) r.min_amps = (uint32_t)std::max(2, atoi(e));
     if (const char* e = getenv("MM_FLOW_EXCLUSIVE")) r.exclusive = atoi(e) != 0;
-    if (const char* e = getenv("MM_FLOW_SLAB0")) r.slab0 = atoi(e) != 0;
     if (const char* e = getenv("MM_FLOW_POLL")) r.poll = atoi(e) != 0;
     return r;
   }();
@@ -368,71 +364,6 @@ int launch_fwd_cluster(const UniformPlan& P, const UniformSrc& src, cudaStream_t
   return MM_ERR_UNSUPPORTED;
 }
 
-// Slab 0 of one large instance (the amplitudes with k_0 = 0) is the Fock tensor of the triple
-// (A[1:, 1:], b[1:], c) over axes 1 .. D-1: with k_0 = 0 the pivot is never axis 0 and every term
-// through axis 0 vanishes, so the reference's recurrence (core.py:85-122) restricted to it is that
-// triple's.  It runs as its own instance on one thread-block cluster (fwd_cluster_kernel), writing
-// G[0, ...]; the sub-matrix is copied to the tail of the progress-word region.  Returns
-// MM_ERR_UNSUPPORTED (nothing launched) when slab 0 does not fit that kernel.
-template <int D>
-bool slab0_fits(const UniformPlan& P) {
-  Geom gs;
-  return D >= 2 && make_geom(D - 1, P.g.shape + 1, gs) == MM_OK && cluster_fits(gs) && gs.strides[0] >= 64;
-}
-
-// The pending fill of level 0 (G[strides[0] ..], see kPendingBits) runs on a side stream while the
-// slab-0 cluster kernel occupies a few SMs: fork after the work already queued on `st`, join
-// before level 0.  One side stream and event pair per device, used under a lock so that
-// concurrent calls cannot interleave their fork / join.
-int fill_pending_overlapped(double2* p, size_t bytes, cudaStream_t st, std::unique_lock<std::mutex>& lk,
-                            cudaEvent_t& join) {
-  struct Side {
-    cudaStream_t s = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-  };
-  static std::mutex mu;
-  static Side side[64];
-  int dev = 0;
-  MM_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return MM_ERR_UNSUPPORTED;
-  lk = std::unique_lock<std::mutex>(mu);
-  Side& sd = side[dev];
-  if (!sd.s) {
-    MM_CUDA(cudaStreamCreateWithFlags(&sd.s, cudaStreamNonBlocking));
-    MM_CUDA(cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming));
-    MM_CUDA(cudaEventCreateWithFlags(&sd.join, cudaEventDisableTiming));
-  }
-  MM_CUDA(cudaEventRecord(sd.fork, st));
-  MM_CUDA(cudaStreamWaitEvent(sd.s, sd.fork, 0));
-  MM_CUDA(cudaMemsetAsync(p, 0xff, bytes, sd.s));
-  MM_CUDA(cudaEventRecord(sd.join, sd.s));
-  join = sd.join;
-  return MM_OK;
-}
-
-template <int D>
-int slab0_cluster(const UniformPlan& P, const UniformSrc& src, char* ws, cudaStream_t st) {
-  if constexpr (D < 2) {
-    return MM_ERR_UNSUPPORTED;
-  } else {
-    UniformPlan Ps;
-    if (!slab0_fits<D>(P) || make_geom(D - 1, P.g.shape + 1, Ps.g) != MM_OK) return MM_ERR_UNSUPPORTED;
-    Ps.B = 1;
-    char* sub = ws + P.L.flags + ((size_t)(P.L.n_flags - kFlowSubWords) * sizeof(uint32_t) + 15) / 16 * 16;
-    double2* As = reinterpret_cast<double2*>(sub);
-    MM_CUDA(cudaMemcpy2DAsync(As, (D - 1) * sizeof(double2), src.A + D + 1, D * sizeof(double2),
-                              (D - 1) * sizeof(double2), D - 1, cudaMemcpyDeviceToDevice, st));
-    UniformSrc ss = {};
-    ss.g = Ps.g;
-    ss.B = 1;
-    ss.A = As;
-    ss.b = src.b + 1;
-    ss.c = src.c;
-    ss.G = src.G;
-    return launch_fwd_cluster_D<D - 1>(Ps, ss, st);
-  }
-}
-
 template <int D>
 int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, int stable, const DevInfo& di,
                          cudaStream_t st) {
@@ -456,36 +387,19 @@ int launch_fwd_uniform_D(const UniformPlan& P, const UniformSrc& src, char* ws, 
     MM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_flow_kernel<D>, t.block, 0));
     if (occ >= 1) {
       const int per_sm = std::min(occ, t.per_sm);
-      // slab 0 first on one cluster (see FlowTuning), then level 0 alone; with polling, level 0's
-      // pending fill overlaps the slab-0 kernel (joined below, whichever path runs)
-      std::unique_lock<std::mutex> side_lock;
-      cudaEvent_t fill_join = nullptr;
-      const int64_t s0 = P.g.strides[0];
-      if (t.slab0 && t.poll && slab0_fits<D>(P)) {
-        int rc = fill_pending_overlapped(src.G + s0, (size_t)(P.g.n - s0) * sizeof(double2), st, side_lock, fill_join);
-        if (rc) return rc;
-      }
-      const bool slab0 = t.slab0 && slab0_cluster<D>(P, src, ws, st) == MM_OK;
-      if (fill_join) {
-        MM_CUDA(cudaStreamWaitEvent(st, fill_join, 0));
-        side_lock.unlock();
-      }
       FlowPlan fp;
-      const int64_t n_flags =
-          flow_plan(P.g, di.sms, per_sm, t.min_amps, slab0 ? 0 : t.exclusive, wait_budget_ns(), fp);
+      const int64_t n_flags = flow_plan(P.g, di.sms, per_sm, t.min_amps, t.exclusive, wait_budget_ns(), fp);
       // progress words, then the SM registration words
-      if (n_flags + (int64_t)kFlowMaxSmid > P.L.n_flags - kFlowSubWords) return MM_ERR_WORKSPACE;
+      if (n_flags + (int64_t)kFlowMaxSmid > P.L.n_flags) return MM_ERR_WORKSPACE;
       uint32_t* prog = reinterpret_cast<uint32_t*>(ws + P.L.flags);
-      if (slab0) {
-        // no CTA takes a level >= 1; their progress words (and word 0, G[0]) read as complete
-        fp.face = 0;
-        if (fill_join) fp.poll_halo = 1;  // level 0's amplitudes read as pending until written
-        MM_CUDA(cudaMemsetAsync(prog, 0xff, (size_t)fp.flag0[0] * sizeof(uint32_t), st));
-        MM_CUDA(cudaMemsetAsync(prog + fp.flag0[0], 0, (size_t)(n_flags - fp.flag0[0] + kFlowMaxSmid) * sizeof(uint32_t),
-                                st));
-      } else {
-        MM_CUDA(cudaMemsetAsync(prog, 0, (size_t)(n_flags + kFlowMaxSmid) * sizeof(uint32_t), st));
+      bool poll = t.poll;
+      for (int i = 0; poll && i < (int)fp.small_lvl && i < D; ++i)
+        poll = fp.ctas[i] > 1 && fp.per[i] <= 2u * (uint32_t)t.block;
+      if (poll) {  // every amplitude reads as pending until written (G[0] is read from c)
+        fp.poll_halo = 1;
+        MM_CUDA(cudaMemsetAsync(src.G, 0xff, (size_t)P.g.n * sizeof(double2), st));
       }
+      MM_CUDA(cudaMemsetAsync(prog, 0, (size_t)(n_flags + kFlowMaxSmid) * sizeof(uint32_t), st));
       UniformSrc s = src;
       void* args[] = {&s, (void*)&rs, &h, &prog, &fp};
       MM_CUDA(cudaLaunchCooperativeKernel((void*)fwd_flow_kernel<D>, dim3(per_sm * di.sms), dim3(t.block), args, 0,

@@ -684,7 +684,7 @@ struct FlowPlan {
   uint32_t exclusive;   // see above
   uint32_t small_lvl;   // levels >= small_lvl live in shared memory (D: none)
   uint32_t small_amps;  // strides[small_lvl - 1]: amplitudes of that region
-  uint32_t poll_halo;   // level 0 alone, its chunks >= 1 pre-filled with kPendingBits: halo values polled
+  uint32_t poll_halo;   // G pre-filled with kPendingBits (but G[0]): every input of another CTA is polled
   uint64_t budget_ns;
 };
 
@@ -1000,29 +1000,37 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
     gp[u] = gpp[u] = 0.0;
   }
   if (Ci < 2) return true;
+  // FlowPlan::poll_halo: no progress words; every amplitude another CTA writes is polled in G (G[0],
+  // which holds c, is read from c: it may carry the pending bits)
+  const bool poll = fp.poll_halo != 0;
+  auto input = [&](int64_t idx) -> double2 {
+    if (!poll) return __ldcg(G + idx);
+    return idx == 0 ? v.c : halo_poll(G + idx, h, fp.budget_ns, s_fail);
+  };
   {  // chunk 1: every input is an amplitude of the lower levels
-    const uint32_t pos = hi - 1;
-    int l = i + 1;
-    while (l < D && pos / (uint32_t)g.strides[l] == 0) ++l;
-    uint32_t w_lo = 0, w_hi = (fv == 0) ? 0u : 1u, target = 1u, skip = kFlowNone;
-    if (l < D) {
-      target = pos / (uint32_t)g.strides[l];
-      w_lo = fp.flag0[l];
-      w_hi = w_lo + fp.ctas[l];
-      if (fv < fp.ctas[l]) skip = w_lo + fv;
+    if (!poll) {
+      const uint32_t pos = hi - 1;
+      int l = i + 1;
+      while (l < D && pos / (uint32_t)g.strides[l] == 0) ++l;
+      uint32_t w_lo = 0, w_hi = (fv == 0) ? 0u : 1u, target = 1u, skip = kFlowNone;
+      if (l < D) {
+        target = pos / (uint32_t)g.strides[l];
+        w_lo = fp.flag0[l];
+        w_hi = w_lo + fp.ctas[l];
+        if (fv < fp.ctas[l]) skip = w_lo + fv;
+      }
+      if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, skip, target, fp.budget_ns, s_fail)) return false;
     }
-    if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, skip, target, fp.budget_ns, s_fail)) return false;
     const double rs1 = rs[1];
 #pragma unroll
     for (int u = 0; u < A; ++u) {
       const uint32_t q = lo + a0 + (uint32_t)u * pairs;
       if (q < hi) {
-        const double2 g0 = __ldcg(G + q);
+        const double2 g0 = input(q);
         double acc = part_fma(bi, g0, im, 0.0);
 #pragma unroll
         for (int j = 1; j < D; ++j)
-          if (j > i && k[u][j] > 0)
-            acc = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + q - (uint32_t)g.strides[j]), im, acc);
+          if (j > i && k[u][j] > 0) acc = part_fma(crow[g.prefC[j] + k[u][j]], input(q - (uint32_t)g.strides[j]), im, acc);
         const double val = rs1 * acc;
         Gd[2 * ((int64_t)si + q) + im] = val;
         Sd[2 * (per + (q - lo)) + im] = val;
@@ -1031,12 +1039,13 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) st_release_u32(my, 1u);
+    if (poll) {
+      if (*s_fail) return false;
+    } else if (threadIdx.x == 0) {
+      st_release_u32(my, 1u);
+    }
   }
   const uint32_t w_lo = fp.flag0[i] + (lo >= snext ? lo - snext : 0u) / per, w_hi = fp.flag0[i] + vr;
-  // level 0 alone with its chunks pre-filled (FlowPlan::poll_halo): no progress words, the halo
-  // values themselves are polled
-  const bool poll = i == 0 && fp.poll_halo != 0;
   for (int m = 2; m < Ci; ++m) {
     const double2 cd = crow[g.prefC[i] + m];
     const double rsm = rs[m];
@@ -1070,9 +1079,7 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
         for (int j = 1; j < D; ++j) {
           const uint32_t sj = (uint32_t)g.strides[j];
           if (j > i && k[u][j] > 0 && q - sj < lo)
-            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]],
-                              poll ? halo_poll(G + prev + (q - sj), h, fp.budget_ns, s_fail) : __ldcg(G + prev + (q - sj)),
-                              im, acc[u]);
+            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], input(prev + (q - sj)), im, acc[u]);
         }
         const double val = rsm * acc[u];
         Gd[2 * ((int64_t)m * si + q) + im] = val;

@@ -215,17 +215,15 @@ def test_single_instance_cluster_shapes(cuda, oracle_lib, shape):
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
 
 
-# A single large instance whose slab 0 (k_0 = 0) fits the one-cluster kernel runs in two phases:
-# slab 0 as the triple (A[1:, 1:], b[1:], c) on one cluster, then level 0 alone over every SM, each
-# range polling its halo amplitudes (pre-filled with a pending pattern) instead of progress words.
-# Corners: the benchmark's 4 x 40 and 4 x 30 states, a cutoff-50 slab (2500 amplitudes, 16 CTAs), a
-# slab of one level-0 chunk (extent 1 on axis 1), D = 3, 6, a slab of 2560 amplitudes.
-SLAB0_SHAPES = [(6, 40, 40, 40), (30, 30, 30, 30), (3, 50, 50, 50), (5, 3, 1000), (2, 2, 2560),
+# Large single instances on the dataflow kernel with polled amplitudes (G pre-filled with a pending
+# pattern, every input of another CTA polled): the benchmark's 4 x 40 and 4 x 30 states, a cutoff-50
+# level 1 (2500 amplitudes per chunk), an extent of 1 on axis 1, D = 3, 6, a 2560-amplitude slab.
+POLLED_SHAPES = [(6, 40, 40, 40), (30, 30, 30, 30), (3, 50, 50, 50), (5, 3, 1000), (2, 2, 2560),
                 (4, 8, 8, 8, 8, 6), (40, 1, 40, 40)]
 
 
-@pytest.mark.parametrize("shape", SLAB0_SHAPES)
-def test_single_instance_slab0_shapes(cuda, oracle_lib, shape):
+@pytest.mark.parametrize("shape", POLLED_SHAPES)
+def test_single_instance_polled_shapes(cuda, oracle_lib, shape):
     A, b, _ = takagi(len(shape), 0.8, 700 + sum(shape))
     c = 0.9 + 0.3j
     Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
@@ -249,11 +247,11 @@ np.savez({path!r}, **out)
 
 
 @pytest.mark.parametrize("env", [{"MM_CLUSTER_FWD": "0"}, {"MM_CLUSTER_CTAS": "1"}, {"MM_CLUSTER_CTAS": "3"},
-                                 {"MM_CLUSTER_CTAS": "16"}, {"MM_FLOW_SLAB0": "0"}, {"MM_FLOW_POLL": "0"}])
+                                 {"MM_CLUSTER_CTAS": "16"}, {"MM_FLOW_POLL": "0"}])
 def test_single_instance_forced_schedules(cuda, oracle_lib, tmp_path, env):
     """The same instances with the cluster kernel off (grid-wide dataflow kernel instead), with
-    fixed cluster sizes and with the two-phase large-instance forward off (schedule knobs are read
-    once per process, so each runs in a child)."""
+    fixed cluster sizes and with the large-instance dataflow on progress words instead of polled
+    amplitudes (schedule knobs are read once per process, so each runs in a child)."""
     import os
     import subprocess
     import sys
