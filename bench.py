@@ -31,7 +31,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Fock amplitudes/s fwd+VJP (c128, <=1e-12 rel) batched vs plain, 1 GB300"
 UNIT = "amplitudes/s"
 N_INST = 4096
-VJP_DRAM_BYTES_PER_AMP = 50.3  # dram read + write per amplitude, ncu capture of the VJP items kernel
+VJP_DRAM_BYTES_PER_AMP = 52.1  # dram read + write per amplitude, ncu capture of the VJP items kernel
 ERR_TOL = 1e-12                # max |x - oracle| / max |oracle| per instance, G and every gradient
 MIN_BATCHED_OVER_PLAIN = 10.0  # one batched launch vs a loop of per-instance launches
 
@@ -349,7 +349,7 @@ def run_gb300(args, rank, local_rank, world):
         dom, t_dom, bytes_dom, ops_dom = "fwd_cta_kernel", t_fwd, 16.0 * total, fwd_ops
     achieved_gbs = bytes_dom / (t_dom * 1e-3) / 1e9
     # DRAM bytes per launch from one ncu capture of the VJP on a 1024-triple batch
-    # (50.3 B per amplitude: dram__bytes_read.sum + dram__bytes_write.sum), scaled by amplitudes
+    # (52.1 B per amplitude: dram__bytes_read.sum + dram__bytes_write.sum), scaled by amplitudes
     traffic = VJP_DRAM_BYTES_PER_AMP * total if dom == "vjp_items_kernel" else None
 
     extras = {}
