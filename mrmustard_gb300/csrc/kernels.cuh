@@ -1902,15 +1902,18 @@ __device__ __forceinline__ void vjp_fibers(const InstView& v, const Tables& T, u
 #pragma unroll
     for (int s = 0; s < NV; ++s) a[s] = cmk(0.0, 0.0);
     // PF (the host-buffer step: the cotangent is read over the host link from pinned host memory):
-    // each cotangent value is loaded one step of k_0 ahead of its use, hiding that latency (from
-    // device memory the early load measured ~1 % slower, so it is not used there)
+    // each cotangent value is loaded two steps of k_0 ahead of its use, hiding that latency (one
+    // step ahead hid part of it; from device memory an early load measured ~1 % slower, so it is
+    // not used there)
     double2 gu_next = PF ? __ldg(gb + q) : cmk(0.0, 0.0);
+    double2 gu_next2 = (PF && C0 > 1) ? __ldg(gb + s0 + q) : cmk(0.0, 0.0);
     for (int m = 0; m < C0; ++m) {
       const int64_t f = (int64_t)m * s0 + q;
       double2 gu;
       if constexpr (PF) {
         gu = gu_next;
-        if (m + 1 < C0) gu_next = __ldg(gb + f + s0);
+        gu_next = gu_next2;
+        if (m + 2 < C0) gu_next2 = __ldg(gb + f + 2 * s0);
       } else {
         gu = __ldg(gb + f);
       }
