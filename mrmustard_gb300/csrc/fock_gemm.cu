@@ -230,11 +230,12 @@ __global__ void __launch_bounds__(256) col_exp_kernel(const double2* __restrict_
 }
 
 // Digits of one value against exponent bound E: dig[p] for p < OZ_MAX_SLICES, the balanced
-// base-256 digits of a = floor(|x| 2^(OZ_TOP - E)) (digit 0 most significant), negated for x < 0.
-// Digits are taken from the least significant end; a digit of 128 or more becomes digit - 256
-// with a carry into the next one, so every digit lies in [-128, 127] and the top one
-// (a >> 48 < 128, plus a carry) in [0, 128].  Keeping only the S most significant digits
+// base-256 digits of a = floor(|x| 2^(OZ_TOP - E)) (digit 0 most significant), negated for x < 0:
+// digits 1..6 in [-128, 127], digit 0 (a >> 48 < 128, plus a carry) in [0, 128].  Branch-free: with
+// u_p = d_p + 128 for p >= 1, a + 0x808080808080 = d_0 2^48 + sum_p u_p 2^(8(6-p)) has the u_p as its
+// low bytes (each in [0, 255]) and d_0 above them.  Keeping only the S most significant digits
 // (S < OZ_MAX_SLICES) leaves a within half a unit of the last kept digit.
+static_assert(OZ_MAX_SLICES == 7 && OZ_BETA == 8 && OZ_TOP == 55, "digit layout of value_digits");
 __device__ __forceinline__ void value_digits(double x, int E, int (&dig)[OZ_MAX_SLICES]) {
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const int e = (int)((bits >> 52) & 0x7ff);
@@ -248,17 +249,11 @@ __device__ __forceinline__ void value_digits(double x, int E, int (&dig)[OZ_MAX_
     if (shift >= 0) a = mant << shift;
     else if (shift > -64) a = mant >> (-shift);
   }
+  const uint64_t u = a + 0x808080808080ull;
+  const int sg = neg ? -1 : 1;
+  dig[0] = sg * (int)(u >> 48);
 #pragma unroll
-  for (int p = OZ_MAX_SLICES - 1; p >= 1; --p) {
-    int v = (int)(a & 0xff);
-    a >>= 8;
-    if (v >= 128) {
-      v -= 256;
-      a += 1;
-    }
-    dig[p] = neg ? -v : v;
-  }
-  dig[0] = neg ? -(int)a : (int)a;
+  for (int p = 1; p < OZ_MAX_SLICES; ++p) dig[p] = sg * ((int)((u >> (8 * (OZ_MAX_SLICES - 1 - p))) & 0xff) - 128);
 }
 
 // Digits p < S of four consecutive values (of one plane row) as four BF16 (exact: |digit| <= 128)
