@@ -893,6 +893,12 @@ __device__ __forceinline__ double2 halo_poll(const double2* p, WsHeader* h, uint
   return cmk(__longlong_as_double((long long)x), __longlong_as_double((long long)y));
 }
 
+// A value as stored where other CTAs poll it: never the pending pattern (a NaN that arithmetic on a
+// NaN input carrying those bits might propagate becomes a plain quiet NaN).
+__device__ __forceinline__ double not_pending(double x) {
+  return (unsigned long long)__double_as_longlong(x) == kPendingBits ? __longlong_as_double(0x7ff8000000000000ll) : x;
+}
+
 // Barrier over the first n threads of the CTA (n a multiple of 32), id != 0.
 #if defined(__CUDA_ARCH__)
 __device__ __forceinline__ void bar_sync_n(uint32_t id, uint32_t n) {
@@ -1031,7 +1037,7 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
 #pragma unroll
         for (int j = 1; j < D; ++j)
           if (j > i && k[u][j] > 0) acc = part_fma(crow[g.prefC[j] + k[u][j]], input(q - (uint32_t)g.strides[j]), im, acc);
-        const double val = rs1 * acc;
+        const double val = not_pending(rs1 * acc);
         Gd[2 * ((int64_t)si + q) + im] = val;
         Sd[2 * (per + (q - lo)) + im] = val;
         gpp[u] = im ? g0.y : g0.x;
@@ -1081,7 +1087,7 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
           if (j > i && k[u][j] > 0 && q - sj < lo)
             acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], input(prev + (q - sj)), im, acc[u]);
         }
-        const double val = rsm * acc[u];
+        const double val = not_pending(rsm * acc[u]);
         Gd[2 * ((int64_t)m * si + q) + im] = val;
         Sn[2 * (q - lo) + im] = val;
         gpp[u] = gp[u];
@@ -1124,7 +1130,8 @@ __global__ void __launch_bounds__(256) fwd_flow_kernel(UniformSrc src, const dou
           small_level<D>(sv, rs, i, Gs, lanes, sv.coef + (int64_t)i * g.sumC, 0, __ldg(sv.b + i));
         __syncthreads();
       }
-      for (uint32_t f = threadIdx.x; f < fp.small_amps; f += blockDim.x) stG(sv, f, Gs[f], 7);
+      for (uint32_t f = threadIdx.x; f < fp.small_amps; f += blockDim.x)
+        stG(sv, f, cmk(not_pending(Gs[f].x), not_pending(Gs[f].y)), 7);
       __syncthreads();
       if (threadIdx.x == 0) {
         st_release_u32(prog, 1u);

@@ -13,6 +13,8 @@ from __future__ import annotations
 
 import ctypes
 
+import time
+
 import numpy as np
 import pytest
 import torch
@@ -229,6 +231,24 @@ def test_single_instance_polled_shapes(cuda, oracle_lib, shape):
     Gd = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
                        torch.tensor(c, dtype=torch.complex128, device=cuda), shape)
     assert rel(Gd, oracle_lib.vanilla(shape, A, b, c)) < FWD_TOL
+
+
+def test_polled_forward_nan_inputs(cuda):
+    """NaN inputs carrying the all-ones bit pattern that the polled dataflow forward pre-fills G with
+    (in c, which G[0] holds, and in b, which every computed amplitude inherits): the call completes
+    (no amplitude is left looking pending, no wait times out) and returns NaNs."""
+    pending = np.frombuffer(np.full(8, 0xFF, np.uint8).tobytes(), np.float64)[0]
+    shape = (6, 40, 40, 40)
+    A, b, _ = takagi(4, 0.8, 811)
+    b = b.copy()
+    b[1] = complex(pending, pending)
+    c = complex(pending, pending)
+    t0 = time.perf_counter()
+    G = mm.device_fwd(torch.as_tensor(A, device=cuda), torch.as_tensor(b, device=cuda),
+                      torch.tensor(c, dtype=torch.complex128, device=cuda), shape)
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 1.0
+    assert torch.isnan(G.real).all() and torch.isnan(G.imag).all()
 
 
 _FORCED = """
