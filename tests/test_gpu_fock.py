@@ -26,11 +26,12 @@ def cn(shape, seed):
     return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
 
 
-# (40, 300, 64): N spans several 40-column tiles with a ragged last one; K = 9345 and 30100 take the
-# int64 slice-order sums (K padded beyond 9344), K = 9344 the int32 ones at their bound, as every other
-# case; K = 1025 and 4200 end in a partial 1024-value unit.
+# (40, 300, 64): N spans several 128-column tiles with a ragged last one (one lane of CTAs per column
+# tile); (64, 8200, 70): 65 column tiles, too many for lanes (one sequence over every tile); K = 9345
+# and 30100 take the int64 slice-order sums (K padded beyond 9344), K = 9344 the int32 ones at their
+# bound, as every other case; K = 1025 and 4200 end in a partial 1024-value unit.
 @pytest.mark.parametrize("M,N,K", [(1, 1, 1), (37, 5, 300), (300, 64, 200), (129, 33, 4200), (40, 300, 64),
-                                   (70, 41, 1025), (20, 9, 9344), (20, 9, 9345), (24, 12, 30100)])
+                                   (64, 8200, 70), (70, 41, 1025), (20, 9, 9344), (20, 9, 9345), (24, 12, 30100)])
 def test_gemm_random(cuda, oracle_lib, M, N, K):
     U, X = cn((M, K), M + K), cn((K, N), N)
     ref = oracle_lib.fock_gemm(U, X)
