@@ -24,7 +24,7 @@ constexpr int kGridBlock = 512;            // threads per CTA of the cooperative
 constexpr int kFlowBlock = 256;            // dataflow forward: threads per CTA
 constexpr int kFlowPerSm = 2;              // dataflow forward: CTAs per SM (capped by occupancy)
 constexpr int kFlowMaxPerSm = 8;           // bound used to size the progress words
-constexpr uint32_t kFlowMinAmps = 128;     // dataflow forward: fewest amplitudes of a chunk per CTA
+constexpr uint32_t kFlowMinAmps = 64;      // dataflow forward: fewest amplitudes of a chunk per CTA
 constexpr int64_t kVjpItemAmps = 65536;    // default amplitudes per VJP work item
 constexpr int kTeamCluster = 8;            // CTAs per cluster for the large instances of a ragged batch
 constexpr size_t kAlign = 256;
