@@ -180,6 +180,12 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const void* p) {
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+// Both 8-byte halves of a polled amplitude in one access.  No "memory" clobber: the amplitude's own
+// bits say whether it has been written, so no other access is ordered by it, and the compiler may
+// issue several of these before the first result is needed.
+__device__ __forceinline__ void ld_relaxed_v2u64(const void* p, unsigned long long& x, unsigned long long& y) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(x), "=l"(y) : "l"(p));
+}
 #else  // host compilation of the device code (CPU emulation of the kernels' indexing)
 __device__ __forceinline__ uint64_t globaltimer_ns() { return 0; }
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
@@ -188,6 +194,11 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) { return _
 __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) { __atomic_store_n(p, v, __ATOMIC_RELEASE); }
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const void* p) {
   return __atomic_load_n(reinterpret_cast<const unsigned long long*>(p), __ATOMIC_RELAXED);
+}
+__device__ __forceinline__ void ld_relaxed_v2u64(const void* p, unsigned long long& x, unsigned long long& y) {
+  const unsigned long long* q = reinterpret_cast<const unsigned long long*>(p);
+  x = __atomic_load_n(q, __ATOMIC_RELAXED);
+  y = __atomic_load_n(q + 1, __ATOMIC_RELAXED);
 }
 #endif
 

@@ -869,11 +869,11 @@ __device__ __forceinline__ double part_fma(double2 x, double2 y, bool im, double
   return fma(x.x, im ? y.y : y.x, fma(flip_sign_if(x.y, !im), im ? y.x : y.y, acc));
 }
 
-// One halo amplitude of the previous chunk, polled until its producer has written both parts
-// (see kPendingBits); bounded: after budget_ns, or when another CTA has given up, records the
-// failure (MM_ERR_WAIT_TIMEOUT on a timeout) and returns what it read.
-__device__ __forceinline__ double2 halo_poll(const double2* p, WsHeader* h, uint64_t budget_ns, int* s_fail) {
-  unsigned long long x = ld_relaxed_u64(p), y = ld_relaxed_u64(reinterpret_cast<const double*>(p) + 1);
+// One halo amplitude of the previous chunk whose bits (x, y) were loaded from p, polled again until
+// its producer has written both parts (see kPendingBits); bounded: after budget_ns, or when another
+// CTA has given up, records the failure (MM_ERR_WAIT_TIMEOUT on a timeout) and returns what it read.
+__device__ __forceinline__ double2 halo_wait(const double2* p, unsigned long long x, unsigned long long y, WsHeader* h,
+                                             uint64_t budget_ns, int* s_fail) {
   if (x == kPendingBits || y == kPendingBits) {
     const uint64_t t0 = globaltimer_ns();
     while (x == kPendingBits || y == kPendingBits) {
@@ -886,8 +886,7 @@ __device__ __forceinline__ double2 halo_poll(const double2* p, WsHeader* h, uint
         *s_fail = 1;
         break;
       }
-      x = ld_relaxed_u64(p);
-      y = ld_relaxed_u64(reinterpret_cast<const double*>(p) + 1);
+      ld_relaxed_v2u64(p, x, y);
     }
   }
   return cmk(__longlong_as_double((long long)x), __longlong_as_double((long long)y));
@@ -1009,10 +1008,6 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
   // FlowPlan::poll_halo: no progress words; every amplitude another CTA writes is polled in G (G[0],
   // which holds c, is read from c: it may carry the pending bits)
   const bool poll = fp.poll_halo != 0;
-  auto input = [&](int64_t idx) -> double2 {
-    if (!poll) return __ldcg(G + idx);
-    return idx == 0 ? v.c : halo_poll(G + idx, h, fp.budget_ns, s_fail);
-  };
   {  // chunk 1: every input is an amplitude of the lower levels
     if (!poll) {
       const uint32_t pos = hi - 1;
@@ -1028,19 +1023,60 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
       if (w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, skip, target, fp.budget_ns, s_fail)) return false;
     }
     const double rs1 = rs[1];
+    double acc1[A];
+    if (poll) {
+      // terms (u, j) in batches as in the later chunks; j = 0 is the amplitude q of the level below
+      constexpr int T = A * D, NB = T < 6 ? T : 6;
+#pragma unroll
+      for (int t0 = 0; t0 < T; t0 += NB) {
+        unsigned long long hx[NB], hy[NB];
+#pragma unroll
+        for (int t = 0; t < NB; ++t) {
+          hx[t] = hy[t] = 0ull;
+          const int u = (t0 + t) / D, j = (t0 + t) % D;
+          if (t0 + t >= T) continue;
+          const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+          const uint32_t idx = j == 0 ? q : q - (uint32_t)g.strides[j];
+          if (q < hi && (j == 0 || (j > i && k[u][j] > 0)) && idx != 0) ld_relaxed_v2u64(G + idx, hx[t], hy[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < NB; ++t) {
+          const int u = (t0 + t) / D, j = (t0 + t) % D;
+          if (t0 + t >= T) continue;
+          const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+          const uint32_t idx = j == 0 ? q : q - (uint32_t)g.strides[j];
+          if (q >= hi || (j != 0 && !(j > i && k[u][j] > 0))) continue;
+          const double2 x = idx == 0 ? v.c : halo_wait(G + idx, hx[t], hy[t], h, fp.budget_ns, s_fail);
+          if (j == 0) {
+            acc1[u] = part_fma(bi, x, im, 0.0);
+            gpp[u] = im ? x.y : x.x;
+          } else {
+            acc1[u] = part_fma(crow[g.prefC[j] + k[u][j]], x, im, acc1[u]);
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < A; ++u) {
+        const uint32_t q = lo + a0 + (uint32_t)u * pairs;
+        if (q < hi) {
+          const double2 g0 = __ldcg(G + q);
+          acc1[u] = part_fma(bi, g0, im, 0.0);
+#pragma unroll
+          for (int j = 1; j < D; ++j)
+            if (j > i && k[u][j] > 0)
+              acc1[u] = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + (q - (uint32_t)g.strides[j])), im, acc1[u]);
+          gpp[u] = im ? g0.y : g0.x;
+        }
+      }
+    }
 #pragma unroll
     for (int u = 0; u < A; ++u) {
       const uint32_t q = lo + a0 + (uint32_t)u * pairs;
       if (q < hi) {
-        const double2 g0 = input(q);
-        double acc = part_fma(bi, g0, im, 0.0);
-#pragma unroll
-        for (int j = 1; j < D; ++j)
-          if (j > i && k[u][j] > 0) acc = part_fma(crow[g.prefC[j] + k[u][j]], input(q - (uint32_t)g.strides[j]), im, acc);
-        const double val = not_pending(rs1 * acc);
+        const double val = not_pending(rs1 * acc1[u]);
         Gd[2 * ((int64_t)si + q) + im] = val;
         Sd[2 * (per + (q - lo)) + im] = val;
-        gpp[u] = im ? g0.y : g0.x;
         gp[u] = val;
       }
     }
@@ -1077,15 +1113,44 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
     if (!poll && w_lo < w_hi && !flow_wait(h, prog, w_lo, w_hi, kFlowNone, (uint32_t)(m - 1), fp.budget_ns, s_fail))
       return false;
     const int64_t prev = (int64_t)(m - 1) * si;
+    if (poll) {
+      // halo terms (u, j) in batches of NB: every load of a batch is issued before the first is
+      // waited on, so a thread pays one round trip to L2 per batch instead of one per term; each
+      // acc[u] still adds its terms in increasing j
+      constexpr int DM = D > 1 ? D - 1 : 1, T = A * (D - 1), NB = T < 6 ? (T > 0 ? T : 1) : 6;
+#pragma unroll
+      for (int t0 = 0; t0 < T; t0 += NB) {
+        unsigned long long hx[NB], hy[NB];
+#pragma unroll
+        for (int t = 0; t < NB; ++t) {
+          hx[t] = hy[t] = 0ull;
+          const int u = (t0 + t) / DM, j = 1 + (t0 + t) % DM;
+          if (t0 + t >= T) continue;
+          const uint32_t q = lo + a0 + (uint32_t)u * pairs, sj = (uint32_t)g.strides[j];
+          if (q < hi && j > i && k[u][j] > 0 && q - sj < lo) ld_relaxed_v2u64(G + prev + (q - sj), hx[t], hy[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < NB; ++t) {
+          const int u = (t0 + t) / DM, j = 1 + (t0 + t) % DM;
+          if (t0 + t >= T) continue;
+          const uint32_t q = lo + a0 + (uint32_t)u * pairs, sj = (uint32_t)g.strides[j];
+          if (q < hi && j > i && k[u][j] > 0 && q - sj < lo)
+            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]],
+                              halo_wait(G + prev + (q - sj), hx[t], hy[t], h, fp.budget_ns, s_fail), im, acc[u]);
+        }
+      }
+    }
 #pragma unroll
     for (int u = 0; u < A; ++u) {
       const uint32_t q = lo + a0 + (uint32_t)u * pairs;
       if (q < hi) {
+        if (!poll) {
 #pragma unroll
-        for (int j = 1; j < D; ++j) {
-          const uint32_t sj = (uint32_t)g.strides[j];
-          if (j > i && k[u][j] > 0 && q - sj < lo)
-            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], input(prev + (q - sj)), im, acc[u]);
+          for (int j = 1; j < D; ++j) {
+            const uint32_t sj = (uint32_t)g.strides[j];
+            if (j > i && k[u][j] > 0 && q - sj < lo)
+              acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + prev + (q - sj)), im, acc[u]);
+          }
         }
         const double val = not_pending(rsm * acc[u]);
         Gd[2 * ((int64_t)m * si + q) + im] = val;
@@ -1105,8 +1170,8 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
 }
 
 template <int D>
-__global__ void __launch_bounds__(256) fwd_flow_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
-                                                       uint32_t* prog, FlowPlan fp) {
+__global__ void __launch_bounds__(256, 2) fwd_flow_kernel(UniformSrc src, const double* __restrict__ rs, WsHeader* h,
+                                                          uint32_t* prog, FlowPlan fp) {
   MM_SHARED(InstView, sv);
   MM_SHARED(int, s_fail);
   MM_SHARED(FlowRole, role);
