@@ -764,7 +764,14 @@ struct FlowRole {
 // that SM; the slot is the CTA's arrival order on it), one grid barrier, then
 // each CTA ranks its SM among the SMs present.  If the launch did not land as
 // per_sm CTAs on each of `sms` SMs (or an SM id is out of range), every CTA
-// falls back to the same blockIdx-based mapping.
+// falls back to the same blockIdx-based mapping.  The n = S - F shared SMs take
+// the level-0 ranges in serpentine order (serpentine_range): slot 0 of the x-th
+// such SM takes range x and slot 1 range 2n - 1 - x, so a range that starts
+// late shares its SM with one that started early (and finishes early) rather
+// than with one that starts mid-way and runs as long as it does.
+__device__ __forceinline__ uint32_t serpentine_range(uint32_t slot, uint32_t x, uint32_t n) {
+  return (slot & 1u) ? (slot + 1u) * n - 1u - x : slot * n + x;
+}
 __device__ bool flow_roles(const FlowPlan& fp, WsHeader* h, uint32_t* reg, FlowRole& r) {
   const uint32_t b = blockIdx.x;
   const uint32_t nsm = sm_id_count();
@@ -803,7 +810,7 @@ __device__ bool flow_roles(const FlowPlan& fp, WsHeader* h, uint32_t* reg, FlowR
           v0 = fp.per_sm * (S - F) + sm;
         }
       } else {
-        v0 = slot * (S - F) + (sm - F);
+        v0 = serpentine_range(slot, sm - F, S - F);
       }
     } else if (r.below < F) {
       if (r.slot == 0) {
@@ -811,7 +818,7 @@ __device__ bool flow_roles(const FlowPlan& fp, WsHeader* h, uint32_t* reg, FlowR
         v0 = fp.per_sm * (S - F) + r.below;
       }
     } else {
-      v0 = r.slot * (S - F) + (r.below - F);
+      v0 = serpentine_range(r.slot, r.below - F, S - F);
     }
     r.face_v = fv;
     r.v0 = v0 < fp.ctas[0] ? v0 : kFlowNone;
