@@ -219,9 +219,12 @@ def test_single_instance_cluster_shapes(cuda, oracle_lib, shape):
 
 # Large single instances on the dataflow kernel with polled amplitudes (G pre-filled with a pending
 # pattern, every input of another CTA polled): the benchmark's 4 x 40 and 4 x 30 states, a cutoff-50
-# level 1 (2500 amplitudes per chunk), an extent of 1 on axis 1, D = 3, 6, a 2560-amplitude slab.
+# level 1 (2500 amplitudes per chunk), an extent of 1 on axis 1, D = 3, 5, 6, 7, 8, a 2560-amplitude
+# slab.  The halo loads of a chunk go out in batches of at most six: at D = 8 a level-0 amplitude has
+# seven possible halo terms (two batches), at 3 x 50^3 four amplitudes per lane pair give twelve.
 POLLED_SHAPES = [(6, 40, 40, 40), (30, 30, 30, 30), (3, 50, 50, 50), (5, 3, 1000), (2, 2, 2560),
-                (4, 8, 8, 8, 8, 6), (40, 1, 40, 40)]
+                (4, 8, 8, 8, 8, 6), (40, 1, 40, 40), (20, 12, 12, 12, 12), (40, 4, 4, 4, 4, 4, 4),
+                (12, 4, 4, 4, 4, 4, 4, 4)]
 
 
 @pytest.mark.parametrize("shape", POLLED_SHAPES)
