@@ -17,8 +17,9 @@
 //   and products are fused (DFMA), so results agree to rounding.
 //   Writes are contiguous (one chunk = one slab of the row-major tensor).
 //   One large instance on the whole GPU (fwd_flow_kernel) drops the per-chunk
-//   grid barrier: ranges of a chunk wait only for the ranges they read
-//   (progress words), the smallest levels run in one CTA's shared memory, and
+//   grid barrier: ranges of a chunk wait only for the amplitudes they read
+//   (polled in a G pre-filled with a pending bit pattern, or progress words),
+//   the smallest levels run in one CTA's shared memory, and
 //   latency-bound chains split each amplitude's real and imaginary parts over
 //   a lane pair (same terms, products rounded per part).
 // stable (core.py:127-213).  Every valid pivot is averaged, so an amplitude also
@@ -672,8 +673,9 @@ __global__ void __launch_bounds__(512) stable_grid_kernel(UniformSrc src, const 
 // (%smid, registered once with one grid barrier): with `exclusive`, the other
 // CTAs on a face CTA's SM stay idle so the face's latency-bound chain owns its
 // SM's FP64 pipes, the face CTAs take the last level-0 ranges (they finish the
-// face last), and consecutive level-0 ranges go to different SMs so the ranges
-// that start last (after the face) run one per SM.
+// face last) and run them one per SM, consecutive level-0 ranges go to
+// different SMs, and the two CTAs of a shared SM hold one early and one late
+// range (serpentine_range).
 struct FlowPlan {
   uint32_t ctas[MM_MAXD];
   uint32_t per[MM_MAXD];
