@@ -1097,6 +1097,37 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
     }
   }
   const uint32_t w_lo = fp.flag0[i] + (lo >= snext ? lo - snext : 0u) / per, w_hi = fp.flag0[i] + vr;
+  // Loop-invariant operands of the chunk loop held in registers instead of being re-read from shared
+  // memory and L1 every chunk: the axis strides and, with at most two amplitudes per lane pair, the
+  // coefficients A_ij sqrt(k_j) (D <= 4, where the registers are free without spills; the indices
+  // are in range of the level's coefficient row for every j, so the unused ones are loaded too).
+  constexpr bool kRegStrides = D <= 4, kRegCoefs = D <= 4 && A <= 2;
+  uint32_t str_r[kRegStrides ? D : 1];
+  double2 cf_r[kRegCoefs ? A : 1][kRegCoefs ? D : 1];
+  if constexpr (kRegStrides) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) str_r[j] = (uint32_t)g.strides[j];
+  }
+  if constexpr (kRegCoefs) {
+#pragma unroll
+    for (int u = 0; u < A; ++u)
+#pragma unroll
+      for (int j = 0; j < D; ++j) cf_r[u][j] = (j > i && k[u][j] > 0) ? crow[g.prefC[j] + k[u][j]] : cmk(0.0, 0.0);
+  }
+  auto stride = [&](int j) -> uint32_t {
+    if constexpr (kRegStrides) {
+      return str_r[j];
+    } else {
+      return (uint32_t)g.strides[j];
+    }
+  };
+  auto coef = [&](int u, int j) -> double2 {
+    if constexpr (kRegCoefs) {
+      return cf_r[u][j];
+    } else {
+      return crow[g.prefC[j] + k[u][j]];
+    }
+  };
   for (int m = 2; m < Ci; ++m) {
     const double2 cd = crow[g.prefC[i] + m];
     const double rsm = rs[m];
@@ -1113,9 +1144,9 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
       if (q < hi) {
 #pragma unroll
         for (int j = 1; j < D; ++j) {
-          const uint32_t sj = (uint32_t)g.strides[j];
+          const uint32_t sj = stride(j);
           if (j > i && k[u][j] > 0 && q - sj >= lo)
-            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], Sp[q - sj - lo], im, acc[u]);
+            acc[u] = part_fma(coef(u, j), Sp[q - sj - lo], im, acc[u]);
         }
       }
     }
@@ -1135,16 +1166,16 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
           hx[t] = hy[t] = 0ull;
           const int u = (t0 + t) / DM, j = 1 + (t0 + t) % DM;
           if (t0 + t >= T) continue;
-          const uint32_t q = lo + a0 + (uint32_t)u * pairs, sj = (uint32_t)g.strides[j];
+          const uint32_t q = lo + a0 + (uint32_t)u * pairs, sj = stride(j);
           if (q < hi && j > i && k[u][j] > 0 && q - sj < lo) ld_relaxed_v2u64(G + prev + (q - sj), hx[t], hy[t]);
         }
 #pragma unroll
         for (int t = 0; t < NB; ++t) {
           const int u = (t0 + t) / DM, j = 1 + (t0 + t) % DM;
           if (t0 + t >= T) continue;
-          const uint32_t q = lo + a0 + (uint32_t)u * pairs, sj = (uint32_t)g.strides[j];
+          const uint32_t q = lo + a0 + (uint32_t)u * pairs, sj = stride(j);
           if (q < hi && j > i && k[u][j] > 0 && q - sj < lo)
-            acc[u] = part_fma(crow[g.prefC[j] + k[u][j]],
+            acc[u] = part_fma(coef(u, j),
                               halo_wait(G + prev + (q - sj), hx[t], hy[t], h, fp.budget_ns, s_fail), im, acc[u]);
         }
       }
@@ -1156,9 +1187,9 @@ __device__ bool flow_level(const InstView& v, const double* __restrict__ rs, WsH
         if (!poll) {
 #pragma unroll
           for (int j = 1; j < D; ++j) {
-            const uint32_t sj = (uint32_t)g.strides[j];
+            const uint32_t sj = stride(j);
             if (j > i && k[u][j] > 0 && q - sj < lo)
-              acc[u] = part_fma(crow[g.prefC[j] + k[u][j]], __ldcg(G + prev + (q - sj)), im, acc[u]);
+              acc[u] = part_fma(coef(u, j), __ldcg(G + prev + (q - sj)), im, acc[u]);
           }
         }
         const double val = not_pending(rsm * acc[u]);
