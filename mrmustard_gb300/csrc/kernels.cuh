@@ -935,6 +935,9 @@ __device__ void small_level(const InstView& v, const double* __restrict__ rs, in
   const int32_t pci = g.prefC[i] - coff;
   double* Gd = reinterpret_cast<double*>(Gs);
   const bool one = si <= pairs;
+  uint32_t str[D];  // strides in registers: the barrier at each chunk's end would force them to be re-read
+#pragma unroll
+  for (int j = 0; j < D; ++j) str[j] = (uint32_t)g.strides[j];
   int32_t k1[D];
   double2 w1[D];
   decompose<D>(a0 < si ? a0 : 0u, i + 1, g, k1);
@@ -958,7 +961,7 @@ __device__ void small_level(const InstView& v, const double* __restrict__ rs, in
         if (m >= 2) acc = part_fma(cd, Gs[p - si], im, acc);
 #pragma unroll
         for (int j = 1; j < D; ++j)
-          if (j > i && k1[j] > 0) acc = part_fma(w1[j], Gs[p - (uint32_t)g.strides[j]], im, acc);
+          if (j > i && k1[j] > 0) acc = part_fma(w1[j], Gs[p - str[j]], im, acc);
         Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
       }
     } else {
@@ -971,7 +974,7 @@ __device__ void small_level(const InstView& v, const double* __restrict__ rs, in
 #pragma unroll
         for (int j = 1; j < D; ++j)
           if (j > i && k[j] > 0)
-            acc = part_fma(crow[g.prefC[j] - coff + k[j]], Gs[p - (uint32_t)g.strides[j]], im, acc);
+            acc = part_fma(crow[g.prefC[j] - coff + k[j]], Gs[p - str[j]], im, acc);
         Gd[2 * f + (im ? 1 : 0)] = rsm * acc;
       }
     }
@@ -1494,6 +1497,9 @@ __global__ void __launch_bounds__(256) fwd_cluster_kernel(UniformSrc src) {
     gpp[u] = 0.0;
     gp[u] = q < hi ? Sd[2 * (q - lo) + (im ? 1 : 0)] : 0.0;  // slab 0 (pushed by CTA 0)
   }
+  uint32_t str[D];  // strides in registers: the cluster barrier at each chunk's end would force them to be re-read
+#pragma unroll
+  for (int j = 0; j < D; ++j) str[j] = (uint32_t)g.strides[j];
   for (int m = 1; m < C0; ++m) {
     const double2 cd = cd0[m];
     const double rsm = rs0[m];
@@ -1510,7 +1516,7 @@ __global__ void __launch_bounds__(256) fwd_cluster_kernel(UniformSrc src) {
         for (int j = 1; j < D; ++j) {
           x[j] = cmk(0.0, 0.0);
           if (k[u][j] > 0) {
-            const uint32_t qn = q - (uint32_t)g.strides[j];
+            const uint32_t qn = q - str[j];
             x[j] = qn >= lo ? Sp[qn - lo] : Hp[lo - 1 - qn];
           }
         }
