@@ -307,15 +307,31 @@ __device__ __forceinline__ void fwd_chunk_scaled(const InstView& v, const Scaled
   const double2* G = v.G;
   const int64_t base = (int64_t)m * si;
   int64_t sj[D];
-  int32_t pj[D];
+  int32_t pj[D], shp[D];
 #pragma unroll
   for (int j = 0; j < D; ++j) {
     sj[j] = g.strides[j];
     pj[j] = g.prefC[j];
+    shp[j] = (int32_t)g.shape[j];
+  }
+  // k of the thread's first amplitude, then advanced by the digits of q_step (mixed-radix addition over
+  // axes i+1..D-1; q < strides[i] for every amplitude used, so the carry out of axis i+1 is dropped)
+  int32_t k[D], dk[D];
+  {
+    uint32_t q0 = q_begin + t < q_end ? q_begin + t : q_begin, st = q_step;
+#pragma unroll
+    for (int j = D - 1; j >= 0; --j) {
+      k[j] = dk[j] = 0;
+      if (j > i) {
+        const uint32_t c = (uint32_t)shp[j];
+        k[j] = (int32_t)(q0 % c);
+        q0 /= c;
+        dk[j] = (int32_t)(st % c);
+        st /= c;
+      }
+    }
   }
   for (uint32_t q = q_begin + t; q < q_end; q += q_step) {
-    int32_t k[D];
-    decompose<D>(q, i + 1, g, k);
     const int64_t f = base + q;
     const int64_t p = f - si;
     double2 acc = cmul(bi, ldGc<CG>(v, G + p, 4));
@@ -325,6 +341,15 @@ __device__ __forceinline__ void fwd_chunk_scaled(const InstView& v, const Scaled
       if (j > i && k[j] > 0) acc = cfma(row.c[pj[j] + k[j]], ldGc<CG>(v, G + p - sj[j], 4), acc);
     }
     stG(v, f, acc, 6);
+    int32_t carry = 0;
+#pragma unroll
+    for (int j = D - 1; j >= 0; --j) {
+      if (j > i) {
+        k[j] += dk[j] + carry;
+        carry = k[j] >= shp[j] ? 1 : 0;
+        if (carry) k[j] -= shp[j];
+      }
+    }
   }
 }
 
