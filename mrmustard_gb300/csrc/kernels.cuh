@@ -600,7 +600,7 @@ __device__ void stable_instance_team(const InstView& v, const double* rs, uint32
 // No CTA ever waits for another cluster, so the launch needs no co-residency
 // guarantee beyond the cluster's own.
 template <int DLO, int DHI>
-__global__ void __launch_bounds__(MM_BLOCK) fwd_ragged_team_kernel(RaggedSrc src, const double* __restrict__ rs,
+__global__ void __launch_bounds__(MM_BLOCK, DHI <= 4 ? 4 : 2) fwd_ragged_team_kernel(RaggedSrc src, const double* __restrict__ rs,
                                                                    int stable, const int32_t* __restrict__ big,
                                                                    int n_big, const int32_t* __restrict__ small,
                                                                    int n_small, WsHeader* h) {
