@@ -598,12 +598,13 @@ __device__ void stable_instance_team(const InstView& v, const double* rs, uint32
 // runs each on all its CTAs.  Phase 2: every CTA pulls the remaining instances
 // (largest first) one at a time from an atomic queue and runs each alone.
 // No CTA ever waits for another cluster, so the launch needs no co-residency
-// guarantee beyond the cluster's own.
+// guarantee beyond the cluster's own.  Four CTAs per SM up to D = 4 (64
+// registers; unbounded, the chunk loop's incremental multi-index takes 76 and
+// three CTAs per SM were measured slower), two above.
 template <int DLO, int DHI>
-__global__ void __launch_bounds__(MM_BLOCK, DHI <= 4 ? 4 : 2) fwd_ragged_team_kernel(RaggedSrc src, const double* __restrict__ rs,
-                                                                   int stable, const int32_t* __restrict__ big,
-                                                                   int n_big, const int32_t* __restrict__ small,
-                                                                   int n_small, WsHeader* h) {
+__global__ void __launch_bounds__(MM_BLOCK, DHI <= 4 ? 4 : 2)
+    fwd_ragged_team_kernel(RaggedSrc src, const double* __restrict__ rs, int stable, const int32_t* __restrict__ big,
+                           int n_big, const int32_t* __restrict__ small, int n_small, WsHeader* h) {
   MM_SHARED(InstView, sv);
   MM_SHARED(int, s_next);
   const uint32_t rank = cluster_rank(), nranks = cluster_size();
